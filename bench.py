@@ -1,0 +1,310 @@
+#!/usr/bin/env python
+"""Throughput of the plain 3D smoke step on GB300 (cell-steps/s).
+
+One step = one full timestep (force+attenuation, velocity advection, red-black
+SOR projection, scalar advection+reinjection) of a device-resident grid,
+replayed as a CUDA graph.  Default workload: plain256 (256^3, four seeded
+sphere sources, K=600, omega 1.9, 20 backtrace substeps).
+
+Prints one JSON line (rank 0).  --impl reference times the CPU path (the FP32
+oracle restatement of the reference's step, all host threads) instead.
+Multi-GPU: a single grid does not shard, so N ranks run N independent
+replicas ("replicas only"); value = all ranks' cell-steps / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import re
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Gcell-steps/s on 1 GB300: batched vs plain (rel err ≤1e-4); adjoint/fwd time ratio"
+UNIT = "Gcell-steps/s"
+SOR_BYTES_PER_CELL_ITER = 13      # read p, div (4+4), flags (1), write p (4)
+STEP_BYTES_FIXED = 133            # the non-SOR stages of the algorithmic model
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default="plain256")
+    ap.add_argument("--sor-depth", type=int, default=0, help="SOR iterations per fused pass (0 = default)")
+    ap.add_argument("--cpu-sample", default="plain128", help="grid of the bounded CPU sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic(name: str):
+    """DRAM bytes per launch of the SOR kernel from the committed ncu summary."""
+    f = ROOT / "profiles" / f"{name}.md"
+    if not f.exists():
+        return None
+    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", f.read_text())
+    return float(m.group(1)) if m else None
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in Path(self.path).read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for nme, val in zip(names, r[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nme)
+        loaded = [s for s in sm if mx and s > 0.5 * max(mx)] or sm
+        return {"sm_mhz": statistics.median(loaded) if loaded else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def cpu_sample_time(args, base_wl, steps: int = 1):
+    """Time `steps` steps of the FP32 oracle on the bounded CPU sample grid."""
+    import numpy as np
+
+    from oracle.binding import Oracle, num_threads
+    from zq_smokesimulation_gb300 import workloads as wl
+    w = wl.make(args.cpu_sample, K=base_wl.params.sor_iters, substeps=base_wl.params.substeps)
+    o = Oracle(np.float32)
+    st = o.state(w)
+    t0 = time.perf_counter()
+    rc, _ = o.step(w.W, w.H, w.D, st, w.occ, w.params, steps)
+    dt = time.perf_counter() - t0
+    if rc != 0:
+        raise RuntimeError(f"oracle step failed: {rc}")
+    return w.cells * steps / dt / 1e9, num_threads(), \
+        f"{steps} full step(s) of the same configuration at {w.W}^3 (K={w.params.sor_iters}), FP32 oracle"
+
+
+def run_reference(args):
+    """Reference arm: the CPU path of the step (FP32 oracle port), rank 0 only."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from zq_smokesimulation_gb300 import workloads as wl
+    base = wl.make(args.workload, K=None)
+    for _ in range(max(0, args.warmup)):
+        cpu_sample_time(args, base, 1)
+    vals = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        v, cores, sample = cpu_sample_time(args, base, 1)
+        vals.append(v)
+    wall = time.perf_counter() - t0
+    value = statistics.mean(vals)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * wall / max(1, args.steps),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": args.workload, "sample": args.cpu_sample},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    from zq_smokesimulation_gb300 import capi
+    from zq_smokesimulation_gb300 import workloads as wl
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    w = wl.make(args.workload)
+    K = w.params.sor_iters
+    g = capi.Grid(w.W, w.H, w.D)
+    g.set_params(w.params)
+    g.set_sor_config(args.sor_depth, False)
+    g.load_state(w.occ, w.u, w.v, w.w, w.T, w.rho)
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    cells = w.cells
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    g.step(max(3, args.warmup), sp)
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    g.step(args.steps, sp)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    barrier()
+    launches_per_step = g.launch_count()
+
+    # -- dominant kernel (temporally blocked SOR): per-launch duration, live --
+    depth = args.sor_depth if args.sor_depth > 0 else 2
+    passes = math.ceil(2 * K / (2 * depth))
+    reps = 3
+    p0 = w.params.copy()
+    p0.sor_iters = 0
+
+    def time_project(params):
+        g.set_params(params)
+        g.project(sp)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            g.project(sp)
+        b.record(stream)
+        b.synchronize()
+        return a.elapsed_time(b) / reps
+
+    t_K = time_project(w.params)
+    t_0 = time_project(p0)
+    g.set_params(w.params)
+    sor_ms_per_launch = max(1e-9, (t_K - t_0) / passes)
+    alg_bytes = SOR_BYTES_PER_CELL_ITER * depth * cells
+    peak, peak_kind = load_peaks()
+    achieved = alg_bytes / (sor_ms_per_launch * 1e-3) / 1e9
+    traffic = profile_traffic(f"k_sor_tb_{args.workload}")
+
+    # -- end to end through the C ABI with pinned host buffers --
+    e2e = None
+    if not args.no_e2e:
+        fields = [capi.FIELD_U, capi.FIELD_V, capi.FIELD_W, capi.FIELD_TEMPERATURE, capi.FIELD_DENSITY]
+        host = {}
+        for f in fields:
+            n = int(np.prod(capi.field_shape(f, w.W, w.H, w.D)))
+            host[f] = torch.empty(n, dtype=torch.float32, pin_memory=True)
+            g.download_into(f, host[f].data_ptr(), sp)
+        torch.cuda.synchronize()
+        nbytes = sum(host[f].numel() * 4 for f in fields)
+        e2e_steps = max(1, min(args.steps, 10))
+        barrier()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(e2e_steps):
+            for f in fields:
+                g.upload_from(f, host[f].data_ptr(), sp)
+            g.step(1, sp)
+            for f in fields:
+                g.download_into(f, host[f].data_ptr(), sp)
+        b.record(stream)
+        b.synchronize()
+        e2e_ms = a.elapsed_time(b)
+        if dist is not None:
+            t = torch.tensor([e2e_ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_ms = float(t.item())
+        e2e = {"value": world * cells * e2e_steps / (e2e_ms * 1e-3) / 1e9, "unit": UNIT,
+               "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+               "path": "zqs_grid_upload x5 (pinned host) + zqs_grid_step + zqs_grid_download x5"}
+    clocks = sampler.stop()
+
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * cells * args.steps / (ms * 1e-3) / 1e9
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, cores, sample = cpu_sample_time(args, w, 1)
+        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+
+    if rank == 0:
+        step_alg = (STEP_BYTES_FIXED + SOR_BYTES_PER_CELL_ITER * K) * cells
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": args.workload, "grid": [w.W, w.H, w.D], "sor_iters": K,
+                       "omega": round(float(w.params.omega), 6), "substeps": int(w.params.substeps),
+                       "advection": "inMAC_outMAC + MAC scalar", "sor_depth": depth, "graph": True,
+                       "l2": "working set %.2f GB > 129 MB L2, no flush" % (g.layout().field_elems * 4 * 21.25 / 1e9),
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "roofline": {"bound": "hbm", "kernel": "k_sor_tb", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                         "alg_bytes_per_launch": alg_bytes, "ms_per_launch": sor_ms_per_launch,
+                         "step_alg_gbs": step_alg / (ms / args.steps * 1e-3) / 1e9,
+                         "step_frac": step_alg / (ms / args.steps * 1e-3) / 1e9 / peak},
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches_per_step * args.steps, "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    g.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,204 @@
+/*
+ * zqs_capi.h -- C ABI of the GB300 smoke-step library (libzqs_gb300.so).
+ *
+ * Plain C: opaque handles, plain pointers and sizes, int status codes.  All
+ * array arguments use the reference's unpadded x-fastest layouts:
+ *   cell fields (occupancy, temperature, density, pressure):  W*H*D
+ *   u faces  (W+1)*H*D,   v faces  W*(H+1)*D,   w faces  W*H*(D+1)
+ * exactly as ZQ_SmokeGrid3D allocates them (ZQ_SmokeSimulation3D/ZQ_SmokeGrid3D.cpp:5-18).
+ * On the device the library keeps its own padded layout (see zqs_grid_layout).
+ *
+ * Every entry point returns ZQS_OK (0) or a positive zqs_status; the message of
+ * the last failure on the calling thread is available from zqs_last_error().
+ * A zqs_grid handle is not thread-safe: use one handle per host thread.
+ * Stream arguments are cudaStream_t passed as void*; NULL selects the handle's
+ * own non-blocking stream.
+ *
+ * The legacy entry points of the reference (Advect_Velocity, AddForce3D, ...)
+ * are declared in zqs_legacy.h and are thin shims over this API.
+ */
+#ifndef ZQS_CAPI_H
+#define ZQS_CAPI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define ZQS_API __attribute__((visibility("default")))
+#else
+#define ZQS_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ZQS_VERSION 1
+
+typedef enum zqs_status {
+    ZQS_OK = 0,
+    ZQS_EINVAL = 1,        /* bad argument: null pointer, size, enum value   */
+    ZQS_ENOMEM = 2,        /* device or pinned-host allocation failed         */
+    ZQS_EUNSUPPORTED = 3,  /* mode not implemented (returned, never silent)    */
+    ZQS_ETIMEOUT = 4,      /* a bounded device-side wait gave up              */
+    ZQS_ECUDA = 5,         /* CUDA runtime error (message has the CUDA text)  */
+    ZQS_ENOTREADY = 6      /* handle not configured (no params / occupancy)   */
+} zqs_status;
+
+/* Projection boundary handling (ZQ_SmokeSimulationUtils3D.cpp:2349-2440):
+ * OPEN   = cells outside the domain are Dirichlet p = 0 (TOTAL_OPEN_POISSON_SOR)
+ * CLOSED = outside is Neumann and the mean divergence over free cells is
+ *          removed first (TOTAL_CLOSED_POISSON_SOR).                          */
+typedef enum zqs_solver { ZQS_SOLVER_OPEN = 0, ZQS_SOLVER_CLOSED = 1 } zqs_solver;
+
+/* Numeric values are those of ZQ_CUDA_Advection3D.h:7-21 (the CUDA header,
+ * not the ZQ_SmokeSimulationPara3D enum). */
+typedef enum zqs_adv_vel {
+    ZQS_ADV_VEL_INREG_OUTREG = 0,
+    ZQS_ADV_VEL_INREG_OUTREG_BFECC = 1,
+    ZQS_ADV_VEL_INMAC_OUTMAC = 2,
+    ZQS_ADV_VEL_INMAC_OUTMAC_BFECC = 3,
+    ZQS_ADV_VEL_INREG_OUTMAC = 4,
+    ZQS_ADV_VEL_INREG_OUTMAC_BFECC = 5
+} zqs_adv_vel;
+
+typedef enum zqs_adv_sca {
+    ZQS_ADV_SCA_MAC = 0,
+    ZQS_ADV_SCA_MAC_BFECC = 1,
+    ZQS_ADV_SCA_REG = 2,
+    ZQS_ADV_SCA_REG_BFECC = 3
+} zqs_adv_sca;
+
+typedef enum zqs_source_shape {
+    ZQS_SOURCE_BOX = 0,     /* |i+.5-cx| <= hx && ... (ZQ_SmokeSimulationUtils3D.cpp:3869) */
+    ZQS_SOURCE_SPHERE = 1   /* (i+.5-cx)^2 + (j+.5-cy)^2 + (k+.5-cz)^2 <= hx^2            */
+} zqs_source_shape;
+
+#define ZQS_MAX_SOURCES 16
+
+/* A smoke source, in CELL units: cell (i,j,k) spans [i,i+1)x[j,j+1)x[k,k+1).
+ * The reference stores unit-cube coordinates and multiplies by W/H/D in float
+ * before use (ZQ_SmokeSimulationUtils3D.cpp:3853-3858); callers do that. */
+typedef struct zqs_source {
+    int32_t shape;
+    float cx, cy, cz;
+    float hx, hy, hz;       /* box half extents; sphere radius in hx */
+    float density;
+    float temperature;
+} zqs_source;
+
+/* Run parameters (a C mirror of the fields of ZQ_SmokeSimulationPara3D that
+ * the per-step path reads, ZQ_SmokeSimulationUtils3D.h:50-125). */
+typedef struct zqs_params {
+    float voxel_size;       /* h  (reference: 1/width, Utils3D:323)              */
+    float step_time;        /* dt (stepTime)                                     */
+    int32_t substeps;       /* backtrace substeps ("steps", reference default 20) */
+    float confine;          /* vorticity confinement eps (confineCoeff)          */
+    float buoyancy;         /* beta: f_y += beta*(T - Tamb)                      */
+    float gravity;          /* alpha: f_y -= alpha*rho  (0 reproduces reference)  */
+    float tamb;             /* ambient temperature                               */
+    float vel_atten;        /* per-step factors, e.g. exp(-dt*coeff) (Utils3D:2098) */
+    float temp_atten;
+    float dens_atten;
+    int32_t solver;         /* zqs_solver                                        */
+    int32_t sor_iters;      /* fixed red-black iteration count K (maxIter)       */
+    float omega;            /* over-relaxation; 1 reproduces the reference       */
+    int32_t adv_vel_mode;   /* zqs_adv_vel                                       */
+    int32_t adv_sca_mode;   /* zqs_adv_sca                                       */
+    int32_t backtrace_full; /* 0: reference rule (sample at the last point that
+                               passed the domain/occupancy test BEFORE the final
+                               move); 1: also test and use the final point       */
+    int32_t n_sources;
+    zqs_source sources[ZQS_MAX_SOURCES];
+} zqs_params;
+
+/* Fields addressable by upload/download. */
+typedef enum zqs_field {
+    ZQS_FIELD_U = 0,
+    ZQS_FIELD_V = 1,
+    ZQS_FIELD_W = 2,
+    ZQS_FIELD_TEMPERATURE = 3,
+    ZQS_FIELD_DENSITY = 4,
+    ZQS_FIELD_PRESSURE = 5,    /* last projection's pressure (download only)  */
+    ZQS_FIELD_OCCUPANCY = 6,   /* 1 byte per cell, nonzero = occupied         */
+    ZQS_FIELD_DIVERGENCE = 7   /* last projection's right-hand side (download) */
+} zqs_field;
+
+/* Diagnostics of the last projection; all reductions in FP64. */
+typedef struct zqs_stats {
+    double max_abs_div;        /* max |div u| over free cells after projection */
+    double residual_l2;        /* || div - L p ||_2 of the final pressure       */
+    double div_mean_removed;   /* closed solver: mean divergence removed        */
+    int64_t free_cells;
+} zqs_stats;
+
+/* Device layout of one grid: every field of a handle shares it. */
+typedef struct zqs_grid_layout {
+    int32_t W, H, D;
+    int32_t pitch_x;           /* floats per row  (>= W+1, multiple of 4)      */
+    int32_t rows;              /* rows per plane  (= H+1)                      */
+    int32_t planes;            /* data planes     (= D+1)                      */
+    int64_t plane_elems;       /* pitch_x * rows                               */
+    int64_t field_elems;       /* elements allocated per field incl. guards    */
+} zqs_grid_layout;
+
+typedef struct zqs_grid zqs_grid;
+
+ZQS_API int zqs_version(void);
+ZQS_API const char* zqs_last_error(void);
+
+/* Reference defaults of ZQ_SmokeSimulationPara3D (Utils3D:18-72) for a grid of
+ * width W: h=1/W, dt=0.01, substeps=20, buoyancy 1, confine 0, Tamb 10, all
+ * attenuation factors 1, open solver, K=100, omega 1, MAC advection modes, one
+ * box source.  */
+ZQS_API void zqs_params_default(zqs_params* p, int W, int H, int D);
+
+ZQS_API int zqs_grid_create(zqs_grid** out, int W, int H, int D);
+ZQS_API int zqs_grid_destroy(zqs_grid* g);
+ZQS_API int zqs_grid_get_layout(const zqs_grid* g, zqs_grid_layout* out);
+ZQS_API int zqs_grid_set_params(zqs_grid* g, const zqs_params* p);
+ZQS_API int zqs_grid_get_params(const zqs_grid* g, zqs_params* p);
+
+/* Copy a field in or out (reference layout).  *_on_device != 0 means the
+ * pointer is device memory.  Asynchronous on the stream; host buffers must
+ * stay valid until the stream is synchronised (pinned buffers overlap). */
+ZQS_API int zqs_grid_upload(zqs_grid* g, int field, const void* src, int src_on_device, void* stream);
+ZQS_API int zqs_grid_download(zqs_grid* g, int field, void* dst, int dst_on_device, void* stream);
+
+/* One full timestep = F, T, A, P, S, R in the order of
+ * ZQ_SmokeSimulation3D::UpdateOneFrame (ZQ_SmokeSimulation3D.cpp:156-243). */
+ZQS_API int zqs_grid_step(zqs_grid* g, int nsteps, void* stream);
+
+/* Enable/disable CUDA-graph replay of zqs_grid_step (default on). */
+ZQS_API int zqs_grid_use_graph(zqs_grid* g, int enable);
+
+/* Single stages, for drop-in use and per-stage parity. */
+ZQS_API int zqs_stage_add_force(zqs_grid* g, void* stream);
+ZQS_API int zqs_stage_attenuate(zqs_grid* g, void* stream);
+ZQS_API int zqs_stage_advect_velocity(zqs_grid* g, int mode, int is_open, void* stream);
+ZQS_API int zqs_stage_project(zqs_grid* g, void* stream);
+ZQS_API int zqs_stage_advect_scalar(zqs_grid* g, int mode, void* stream);
+ZQS_API int zqs_stage_reinject(zqs_grid* g, void* stream);
+
+/* Cell-centred velocity (u,v,w,0) per cell, W*H*D float4 (MAC_to_Regular4). */
+ZQS_API int zqs_grid_mac_to_regular4(zqs_grid* g, float* vel4, int dst_on_device, void* stream);
+
+/* FP64 diagnostics of the current velocity/pressure; synchronises the stream. */
+ZQS_API int zqs_grid_stats(zqs_grid* g, zqs_stats* out, void* stream);
+
+/* SOR kernel selection: temporal_depth = red-black iterations fused per HBM
+ * pass (0 = autotuned choice, 1 = one iteration per pass); split_colours != 0
+ * runs the plain one-colour-per-launch kernel (the self-check path). */
+ZQS_API int zqs_grid_set_sor_config(zqs_grid* g, int temporal_depth, int split_colours);
+
+/* Wait for all work queued on the stream (NULL: the handle's own stream). */
+ZQS_API int zqs_grid_synchronize(zqs_grid* g, void* stream);
+
+/* Kernel launches issued by the last zqs_grid_step call (for accounting). */
+ZQS_API int64_t zqs_grid_launch_count(const zqs_grid* g);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ZQS_CAPI_H */

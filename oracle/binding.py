@@ -1,0 +1,109 @@
+"""ctypes binding of the CPU oracle (oracle/_build/libzqs_oracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline / reference arm of bench.py, always as the checker.  The oracle
+restates the reference's per-timestep path (see zqs_oracle.cpp); parity of the
+reference itself is unpinned (no golden outputs exist in the reference).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+_libs: dict = {}
+
+
+def load():
+    if "lib" in _libs:
+        return _libs["lib"]
+    from . import build as _b  # type: ignore
+    path = _b.build()
+    lib = C.CDLL(str(path))
+    _libs["lib"] = lib
+    return lib
+
+
+def _p(a):
+    if a is None:
+        return None
+    assert a.flags["C_CONTIGUOUS"]
+    return C.c_void_p(a.ctypes.data)
+
+
+class Oracle:
+    """Oracle in FP32 (dtype=np.float32) or FP64 (np.float64)."""
+
+    def __init__(self, dtype=np.float32):
+        self.lib = load()
+        self.dtype = np.dtype(dtype)
+        self.sfx = "f32" if self.dtype == np.float32 else "f64"
+
+    def _f(self, name):
+        return getattr(self.lib, f"zqo_{name}_{self.sfx}")
+
+    def arr(self, a):
+        return np.ascontiguousarray(a, dtype=self.dtype)
+
+    def mac_to_regular4(self, W, H, D, u, v, w):
+        out = np.empty((D, H, W, 4), self.dtype)
+        self._f("mac_to_regular4")(W, H, D, _p(u), _p(v), _p(w), _p(out))
+        return out
+
+    def regular4_to_mac(self, W, H, D, vel4):
+        u = np.empty((D, H, W + 1), self.dtype)
+        v = np.empty((D, H + 1, W), self.dtype)
+        w = np.empty((D + 1, H, W), self.dtype)
+        self._f("regular4_to_mac")(W, H, D, _p(self.arr(vel4)), _p(u), _p(v), _p(w))
+        return u, v, w
+
+    def vorticity(self, W, H, D, u, v, w, h):
+        vort = np.empty((D, H, W, 3), self.dtype)
+        vs = np.empty((D, H, W), self.dtype)
+        self._f("vorticity")(W, H, D, _p(self.arr(u)), _p(self.arr(v)), _p(self.arr(w)),
+                             (C.c_float if self.sfx == "f32" else C.c_double)(h), _p(vort), _p(vs))
+        return vort, vs
+
+    def add_force(self, W, H, D, st, occ, params):
+        self._f("add_force")(W, H, D, _p(st["u"]), _p(st["v"]), _p(st["w"]), _p(occ), _p(st["T"]), _p(st["rho"]),
+                             C.byref(params))
+
+    def attenuate(self, W, H, D, st, occ, params):
+        self._f("attenuate")(W, H, D, _p(st["u"]), _p(st["v"]), _p(st["w"]), _p(st["T"]), _p(st["rho"]), _p(occ),
+                             C.byref(params))
+
+    def advect_velocity(self, W, H, D, st, occ, params, mode, is_open=True):
+        return self._f("advect_velocity")(W, H, D, _p(st["u"]), _p(st["v"]), _p(st["w"]), _p(occ),
+                                          C.byref(params), mode, 1 if is_open else 0)
+
+    def advect_scalar(self, W, H, D, st, occ, params, mode):
+        return self._f("advect_scalar")(W, H, D, _p(st["u"]), _p(st["v"]), _p(st["w"]), _p(occ), _p(st["T"]),
+                                        _p(st["rho"]), _p(st["T"]), _p(st["rho"]), C.byref(params), mode)
+
+    def project(self, W, H, D, st, occ, params, want=False):
+        from zq_smokesimulation_gb300 import capi
+        p = np.zeros((D, H, W), self.dtype)
+        div = np.zeros((D, H, W), self.dtype)
+        stats = capi.Stats()
+        self._f("project")(W, H, D, _p(st["u"]), _p(st["v"]), _p(st["w"]), _p(occ), C.byref(params), _p(p), _p(div),
+                           C.byref(stats))
+        return (p, div, stats) if want else stats
+
+    def reinject(self, W, H, D, st, params):
+        self._f("reinject")(W, H, D, _p(st["T"]), _p(st["rho"]), C.byref(params))
+
+    def step(self, W, H, D, st, occ, params, nsteps=1):
+        p = np.zeros((D, H, W), self.dtype)
+        rc = self._f("step")(W, H, D, _p(st["u"]), _p(st["v"]), _p(st["w"]), _p(st["T"]), _p(st["rho"]), _p(occ),
+                             C.byref(params), nsteps, _p(p))
+        return rc, p
+
+    def state(self, wl):
+        """Copy of a workload's state in this oracle's dtype."""
+        return {k: self.arr(getattr(wl, k)).copy() for k in ("u", "v", "w", "T", "rho")}
+
+
+def num_threads() -> int:
+    return int(load().zqo_num_threads())

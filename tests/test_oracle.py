@@ -1,0 +1,344 @@
+"""Known-answer tests of the CPU oracle (no GPU).
+
+The reference ships no tests or golden outputs, so the oracle is pinned by
+(1) analytic known answers, (2) small pure-Python restatements of the
+reference loops that the C++ oracle must match bit for bit, (3) FP32 vs FP64
+agreement, and (4) the committed golden fixtures under tests/golden/.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+from zq_smokesimulation_gb300 import capi
+from zq_smokesimulation_gb300 import workloads as wl
+
+
+def free_occ(W, H, D):
+    return np.zeros((D, H, W), np.uint8)
+
+
+def test_mac_to_regular_constant_and_linear(oracle64):
+    W, H, D = 6, 5, 4
+    i = np.arange(W + 1, dtype=np.float64)
+    u = np.broadcast_to(0.5 + 2.0 * i, (D, H, W + 1)).copy()
+    v = np.full((D, H + 1, W), 3.0)
+    w = np.full((D + 1, H, W), -1.25)
+    c4 = oracle64.mac_to_regular4(W, H, D, u, v, w)
+    assert np.all(c4[..., 1] == 3.0) and np.all(c4[..., 2] == -1.25) and np.all(c4[..., 3] == 0.0)
+    np.testing.assert_allclose(c4[..., 0], np.broadcast_to(0.5 + 2.0 * (np.arange(W) + 0.5), (D, H, W)))
+    u2, v2, w2 = oracle64.regular4_to_mac(W, H, D, c4)
+    # interior faces of a linear field come back exactly; domain faces copy the inner centre
+    np.testing.assert_allclose(u2[:, :, 1:W], u[:, :, 1:W], rtol=0, atol=1e-14)
+    np.testing.assert_allclose(u2[:, :, 0], c4[:, :, 0, 0])
+    np.testing.assert_allclose(u2[:, :, W], c4[:, :, W - 1, 0])
+    assert np.all(v2 == 3.0) and np.all(w2 == -1.25)
+
+
+@pytest.mark.parametrize("mode", [capi.ADV_VEL_INMAC_OUTMAC, capi.ADV_VEL_INREG_OUTMAC, capi.ADV_VEL_INREG_OUTREG])
+def test_advect_velocity_constant_field_invariant(oracle32, mode):
+    W, H, D = 7, 6, 5
+    p = wl.smoke_params(W, 1, substeps=5)
+    st = {"u": np.full((D, H, W + 1), 0.3, np.float32), "v": np.full((D, H + 1, W), -0.2, np.float32),
+          "w": np.full((D + 1, H, W), 0.1, np.float32)}
+    before = {k: v.copy() for k, v in st.items()}
+    assert oracle32.advect_velocity(W, H, D, st, free_occ(W, H, D), p, mode) == 0
+    for k in st:
+        assert np.array_equal(st[k], before[k]), k
+
+
+def test_advect_zero_velocity_is_identity(oracle32):
+    w = wl.small_case(8, 7, 6, vel_amp=0.0)
+    st = oracle32.state(w)
+    T0, R0 = st["T"].copy(), st["rho"].copy()
+    assert oracle32.advect_scalar(w.W, w.H, w.D, st, w.occ, w.params, capi.ADV_SCA_MAC) == 0
+    assert np.array_equal(st["T"], T0) and np.array_equal(st["rho"], R0)
+    st2 = oracle32.state(w)
+    u0 = st2["u"].copy()
+    assert oracle32.advect_velocity(w.W, w.H, w.D, st2, w.occ, w.params, capi.ADV_VEL_INMAC_OUTMAC) == 0
+    assert np.array_equal(st2["u"], u0)
+
+
+def _translation_case(substeps, full):
+    W, H, D = 16, 6, 6
+    p = wl.smoke_params(W, 1, substeps=substeps)
+    p.voxel_size = 1.0 / W
+    p.step_time = 2.0 * p.voxel_size   # with u = 1: (u*dt)/h = 2 cells in total
+    p.backtrace_full = 1 if full else 0
+    st = {"u": np.ones((D, H, W + 1), np.float32), "v": np.zeros((D, H + 1, W), np.float32),
+          "w": np.zeros((D + 1, H, W), np.float32)}
+    T = np.random.default_rng(3).random((D, H, W)).astype(np.float32)
+    st["T"], st["rho"] = T.copy(), T.copy()
+    return W, H, D, p, st, T
+
+
+def test_backtrace_reference_rule_uses_point_before_last_move(oracle32):
+    # substeps=2: the reference samples after 1 of the 2 moves -> a 1-cell shift
+    W, H, D, p, st, T = _translation_case(2, False)
+    oracle32.advect_scalar(W, H, D, st, free_occ(W, H, D), p, capi.ADV_SCA_MAC)
+    np.testing.assert_array_equal(st["T"][:, :, 4:W - 1], T[:, :, 3:W - 2])
+    # substeps=1: no move survives -> identity (the documented reference quirk)
+    W, H, D, p, st, T = _translation_case(1, False)
+    oracle32.advect_scalar(W, H, D, st, free_occ(W, H, D), p, capi.ADV_SCA_MAC)
+    np.testing.assert_array_equal(st["T"], T)
+
+
+def test_backtrace_full_rule_uses_final_point(oracle32):
+    W, H, D, p, st, T = _translation_case(1, True)
+    oracle32.advect_scalar(W, H, D, st, free_occ(W, H, D), p, capi.ADV_SCA_MAC)
+    np.testing.assert_array_equal(st["T"][:, :, 4:W - 1], T[:, :, 2:W - 3])
+
+
+def test_linear_field_interpolates_exactly(oracle64):
+    W, H, D = 12, 10, 8
+    p = wl.smoke_params(W, 1, substeps=3)
+    p.step_time = 0.37 * p.voxel_size
+    occ = free_occ(W, H, D)
+    k, j, i = np.meshgrid(np.arange(D), np.arange(H), np.arange(W), indexing="ij")
+    T = 0.25 + 0.5 * (i + 0.5) - 0.125 * (j + 0.5) + 0.0625 * (k + 0.5)
+    st = {"u": np.full((D, H, W + 1), 0.7), "v": np.full((D, H + 1, W), 0.4), "w": np.full((D + 1, H, W), -0.3),
+          "T": T.copy(), "rho": T.copy()}
+    oracle64.advect_scalar(W, H, D, st, occ, p, capi.ADV_SCA_MAC)
+    dt_sub = float(p.step_time) / 3.0                      # the params hold float32 values
+    shift = 2 * dt_sub / float(p.voxel_size) * np.array([0.7, 0.4, -0.3])   # 2 of 3 moves survive
+    exp = T - (0.5 * shift[0] - 0.125 * shift[1] + 0.0625 * shift[2])
+    sl = (slice(2, D - 2), slice(2, H - 2), slice(2, W - 2))
+    np.testing.assert_allclose(st["T"][sl], exp[sl], rtol=0, atol=1e-12)
+
+
+def test_vorticity_of_rigid_rotation(oracle64):
+    W = H = D = 9
+    h = 1.0 / W
+    Om = 0.75
+    # u_c = -Om*(y - yc), v_c = Om*(x - xc) (physical units), on faces
+    y_u = (np.arange(H) + 0.5) * h - 0.5
+    x_v = (np.arange(W) + 0.5) * h - 0.5
+    u = np.broadcast_to((-Om * y_u)[None, :, None], (D, H, W + 1)).copy()
+    v = np.broadcast_to((Om * x_v)[None, None, :], (D, H + 1, W)).copy()
+    w = np.zeros((D + 1, H, W))
+    vort, vs = oracle64.vorticity(W, H, D, u, v, w, h)
+    inner = (slice(1, D - 1), slice(1, H - 1), slice(1, W - 1))
+    np.testing.assert_allclose(vort[inner][..., 2], 2 * Om, rtol=1e-12)
+    np.testing.assert_allclose(vort[inner][..., 0], 0, atol=1e-12)
+    np.testing.assert_allclose(vs[inner], 2 * Om, rtol=1e-12)
+    assert np.all(vort[0] == 0) and np.all(vs[:, :, 0] == 0)   # boundary cells stay zero
+
+
+def _gradient_field(pstar, occ):
+    """Live-face gradient of pstar with p = 0 outside (open rule)."""
+    D, H, W = occ.shape
+    lu, lv, lw = wl.live_faces(occ)
+    pp = np.pad(pstar, 1)
+    u = (pp[1:-1, 1:-1, 1:] - pp[1:-1, 1:-1, :-1]) * lu
+    v = (pp[1:-1, 1:, 1:-1] - pp[1:-1, :-1, 1:-1]) * lv
+    w = (pp[1:, 1:-1, 1:-1] - pp[:-1, 1:-1, 1:-1]) * lw
+    return u, v, w
+
+
+def test_sor_recovers_manufactured_pressure(oracle64):
+    W, H, D = 10, 9, 8
+    occ = wl.walls_open_top(W, H, D)
+    wl.add_box(occ, 4, 5, 4, 5, 3, 4)
+    rng = np.random.default_rng(11)
+    pstar = rng.standard_normal((D, H, W)) * (occ == 0)
+    u, v, w = _gradient_field(pstar, occ)
+    p = wl.smoke_params(W, 3000, omega=1.8)
+    st = {"u": u.copy(), "v": v.copy(), "w": w.copy()}
+    pr, div, stats = oracle64.project(W, H, D, st, occ, p, want=True)
+    np.testing.assert_allclose(pr, pstar, atol=1e-9)
+    for k in ("u", "v", "w"):
+        assert np.abs(st[k]).max() < 1e-9
+    assert stats.max_abs_div < 1e-9 and stats.residual_l2 < 1e-9
+
+
+def test_closed_solver_removes_mean_divergence(oracle64):
+    w_ = wl.small_case(9, 8, 7, closed=True, K=4000, vel_amp=0.2)
+    st = oracle64.state(w_)
+    w_.params.omega = 1.7
+    pr, div, stats = oracle64.project(w_.W, w_.H, w_.D, st, w_.occ, w_.params, want=True)
+    u, v, w = st["u"], st["v"], st["w"]
+    d = (u[:, :, 1:] - u[:, :, :-1]) + (v[:, 1:, :] - v[:, :-1, :]) + (w[1:] - w[:-1])
+    free = w_.occ == 0
+    np.testing.assert_allclose(d[free], stats.div_mean_removed, atol=1e-9)
+    assert stats.residual_l2 < 1e-9
+
+
+def _py_sor(div, occ, K, omega, open_):
+    """Pure-Python red-black SOR on a tiny grid (same operation order)."""
+    D, H, W = occ.shape
+    p = np.zeros((D, H, W))
+    nb = [(-1, 0, 0), (1, 0, 0), (0, -1, 0), (0, 1, 0), (0, 0, -1), (0, 0, 1)]
+    for _ in range(K):
+        for colour in (0, 1):
+            for k in range(D):
+                for j in range(H):
+                    for i in range(W):
+                        if (i + j + k) % 2 != colour or occ[k, j, i]:
+                            continue
+                        s, cnt = 0.0, 0
+                        for di, dj, dk in nb:
+                            a, b, c = i + di, j + dj, k + dk
+                            if 0 <= a < W and 0 <= b < H and 0 <= c < D:
+                                if not occ[c, b, a]:
+                                    s = s + p[c, b, a]
+                                    cnt += 1
+                            elif open_:
+                                cnt += 1
+                        if cnt == 0:
+                            continue
+                        p[k, j, i] = (1.0 - omega) * p[k, j, i] + omega * ((s - div[k, j, i]) / cnt)
+    return p
+
+
+@pytest.mark.parametrize("open_,omega", [(True, 1.0), (True, 1.9), (False, 1.3)])
+def test_sor_matches_pure_python_restatement(oracle64, open_, omega):
+    W, H, D = 5, 4, 4
+    occ = np.zeros((D, H, W), np.uint8)
+    occ[1, 1, 2] = 1
+    occ[2, 3, 0] = 1
+    rng = np.random.default_rng(5)
+    st = {"u": rng.standard_normal((D, H, W + 1)), "v": rng.standard_normal((D, H + 1, W)),
+          "w": rng.standard_normal((D + 1, H, W))}
+    lu, lv, lw = wl.live_faces(occ)
+    for k_, m in zip(("u", "v", "w"), (lu, lv, lw)):
+        st[k_] = st[k_] * m
+    p = wl.smoke_params(W, 3, omega=omega, solver=capi.SOLVER_OPEN if open_ else capi.SOLVER_CLOSED)
+    pr, div, _ = oracle64.project(W, H, D, {k: v.copy() for k, v in st.items()}, occ, p, want=True)
+    u, v, w = st["u"], st["v"], st["w"]
+    d = ((((u[:, :, 1:] - u[:, :, :-1]) + v[:, 1:, :]) - v[:, :-1, :]) + w[1:]) - w[:-1]
+    d = d * (occ == 0)
+    if not open_:
+        # FP64 mean: per-plane sequential partial sums combined in plane order
+        total, n = 0.0, 0
+        for k in range(D):
+            part = 0.0
+            for j in range(H):
+                for i in range(W):
+                    if not occ[k, j, i]:
+                        part += d[k, j, i]
+                        n += 1
+            total += part
+        d = d - (total / n) * (occ == 0)
+    np.testing.assert_array_equal(div, d)
+    np.testing.assert_array_equal(pr, _py_sor(d, occ, 3, float(p.omega), open_))  # omega as stored (float32)
+
+
+def _py_backtrace_mac(u, v, w, occ, start, steps, dt, h):
+    D, H, W = occ.shape
+
+    def tri(f, g):
+        nz, ny, nx = f.shape
+        idx, ts = [], []
+        for gg, n in zip(g, (nx, ny, nz)):
+            gg = min(max(gg, -1.0), float(n))
+            fl = math.floor(gg)
+            ts.append(gg - fl)
+            idx.append((min(max(fl, 0), n - 1), min(max(fl + 1, 0), n - 1)))
+        (x0, x1), (y0, y1), (z0, z1) = idx
+        tx, ty, tz = ts
+        L = lambda a, b, t: a + t * (b - a)
+        c00 = L(f[z0, y0, x0], f[z0, y0, x1], tx)
+        c10 = L(f[z0, y1, x0], f[z0, y1, x1], tx)
+        c01 = L(f[z1, y0, x0], f[z1, y0, x1], tx)
+        c11 = L(f[z1, y1, x0], f[z1, y1, x1], tx)
+        return L(L(c00, c10, ty), L(c01, c11, ty), tz)
+
+    def vel(x, y, z):
+        return (tri(u, (x, y - 0.5, z - 0.5)), tri(v, (x - 0.5, y, z - 0.5)), tri(w, (x - 0.5, y - 0.5, z)))
+
+    x, y, z = start
+    vx, vy, vz = vel(x, y, z)
+    last = (x, y, z)
+    for _ in range(steps):
+        if not (0 <= x <= W and 0 <= y <= H and 0 <= z <= D):
+            break
+        if occ[min(max(int(math.floor(z)), 0), D - 1), min(max(int(math.floor(y)), 0), H - 1),
+               min(max(int(math.floor(x)), 0), W - 1)]:
+            break
+        last = (x, y, z)
+        x, y, z = x - (vx * dt) / h, y - (vy * dt) / h, z - (vz * dt) / h
+        vx, vy, vz = vel(x, y, z)
+    return last, tri
+
+
+def test_scalar_advection_matches_pure_python_restatement(oracle64):
+    w_ = wl.small_case(7, 6, 5, vel_amp=0.4, substeps=3)
+    st = {k: np.asarray(v, np.float64).copy() for k, v in w_.state().items()}
+    T0 = st["T"].copy()
+    oracle64.advect_scalar(w_.W, w_.H, w_.D, st, w_.occ, w_.params, capi.ADV_SCA_MAC)
+    dt = float(w_.params.step_time) / w_.params.substeps
+    h = float(np.float32(w_.params.voxel_size))
+    for (k, j, i) in [(0, 0, 0), (2, 3, 4), (4, 5, 6), (1, 2, 3), (3, 1, 5)]:
+        last, tri = _py_backtrace_mac(st["u"], st["v"], st["w"], w_.occ, (i + 0.5, j + 0.5, k + 0.5),
+                                      w_.params.substeps, dt, h)
+        exp = tri(T0, (last[0] - 0.5, last[1] - 0.5, last[2] - 0.5))
+        assert st["T"][k, j, i] == exp
+
+
+def test_fp32_and_fp64_oracles_agree_over_steps(oracle32, oracle64):
+    w_ = wl.small_case(12, 12, 10, K=30, substeps=4)
+    s32, s64 = oracle32.state(w_), oracle64.state(w_)
+    oracle32.step(w_.W, w_.H, w_.D, s32, w_.occ, w_.params, 5)
+    oracle64.step(w_.W, w_.H, w_.D, s64, w_.occ, w_.params, 5)
+    for k in ("u", "v", "w", "rho", "T"):
+        assert rel_l2(s32[k], s64[k]) < 1e-5, k
+
+
+def test_reinject_box_and_sphere(oracle32):
+    W, H, D = 10, 9, 8
+    p = wl.smoke_params(W, 1)
+    p.set_sources([wl.sphere(5.0, 3.0, 4.0, 2.2, 0.8, 0.6), wl.box(2.0, 6.0, 3.0, 1.0, 0.5, 1.5, 0.3, 0.2)])
+    st = {"T": np.zeros((D, H, W), np.float32), "rho": np.zeros((D, H, W), np.float32)}
+    oracle32.reinject(W, H, D, st, p)
+    k, j, i = np.meshgrid(np.arange(D), np.arange(H), np.arange(W), indexing="ij")
+    x, y, z = (i + np.float32(0.5)).astype(np.float32), (j + np.float32(0.5)).astype(np.float32), \
+        (k + np.float32(0.5)).astype(np.float32)
+    dx, dy, dz = x - np.float32(5), y - np.float32(3), z - np.float32(4)
+    sph = (dx * dx + dy * dy) + dz * dz <= np.float32(2.2) * np.float32(2.2)
+    bx = (np.abs(x - 2) <= 1.0) & (np.abs(y - 6) <= 0.5) & (np.abs(z - 3) <= 1.5)
+    exp_rho = np.where(bx, np.float32(0.3), np.where(sph, np.float32(0.8), 0)).astype(np.float32)
+    assert np.array_equal(st["rho"], exp_rho)
+    assert sph.sum() > 10 and bx.sum() > 0
+
+
+def test_force_only_buoyancy_without_confinement(oracle64):
+    W, H, D = 6, 7, 5
+    occ = wl.walls_open_top(W, H, D)
+    p = wl.smoke_params(W, 1)
+    p.confine = 0.0
+    rng = np.random.default_rng(2)
+    st = {"u": np.zeros((D, H, W + 1)), "v": np.zeros((D, H + 1, W)), "w": np.zeros((D + 1, H, W)),
+          "T": rng.random((D, H, W)), "rho": rng.random((D, H, W))}
+    oracle64.add_force(W, H, D, st, occ, p)
+    f = float(p.buoyancy) * (st["T"] - float(p.tamb)) - float(np.float32(p.gravity)) * st["rho"]
+    lu, lv, lw = wl.live_faces(occ)
+    dt = float(np.float32(p.step_time))
+    exp = np.zeros((D, H + 1, W))
+    exp[:, 1:H, :] = dt * 0.5 * (f[:, 1:, :] + f[:, :-1, :])
+    exp[:, H, :] = dt * f[:, H - 1, :]
+    exp[:, 0, :] = dt * f[:, 0, :]
+    np.testing.assert_allclose(st["v"], exp * lv, rtol=1e-12, atol=1e-15)
+    assert np.all(st["u"] == 0) and np.all(st["w"] == 0)
+
+
+def test_golden_fixtures(oracle32, oracle64):
+    import json
+    from pathlib import Path
+    gdir = Path(__file__).parent / "golden"
+    files = sorted(gdir.glob("*.npz"))
+    assert files, "no golden fixtures committed"
+    for f in files:
+        g = np.load(f)
+        meta = json.loads(str(g["meta"]))
+        w_ = wl.small_case(*meta["dims"], seed=meta["seed"], K=meta["K"], substeps=meta["substeps"],
+                           closed=meta["closed"], vel_mode=meta["vel_mode"], sca_mode=meta["sca_mode"])
+        for o, tag in ((oracle32, "f32"), (oracle64, "f64")):
+            st = o.state(w_)
+            o.step(w_.W, w_.H, w_.D, st, w_.occ, w_.params, meta["steps"])
+            for k in ("u", "v", "w", "T", "rho"):
+                ref = g[f"{tag}_{k}"]
+                if tag == "f32":
+                    assert np.array_equal(st[k], ref), (f.name, k)
+                else:
+                    np.testing.assert_allclose(st[k], ref, rtol=0, atol=1e-13, err_msg=f"{f.name} {k}")

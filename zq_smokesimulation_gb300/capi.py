@@ -1,0 +1,315 @@
+"""ctypes binding of libzqs_gb300.so (include/zqs_capi.h, include/zqs_legacy.h).
+
+The library is the product: this module only loads it and mirrors its C
+structs.  Loading fails loudly when the shared object is missing; there is no
+fallback implementation.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "lib" / "libzqs_gb300.so"
+
+ZQS_OK, ZQS_EINVAL, ZQS_ENOMEM, ZQS_EUNSUPPORTED, ZQS_ETIMEOUT, ZQS_ECUDA, ZQS_ENOTREADY = range(7)
+STATUS_NAMES = {0: "ZQS_OK", 1: "ZQS_EINVAL", 2: "ZQS_ENOMEM", 3: "ZQS_EUNSUPPORTED", 4: "ZQS_ETIMEOUT",
+                5: "ZQS_ECUDA", 6: "ZQS_ENOTREADY"}
+
+SOLVER_OPEN, SOLVER_CLOSED = 0, 1
+# ZQ_CUDA_Advection3D.h:7-21 numbering
+ADV_VEL_INREG_OUTREG, ADV_VEL_INREG_OUTREG_BFECC, ADV_VEL_INMAC_OUTMAC, ADV_VEL_INMAC_OUTMAC_BFECC, \
+    ADV_VEL_INREG_OUTMAC, ADV_VEL_INREG_OUTMAC_BFECC = range(6)
+ADV_SCA_MAC, ADV_SCA_MAC_BFECC, ADV_SCA_REG, ADV_SCA_REG_BFECC = range(4)
+SOURCE_BOX, SOURCE_SPHERE = 0, 1
+MAX_SOURCES = 16
+
+FIELD_U, FIELD_V, FIELD_W, FIELD_TEMPERATURE, FIELD_DENSITY, FIELD_PRESSURE, FIELD_OCCUPANCY, \
+    FIELD_DIVERGENCE = range(8)
+
+
+class Source(C.Structure):
+    _fields_ = [("shape", C.c_int32), ("cx", C.c_float), ("cy", C.c_float), ("cz", C.c_float),
+                ("hx", C.c_float), ("hy", C.c_float), ("hz", C.c_float), ("density", C.c_float),
+                ("temperature", C.c_float)]
+
+
+class Params(C.Structure):
+    _fields_ = [("voxel_size", C.c_float), ("step_time", C.c_float), ("substeps", C.c_int32),
+                ("confine", C.c_float), ("buoyancy", C.c_float), ("gravity", C.c_float), ("tamb", C.c_float),
+                ("vel_atten", C.c_float), ("temp_atten", C.c_float), ("dens_atten", C.c_float),
+                ("solver", C.c_int32), ("sor_iters", C.c_int32), ("omega", C.c_float),
+                ("adv_vel_mode", C.c_int32), ("adv_sca_mode", C.c_int32), ("backtrace_full", C.c_int32),
+                ("n_sources", C.c_int32), ("sources", Source * MAX_SOURCES)]
+
+    def copy(self) -> "Params":
+        p = Params()
+        C.memmove(C.byref(p), C.byref(self), C.sizeof(Params))
+        return p
+
+    def set_sources(self, sources):
+        if len(sources) > MAX_SOURCES:
+            raise ValueError("at most 16 sources")
+        self.n_sources = len(sources)
+        for i, s in enumerate(sources):
+            self.sources[i] = s
+
+
+class Stats(C.Structure):
+    _fields_ = [("max_abs_div", C.c_double), ("residual_l2", C.c_double), ("div_mean_removed", C.c_double),
+                ("free_cells", C.c_int64)]
+
+
+class Layout(C.Structure):
+    _fields_ = [("W", C.c_int32), ("H", C.c_int32), ("D", C.c_int32), ("pitch_x", C.c_int32),
+                ("rows", C.c_int32), ("planes", C.c_int32), ("plane_elems", C.c_int64),
+                ("field_elems", C.c_int64)]
+
+
+# Every symbol include/zqs_capi.h and include/zqs_legacy.h declare with C linkage.
+CAPI_SYMBOLS = [
+    "zqs_version", "zqs_last_error", "zqs_params_default", "zqs_grid_create", "zqs_grid_destroy",
+    "zqs_grid_get_layout", "zqs_grid_set_params", "zqs_grid_get_params", "zqs_grid_upload",
+    "zqs_grid_download", "zqs_grid_step", "zqs_grid_use_graph", "zqs_stage_add_force", "zqs_stage_attenuate",
+    "zqs_stage_advect_velocity", "zqs_stage_project", "zqs_stage_advect_scalar", "zqs_stage_reinject",
+    "zqs_grid_mac_to_regular4", "zqs_grid_stats", "zqs_grid_set_sor_config", "zqs_grid_synchronize",
+    "zqs_grid_launch_count",
+]
+LEGACY_C_SYMBOLS = ["ZQ_Cuda_Prepare_Advection", "Advect_Velocity", "Advect_Scalar", "AddForce3D",
+                    "Attenuation3D", "zqs_project_sor"]
+LEGACY_CXX_SYMBOLS = [
+    "_ZN20ZQ_CUDA_MACtoRegular18cu_MAC_to_Regular4EPKfS1_S1_P6float4iii",
+    "_ZN20ZQ_CUDA_MACtoRegular18cu_Regular4_to_MACEPK6float4PfS3_S3_iii",
+    "_ZN23ZQ_CUDA_PoissonSolver3D40SolveOpenPoissonRedBlackwithOccupy3D_MACEPfS0_S0_PKbiiii",
+    "_ZN23ZQ_CUDA_PoissonSolver3D42SolveClosedPoissonRedBlackwithOccupy3D_MACEPfS0_S0_PKbfiiii",
+    "_ZN23ZQ_CUDA_PoissonSolver3D21cu_MAC_to_Regular_velEPfS0_S0_PKfS2_S2_iii",
+]
+
+_lib = None
+
+
+class ZQSError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+def load(path: str | os.PathLike | None = None) -> C.CDLL:
+    """Load libzqs_gb300.so (build it with __graft_entry__.build())."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise FileNotFoundError(f"{p} is missing: build the CUDA library first (python -c 'import "
+                                f"__graft_entry__ as g; g.build()')")
+    lib = C.CDLL(str(p))
+    vp, i, f = C.c_void_p, C.c_int, C.c_float
+    lib.zqs_version.restype = i
+    lib.zqs_last_error.restype = C.c_char_p
+    lib.zqs_params_default.argtypes = [C.POINTER(Params), i, i, i]
+    lib.zqs_params_default.restype = None
+    lib.zqs_grid_create.argtypes = [C.POINTER(vp), i, i, i]
+    lib.zqs_grid_destroy.argtypes = [vp]
+    lib.zqs_grid_get_layout.argtypes = [vp, C.POINTER(Layout)]
+    lib.zqs_grid_set_params.argtypes = [vp, C.POINTER(Params)]
+    lib.zqs_grid_get_params.argtypes = [vp, C.POINTER(Params)]
+    lib.zqs_grid_upload.argtypes = [vp, i, vp, i, vp]
+    lib.zqs_grid_download.argtypes = [vp, i, vp, i, vp]
+    lib.zqs_grid_step.argtypes = [vp, i, vp]
+    lib.zqs_grid_use_graph.argtypes = [vp, i]
+    lib.zqs_stage_add_force.argtypes = [vp, vp]
+    lib.zqs_stage_attenuate.argtypes = [vp, vp]
+    lib.zqs_stage_advect_velocity.argtypes = [vp, i, i, vp]
+    lib.zqs_stage_project.argtypes = [vp, vp]
+    lib.zqs_stage_advect_scalar.argtypes = [vp, i, vp]
+    lib.zqs_stage_reinject.argtypes = [vp, vp]
+    lib.zqs_grid_mac_to_regular4.argtypes = [vp, vp, i, vp]
+    lib.zqs_grid_stats.argtypes = [vp, C.POINTER(Stats), vp]
+    lib.zqs_grid_set_sor_config.argtypes = [vp, i, i]
+    lib.zqs_grid_launch_count.argtypes = [vp]
+    lib.zqs_grid_launch_count.restype = C.c_int64
+    lib.zqs_grid_synchronize.argtypes = [vp, vp]
+    # legacy shims
+    lib.ZQ_Cuda_Prepare_Advection.argtypes = [C.c_uint, C.c_uint, C.c_uint, f, C.c_uint, f]
+    lib.ZQ_Cuda_Prepare_Advection.restype = None
+    lib.Advect_Velocity.argtypes = [vp, vp, vp, vp, C.c_bool, i]
+    lib.Advect_Velocity.restype = f
+    lib.Advect_Scalar.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, i]
+    lib.Advect_Scalar.restype = f
+    lib.AddForce3D.argtypes = [vp, vp, vp, vp, vp, f, f, f, f, f, i, i, i, i]
+    lib.AddForce3D.restype = f
+    lib.Attenuation3D.argtypes = [vp, vp, vp, vp, vp, vp, f, f, f, i, i, i]
+    lib.Attenuation3D.restype = f
+    lib.zqs_project_sor.argtypes = [vp, vp, vp, vp, i, i, i, i, i, f]
+    lib.zqs_project_sor.restype = i
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def last_error() -> str:
+    return load().zqs_last_error().decode(errors="replace")
+
+
+def check(rc: int, what: str = "") -> None:
+    if rc != ZQS_OK:
+        raise ZQSError(rc, f"{what}: {last_error()}")
+
+
+def default_params(W: int, H: int, D: int) -> Params:
+    p = Params()
+    load().zqs_params_default(C.byref(p), W, H, D)
+    return p
+
+
+def ptr(a: np.ndarray) -> int:
+    if not a.flags["C_CONTIGUOUS"]:
+        raise ValueError("array must be C-contiguous")
+    return a.ctypes.data
+
+
+def field_shape(field: int, W: int, H: int, D: int) -> tuple[int, int, int]:
+    """numpy shape (z, y, x) of a field in the reference layout."""
+    if field == FIELD_U:
+        return (D, H, W + 1)
+    if field == FIELD_V:
+        return (D, H + 1, W)
+    if field == FIELD_W:
+        return (D + 1, H, W)
+    return (D, H, W)
+
+
+class Grid:
+    """One device-resident smoke grid (a zqs_grid handle)."""
+
+    def __init__(self, W: int, H: int, D: int):
+        self.lib = load()
+        self.W, self.H, self.D = W, H, D
+        h = C.c_void_p()
+        check(self.lib.zqs_grid_create(C.byref(h), W, H, D), "zqs_grid_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            self.lib.zqs_grid_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- configuration ---------------------------------------------------------------
+    def set_params(self, p: Params):
+        check(self.lib.zqs_grid_set_params(self.h, C.byref(p)), "zqs_grid_set_params")
+
+    def params(self) -> Params:
+        p = Params()
+        check(self.lib.zqs_grid_get_params(self.h, C.byref(p)), "zqs_grid_get_params")
+        return p
+
+    def layout(self) -> Layout:
+        L = Layout()
+        check(self.lib.zqs_grid_get_layout(self.h, C.byref(L)), "zqs_grid_get_layout")
+        return L
+
+    def set_sor_config(self, temporal_depth: int = 0, split: bool = False):
+        check(self.lib.zqs_grid_set_sor_config(self.h, temporal_depth, 1 if split else 0), "set_sor_config")
+
+    def use_graph(self, enable: bool):
+        check(self.lib.zqs_grid_use_graph(self.h, 1 if enable else 0), "use_graph")
+
+    # -- data -------------------------------------------------------------------------
+    def upload(self, field: int, arr: np.ndarray, stream: int | None = None):
+        dt = np.uint8 if field == FIELD_OCCUPANCY else np.float32
+        shape = field_shape(field, self.W, self.H, self.D)
+        a = np.ascontiguousarray(arr, dtype=dt)
+        if a.size != int(np.prod(shape)):
+            raise ValueError(f"field {field}: expected {shape}, got {arr.shape}")
+        check(self.lib.zqs_grid_upload(self.h, field, C.c_void_p(ptr(a)), 0, C.c_void_p(stream or 0)),
+              "zqs_grid_upload")
+        self._keep = a  # pageable source must outlive the async copy until the next sync
+        self.sync(stream)
+
+    def upload_device(self, field: int, dev_ptr: int, stream: int | None = None):
+        check(self.lib.zqs_grid_upload(self.h, field, C.c_void_p(dev_ptr), 1, C.c_void_p(stream or 0)),
+              "zqs_grid_upload(device)")
+
+    def download(self, field: int, stream: int | None = None) -> np.ndarray:
+        dt = np.uint8 if field == FIELD_OCCUPANCY else np.float32
+        out = np.empty(field_shape(field, self.W, self.H, self.D), dtype=dt)
+        check(self.lib.zqs_grid_download(self.h, field, C.c_void_p(ptr(out)), 0, C.c_void_p(stream or 0)),
+              "zqs_grid_download")
+        self.sync(stream)
+        return out
+
+    def download_into(self, field: int, host_ptr: int, stream: int | None = None):
+        check(self.lib.zqs_grid_download(self.h, field, C.c_void_p(host_ptr), 0, C.c_void_p(stream or 0)),
+              "zqs_grid_download")
+
+    def upload_from(self, field: int, host_ptr: int, stream: int | None = None):
+        check(self.lib.zqs_grid_upload(self.h, field, C.c_void_p(host_ptr), 0, C.c_void_p(stream or 0)),
+              "zqs_grid_upload")
+
+    def sync(self, stream: int | None = None):
+        check(self.lib.zqs_grid_synchronize(self.h, C.c_void_p(stream or 0)), "zqs_grid_synchronize")
+
+    def load_state(self, occ, u, v, w, T, rho):
+        self.upload(FIELD_OCCUPANCY, occ)
+        self.upload(FIELD_U, u)
+        self.upload(FIELD_V, v)
+        self.upload(FIELD_W, w)
+        self.upload(FIELD_TEMPERATURE, T)
+        self.upload(FIELD_DENSITY, rho)
+
+    def state(self) -> dict:
+        return {"u": self.download(FIELD_U), "v": self.download(FIELD_V), "w": self.download(FIELD_W),
+                "T": self.download(FIELD_TEMPERATURE), "rho": self.download(FIELD_DENSITY)}
+
+    # -- compute ----------------------------------------------------------------------
+    def step(self, n: int = 1, stream: int | None = None):
+        check(self.lib.zqs_grid_step(self.h, n, C.c_void_p(stream or 0)), "zqs_grid_step")
+
+    def add_force(self, stream=None):
+        check(self.lib.zqs_stage_add_force(self.h, C.c_void_p(stream or 0)), "add_force")
+
+    def attenuate(self, stream=None):
+        check(self.lib.zqs_stage_attenuate(self.h, C.c_void_p(stream or 0)), "attenuate")
+
+    def advect_velocity(self, mode: int, is_open: bool = True, stream=None):
+        check(self.lib.zqs_stage_advect_velocity(self.h, mode, 1 if is_open else 0, C.c_void_p(stream or 0)),
+              "advect_velocity")
+
+    def project(self, stream=None):
+        check(self.lib.zqs_stage_project(self.h, C.c_void_p(stream or 0)), "project")
+
+    def advect_scalar(self, mode: int, stream=None):
+        check(self.lib.zqs_stage_advect_scalar(self.h, mode, C.c_void_p(stream or 0)), "advect_scalar")
+
+    def reinject(self, stream=None):
+        check(self.lib.zqs_stage_reinject(self.h, C.c_void_p(stream or 0)), "reinject")
+
+    def mac_to_regular4(self) -> np.ndarray:
+        out = np.empty((self.D, self.H, self.W, 4), dtype=np.float32)
+        check(self.lib.zqs_grid_mac_to_regular4(self.h, C.c_void_p(ptr(out)), 0, None), "mac_to_regular4")
+        self.sync()
+        return out
+
+    def stats(self) -> Stats:
+        st = Stats()
+        check(self.lib.zqs_grid_stats(self.h, C.byref(st), None), "zqs_grid_stats")
+        return st
+
+    def launch_count(self) -> int:
+        return int(self.lib.zqs_grid_launch_count(self.h))

@@ -1,0 +1,653 @@
+// Host implementation of the handle-based C ABI (include/zqs_capi.h).
+//
+// A zqs_grid owns one device allocation holding every field in the padded
+// layout (zqs_internal.h), its own non-blocking stream, the per-step CUDA
+// graphs and the parameters.  The step replays a captured graph: one graph per
+// (velocity buffer, scalar buffer) parity, rebuilt when parameters or the SOR
+// configuration change.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <utility>
+
+#include "zqs_internal.h"
+
+namespace zqs {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+int cuda_fail(cudaError_t e, const char* what) {
+    set_error(std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")");
+    return e == cudaErrorMemoryAllocation ? ZQS_ENOMEM : ZQS_ECUDA;
+}
+
+static bool is_pow2(float h) {
+    if (!(h > 0.0f) || !std::isfinite(h)) return false;
+    int e;
+    float m = std::frexp(h, &e);
+    return m == 0.5f;
+}
+
+int make_kparams(const zqs_params& p, KParams& kp) {
+    kp.h = p.voxel_size;
+    kp.dt = p.step_time;
+    kp.dt_sub = (float)p.step_time / (float)p.substeps;  // Utils3D:2155
+    kp.inv_h = is_pow2(p.voxel_size) ? 1.0f / p.voxel_size : 0.0f;
+    kp.substeps = p.substeps;
+    kp.full = p.backtrace_full ? 1 : 0;
+    kp.cc = p.confine * p.voxel_size;
+    kp.twoh = 2.0f * p.voxel_size;
+    kp.beta = p.buoyancy;
+    kp.alpha = p.gravity;
+    kp.tamb = p.tamb;
+    kp.vel_atten = p.vel_atten;
+    kp.temp_atten = p.temp_atten;
+    kp.dens_atten = p.dens_atten;
+    kp.omega = p.omega;
+    kp.om1 = 1.0f - p.omega;
+    kp.solver = p.solver;
+    kp.mean_override = 0;
+    kp.mean_value = 0.0f;
+    return ZQS_OK;
+}
+
+int validate_params(const zqs_params& p) {
+    if (!(p.voxel_size > 0.0f) || !std::isfinite(p.voxel_size)) {
+        set_error("voxel_size must be a positive finite number");
+        return ZQS_EINVAL;
+    }
+    if (!std::isfinite(p.step_time)) {
+        set_error("step_time must be finite");
+        return ZQS_EINVAL;
+    }
+    if (p.substeps < 1) {
+        set_error("substeps must be >= 1");
+        return ZQS_EINVAL;
+    }
+    if (p.sor_iters < 0) {
+        set_error("sor_iters must be >= 0");
+        return ZQS_EINVAL;
+    }
+    if (p.solver != ZQS_SOLVER_OPEN && p.solver != ZQS_SOLVER_CLOSED) {
+        set_error("solver must be ZQS_SOLVER_OPEN or ZQS_SOLVER_CLOSED");
+        return ZQS_EINVAL;
+    }
+    if (p.adv_vel_mode < 0 || p.adv_vel_mode > 5 || p.adv_sca_mode < 0 || p.adv_sca_mode > 3) {
+        set_error("advection mode out of range");
+        return ZQS_EINVAL;
+    }
+    if (p.n_sources < 0 || p.n_sources > ZQS_MAX_SOURCES) {
+        set_error("n_sources must be in [0, 16]");
+        return ZQS_EINVAL;
+    }
+    for (int s = 0; s < p.n_sources; s++)
+        if (p.sources[s].shape != ZQS_SOURCE_BOX && p.sources[s].shape != ZQS_SOURCE_SPHERE) {
+            set_error("source shape must be ZQS_SOURCE_BOX or ZQS_SOURCE_SPHERE");
+            return ZQS_EINVAL;
+        }
+    return ZQS_OK;
+}
+
+}  // namespace zqs
+
+using namespace zqs;
+
+struct zqs_grid {
+    DevGrid g{};
+    void* base = nullptr;
+    uint8_t* occ_dense = nullptr;
+    cudaStream_t own = nullptr;
+    zqs_params params{};
+    bool has_params = false;
+    bool has_occ = false;
+    KParams kp{};
+    SourceList src{};
+    SorConfig sor{2, 0};
+    float* p_last = nullptr;
+    bool use_graph = true;
+    cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};
+    int vel_par = 0, sca_par = 0;   // which buffer of each ping-pong pair is current
+    long long step_launches = 0;
+    long long graph_launches[4] = {0, 0, 0, 0};
+    float* graph_p_last[4] = {nullptr, nullptr, nullptr, nullptr};
+
+    cudaStream_t pick(void* s) const { return s ? (cudaStream_t)s : own; }
+
+    void drop_graphs() {
+        for (int q = 0; q < 4; q++) {
+            if (graph[q]) cudaGraphExecDestroy(graph[q]);
+            graph[q] = nullptr;
+        }
+    }
+    void swap_velocity() {
+        std::swap(g.u, g.u2);
+        std::swap(g.v, g.v2);
+        std::swap(g.w, g.w2);
+        vel_par ^= 1;
+    }
+    void swap_scalars() {
+        std::swap(g.T, g.T2);
+        std::swap(g.rho, g.rho2);
+        sca_par ^= 1;
+    }
+    int ready() const {
+        if (!has_params) {
+            set_error("grid has no parameters (call zqs_grid_set_params)");
+            return ZQS_ENOTREADY;
+        }
+        if (!has_occ) {
+            set_error("grid has no occupancy (upload ZQS_FIELD_OCCUPANCY)");
+            return ZQS_ENOTREADY;
+        }
+        return ZQS_OK;
+    }
+    // The launches of one step, issued on stream s (captured or direct).
+    int issue_step(cudaStream_t s, LaunchCounter& lc) {
+        int rc = launch_force(g, kp, true, s, lc);
+        if (rc) return rc;
+        rc = launch_advect_velocity(g, kp, params.adv_vel_mode, true, s, lc);
+        if (rc) return rc;
+        swap_velocity();
+        rc = launch_project(g, kp, params.sor_iters, sor, s, lc, &p_last);
+        if (rc) return rc;
+        rc = launch_advect_scalar(g, kp, params.adv_sca_mode, true, &src, s, lc);
+        if (rc) return rc;
+        swap_scalars();
+        return ZQS_OK;
+    }
+};
+
+namespace zqs {
+// Internal hooks for the legacy shims (same library).
+DevGrid& grid_dev(zqs_grid* g) { return g->g; }
+KParams& grid_kparams(zqs_grid* g) { return g->kp; }
+cudaStream_t grid_stream(zqs_grid* g) { return g->own; }
+void grid_swap_velocity(zqs_grid* g) { g->swap_velocity(); }
+void grid_swap_scalars(zqs_grid* g) { g->swap_scalars(); }
+float*& grid_p_last(zqs_grid* g) { return g->p_last; }
+SorConfig& grid_sor(zqs_grid* g) { return g->sor; }
+}  // namespace zqs
+
+namespace {
+
+Layout make_layout(int W, int H, int D) {
+    Layout L;
+    L.W = W;
+    L.H = H;
+    L.D = D;
+    L.px = ((W + 1) + 3) / 4 * 4;
+    L.py = H + 1;
+    L.pz = D + 1;
+    L.plane = (long long)L.px * L.py;
+    L.elems = L.plane * (L.pz + 2);
+    return L;
+}
+
+// (rows, row elements, planes) of a field in the reference layout.
+bool field_shape(const Layout& L, int field, int& nx, int& ny, int& nz, size_t& esize) {
+    nx = L.W;
+    ny = L.H;
+    nz = L.D;
+    esize = 4;
+    switch (field) {
+        case ZQS_FIELD_U: nx = L.W + 1; return true;
+        case ZQS_FIELD_V: ny = L.H + 1; return true;
+        case ZQS_FIELD_W: nz = L.D + 1; return true;
+        case ZQS_FIELD_TEMPERATURE:
+        case ZQS_FIELD_DENSITY:
+        case ZQS_FIELD_PRESSURE:
+        case ZQS_FIELD_DIVERGENCE: return true;
+        case ZQS_FIELD_OCCUPANCY: esize = 1; return true;
+        default: return false;
+    }
+}
+
+float* field_ptr(zqs_grid* g, int field) {
+    switch (field) {
+        case ZQS_FIELD_U: return g->g.u;
+        case ZQS_FIELD_V: return g->g.v;
+        case ZQS_FIELD_W: return g->g.w;
+        case ZQS_FIELD_TEMPERATURE: return g->g.T;
+        case ZQS_FIELD_DENSITY: return g->g.rho;
+        case ZQS_FIELD_PRESSURE: return g->p_last ? g->p_last : g->g.p;
+        case ZQS_FIELD_DIVERGENCE: return g->g.div;
+        default: return nullptr;
+    }
+}
+
+int copy3d(void* dst, size_t dpitch, size_t dysize, const void* src, size_t spitch, size_t sysize, size_t rowbytes,
+           size_t rows, size_t planes, cudaMemcpyKind kind, cudaStream_t s) {
+    cudaMemcpy3DParms m;
+    memset(&m, 0, sizeof(m));
+    m.srcPtr = make_cudaPitchedPtr(const_cast<void*>(src), spitch, rowbytes, sysize);
+    m.dstPtr = make_cudaPitchedPtr(dst, dpitch, rowbytes, dysize);
+    m.extent = make_cudaExtent(rowbytes, rows, planes);
+    m.kind = kind;
+    ZQS_CUDA_TRY(cudaMemcpy3DAsync(&m, s));
+    return ZQS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+ZQS_API int zqs_version(void) { return ZQS_VERSION; }
+
+ZQS_API const char* zqs_last_error(void) { return zqs::g_last_error.c_str(); }
+
+ZQS_API void zqs_params_default(zqs_params* p, int W, int H, int D) {
+    if (!p) return;
+    memset(p, 0, sizeof(*p));
+    p->voxel_size = (float)(1.0 / (double)W);  // Utils3D:323
+    p->step_time = 0.01f;
+    p->substeps = 20;
+    p->confine = 0.0f;
+    p->buoyancy = 1.0f;
+    p->gravity = 0.0f;
+    p->tamb = 10.0f;
+    p->vel_atten = 1.0f;
+    p->temp_atten = 1.0f;
+    p->dens_atten = 1.0f;
+    p->solver = ZQS_SOLVER_OPEN;
+    p->sor_iters = 100;
+    p->omega = 1.0f;
+    p->adv_vel_mode = ZQS_ADV_VEL_INMAC_OUTMAC;
+    p->adv_sca_mode = ZQS_ADV_SCA_MAC;
+    p->backtrace_full = 0;
+    p->n_sources = 1;
+    zqs_source& s = p->sources[0];  // Utils3D:31-40, unit coordinates times W/H/D in float
+    s.shape = ZQS_SOURCE_BOX;
+    s.cx = 0.5f * (float)W;
+    s.cy = 0.1f * (float)H;
+    s.cz = 0.5f * (float)D;
+    s.hx = 0.1f * (float)W;
+    s.hy = 0.05f * (float)H;
+    s.hz = 0.1f * (float)D;
+    s.density = 1.0f;
+    s.temperature = 10.0f * 20.0f;
+}
+
+ZQS_API int zqs_grid_create(zqs_grid** out, int W, int H, int D) {
+    if (!out) {
+        set_error("zqs_grid_create: out is NULL");
+        return ZQS_EINVAL;
+    }
+    *out = nullptr;
+    if (W < 2 || H < 2 || D < 2) {
+        set_error("zqs_grid_create: every dimension must be >= 2");
+        return ZQS_EINVAL;
+    }
+    Layout L = make_layout(W, H, D);
+    if (L.elems >= (1LL << 31) - 1) {
+        set_error("zqs_grid_create: grid too large for 32-bit indexing");
+        return ZQS_EINVAL;
+    }
+    zqs_grid* g = new zqs_grid();
+    g->g.L = L;
+    // 13 float fields + 2 float4 fields + flags + FP64 scratch
+    const size_t fbytes = (size_t)L.elems * 4;
+    const size_t nflt = 13;
+    const long long nblocks = (long long)((W + 31) / 32) * ((H + 7) / 8) * D;
+    g->g.red_len = 3 * nblocks + 16;
+    size_t total = nflt * fbytes + 2 * (size_t)L.elems * 16 + (((size_t)L.elems + 255) / 256) * 256 +
+                   (size_t)g->g.red_len * 8 + 256;
+    cudaError_t e = cudaMalloc(&g->base, total);
+    if (e != cudaSuccess) {
+        delete g;
+        return cuda_fail(e, "zqs_grid_create: cudaMalloc");
+    }
+    e = cudaMalloc(&g->occ_dense, (size_t)W * H * D);
+    if (e != cudaSuccess) {
+        cudaFree(g->base);
+        delete g;
+        return cuda_fail(e, "zqs_grid_create: cudaMalloc(occupancy)");
+    }
+    e = cudaStreamCreateWithFlags(&g->own, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        cudaFree(g->occ_dense);
+        cudaFree(g->base);
+        delete g;
+        return cuda_fail(e, "zqs_grid_create: cudaStreamCreate");
+    }
+    e = cudaMemsetAsync(g->base, 0, total, g->own);
+    if (e == cudaSuccess) e = cudaMemsetAsync(g->occ_dense, 0, (size_t)W * H * D, g->own);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->own);
+    if (e != cudaSuccess) {
+        int rc = cuda_fail(e, "zqs_grid_create: clear");
+        cudaStreamDestroy(g->own);
+        cudaFree(g->occ_dense);
+        cudaFree(g->base);
+        delete g;
+        return rc;
+    }
+    int prc = sor_prepare();
+    if (prc) {
+        cudaStreamDestroy(g->own);
+        cudaFree(g->occ_dense);
+        cudaFree(g->base);
+        delete g;
+        return prc;
+    }
+    char* b = (char*)g->base;
+    auto take_f = [&](void) -> float* {
+        float* p = (float*)b + L.plane;  // skip the leading guard plane
+        b += fbytes;
+        return p;
+    };
+    g->g.u = take_f();
+    g->g.v = take_f();
+    g->g.w = take_f();
+    g->g.u2 = take_f();
+    g->g.v2 = take_f();
+    g->g.w2 = take_f();
+    g->g.T = take_f();
+    g->g.rho = take_f();
+    g->g.T2 = take_f();
+    g->g.rho2 = take_f();
+    g->g.p = take_f();
+    g->g.p2 = take_f();
+    g->g.div = take_f();
+    g->g.t4a = (float4*)b + L.plane;
+    b += (size_t)L.elems * 16;
+    g->g.t4b = (float4*)b + L.plane;
+    b += (size_t)L.elems * 16;
+    g->g.flags = (uint8_t*)b + L.plane;
+    b += (((size_t)L.elems + 255) / 256) * 256;
+    g->g.red = (double*)b;
+    *out = g;
+    return ZQS_OK;
+}
+
+ZQS_API int zqs_grid_destroy(zqs_grid* g) {
+    if (!g) return ZQS_OK;
+    g->drop_graphs();
+    if (g->own) cudaStreamSynchronize(g->own);
+    cudaStreamDestroy(g->own);
+    cudaFree(g->occ_dense);
+    cudaFree(g->base);
+    delete g;
+    return ZQS_OK;
+}
+
+ZQS_API int zqs_grid_get_layout(const zqs_grid* g, zqs_grid_layout* out) {
+    if (!g || !out) {
+        set_error("zqs_grid_get_layout: NULL argument");
+        return ZQS_EINVAL;
+    }
+    const Layout& L = g->g.L;
+    out->W = L.W;
+    out->H = L.H;
+    out->D = L.D;
+    out->pitch_x = L.px;
+    out->rows = L.py;
+    out->planes = L.pz;
+    out->plane_elems = L.plane;
+    out->field_elems = L.elems;
+    return ZQS_OK;
+}
+
+ZQS_API int zqs_grid_set_params(zqs_grid* g, const zqs_params* p) {
+    if (!g || !p) {
+        set_error("zqs_grid_set_params: NULL argument");
+        return ZQS_EINVAL;
+    }
+    int rc = validate_params(*p);
+    if (rc) return rc;
+    bool solver_changed = !g->has_params || g->params.solver != p->solver;
+    g->params = *p;
+    make_kparams(*p, g->kp);
+    g->src.n = p->n_sources;
+    for (int s = 0; s < p->n_sources; s++) g->src.s[s] = p->sources[s];
+    g->has_params = true;
+    g->drop_graphs();
+    if (solver_changed && g->has_occ) {
+        LaunchCounter lc;
+        rc = launch_build_flags(g->g, g->occ_dense, p->solver, g->own, lc);
+        if (rc) return rc;
+        ZQS_CUDA_TRY(cudaStreamSynchronize(g->own));
+    }
+    return ZQS_OK;
+}
+
+ZQS_API int zqs_grid_get_params(const zqs_grid* g, zqs_params* p) {
+    if (!g || !p) {
+        set_error("zqs_grid_get_params: NULL argument");
+        return ZQS_EINVAL;
+    }
+    if (!g->has_params) {
+        set_error("zqs_grid_get_params: no parameters set");
+        return ZQS_ENOTREADY;
+    }
+    *p = g->params;
+    return ZQS_OK;
+}
+
+ZQS_API int zqs_grid_upload(zqs_grid* g, int field, const void* src, int src_on_device, void* stream) {
+    if (!g || !src) {
+        set_error("zqs_grid_upload: NULL argument");
+        return ZQS_EINVAL;
+    }
+    const Layout& L = g->g.L;
+    cudaStream_t s = g->pick(stream);
+    int nx, ny, nz;
+    size_t es;
+    if (!field_shape(L, field, nx, ny, nz, es) || field == ZQS_FIELD_PRESSURE || field == ZQS_FIELD_DIVERGENCE) {
+        set_error("zqs_grid_upload: field cannot be uploaded");
+        return ZQS_EINVAL;
+    }
+    cudaMemcpyKind kind = src_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    if (field == ZQS_FIELD_OCCUPANCY) {
+        ZQS_CUDA_TRY(cudaMemcpyAsync(g->occ_dense, src, (size_t)L.W * L.H * L.D, kind, s));
+        g->has_occ = true;
+        LaunchCounter lc;
+        int rc = launch_build_flags(g->g, g->occ_dense, g->has_params ? g->params.solver : ZQS_SOLVER_OPEN, s, lc);
+        if (rc) return rc;
+        g->drop_graphs();
+        return ZQS_OK;
+    }
+    float* dst = field_ptr(g, field);
+    return copy3d(dst, (size_t)L.px * 4, (size_t)L.py, src, (size_t)nx * 4, (size_t)ny, (size_t)nx * 4, ny, nz, kind,
+                  s);
+}
+
+ZQS_API int zqs_grid_download(zqs_grid* g, int field, void* dst, int dst_on_device, void* stream) {
+    if (!g || !dst) {
+        set_error("zqs_grid_download: NULL argument");
+        return ZQS_EINVAL;
+    }
+    const Layout& L = g->g.L;
+    cudaStream_t s = g->pick(stream);
+    int nx, ny, nz;
+    size_t es;
+    if (!field_shape(L, field, nx, ny, nz, es)) {
+        set_error("zqs_grid_download: unknown field");
+        return ZQS_EINVAL;
+    }
+    cudaMemcpyKind kind = dst_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    if (field == ZQS_FIELD_OCCUPANCY) {
+        ZQS_CUDA_TRY(cudaMemcpyAsync(dst, g->occ_dense, (size_t)L.W * L.H * L.D, kind, s));
+        return ZQS_OK;
+    }
+    const float* src = field_ptr(g, field);
+    return copy3d(dst, (size_t)nx * 4, (size_t)ny, src, (size_t)L.px * 4, (size_t)L.py, (size_t)nx * 4, ny, nz, kind,
+                  s);
+}
+
+ZQS_API int zqs_grid_use_graph(zqs_grid* g, int enable) {
+    if (!g) {
+        set_error("zqs_grid_use_graph: NULL grid");
+        return ZQS_EINVAL;
+    }
+    g->use_graph = enable != 0;
+    if (!g->use_graph) g->drop_graphs();
+    return ZQS_OK;
+}
+
+ZQS_API int zqs_grid_set_sor_config(zqs_grid* g, int temporal_depth, int split_colours) {
+    if (!g || temporal_depth < 0 || temporal_depth > 4) {
+        set_error("zqs_grid_set_sor_config: temporal_depth must be in [0, 4]");
+        return ZQS_EINVAL;
+    }
+    g->sor.temporal_depth = temporal_depth == 0 ? 2 : temporal_depth;
+    g->sor.split = split_colours ? 1 : 0;
+    g->drop_graphs();
+    return ZQS_OK;
+}
+
+ZQS_API int zqs_grid_step(zqs_grid* g, int nsteps, void* stream) {
+    if (!g || nsteps < 0) {
+        set_error("zqs_grid_step: bad arguments");
+        return ZQS_EINVAL;
+    }
+    int rc = g->ready();
+    if (rc) return rc;
+    cudaStream_t s = g->pick(stream);
+    for (int n = 0; n < nsteps; n++) {
+        if (!g->use_graph) {
+            LaunchCounter lc;
+            rc = g->issue_step(s, lc);
+            if (rc) return rc;
+            g->step_launches = lc.n;
+            continue;
+        }
+        const int key = g->vel_par * 2 + g->sca_par;
+        if (!g->graph[key]) {
+            // Capture on the grid's own stream: the launches read the current
+            // buffer pointers, so capturing advances the parities; restore them.
+            const int vp = g->vel_par, sp = g->sca_par;
+            DevGrid saved = g->g;
+            float* saved_p = g->p_last;
+            LaunchCounter lc;
+            ZQS_CUDA_TRY(cudaStreamBeginCapture(g->own, cudaStreamCaptureModeThreadLocal));
+            rc = g->issue_step(g->own, lc);
+            cudaGraph_t graph = nullptr;
+            cudaError_t e = cudaStreamEndCapture(g->own, &graph);
+            float* captured_p = g->p_last;  // p and p2 never move, so this holds for every replay
+            g->g = saved;
+            g->vel_par = vp;
+            g->sca_par = sp;
+            g->p_last = saved_p;
+            if (rc) {
+                if (graph) cudaGraphDestroy(graph);
+                return rc;
+            }
+            if (e != cudaSuccess) return cuda_fail(e, "zqs_grid_step: cudaStreamEndCapture");
+            e = cudaGraphInstantiate(&g->graph[key], graph, 0);
+            cudaGraphDestroy(graph);
+            if (e != cudaSuccess) {
+                g->graph[key] = nullptr;
+                return cuda_fail(e, "zqs_grid_step: cudaGraphInstantiate");
+            }
+            g->graph_launches[key] = lc.n;
+            g->graph_p_last[key] = captured_p;
+        }
+        ZQS_CUDA_TRY(cudaGraphLaunch(g->graph[key], s));
+        // advance the buffer roles exactly as issue_step does
+        g->swap_velocity();
+        g->swap_scalars();
+        g->p_last = g->graph_p_last[key];
+        g->step_launches = g->graph_launches[key];
+    }
+    return ZQS_OK;
+}
+
+ZQS_API int zqs_stage_add_force(zqs_grid* g, void* stream) {
+    if (!g) return set_error("NULL grid"), ZQS_EINVAL;
+    int rc = g->ready();
+    if (rc) return rc;
+    LaunchCounter lc;
+    return launch_force(g->g, g->kp, false, g->pick(stream), lc);
+}
+
+ZQS_API int zqs_stage_attenuate(zqs_grid* g, void* stream) {
+    if (!g) return set_error("NULL grid"), ZQS_EINVAL;
+    int rc = g->ready();
+    if (rc) return rc;
+    LaunchCounter lc;
+    return launch_attenuate(g->g, g->kp, g->pick(stream), lc);
+}
+
+ZQS_API int zqs_stage_advect_velocity(zqs_grid* g, int mode, int is_open, void* stream) {
+    if (!g) return set_error("NULL grid"), ZQS_EINVAL;
+    int rc = g->ready();
+    if (rc) return rc;
+    LaunchCounter lc;
+    rc = launch_advect_velocity(g->g, g->kp, mode, is_open != 0, g->pick(stream), lc);
+    if (rc) return rc;
+    g->swap_velocity();
+    return ZQS_OK;
+}
+
+ZQS_API int zqs_stage_project(zqs_grid* g, void* stream) {
+    if (!g) return set_error("NULL grid"), ZQS_EINVAL;
+    int rc = g->ready();
+    if (rc) return rc;
+    LaunchCounter lc;
+    return launch_project(g->g, g->kp, g->params.sor_iters, g->sor, g->pick(stream), lc, &g->p_last);
+}
+
+ZQS_API int zqs_stage_advect_scalar(zqs_grid* g, int mode, void* stream) {
+    if (!g) return set_error("NULL grid"), ZQS_EINVAL;
+    int rc = g->ready();
+    if (rc) return rc;
+    LaunchCounter lc;
+    rc = launch_advect_scalar(g->g, g->kp, mode, false, nullptr, g->pick(stream), lc);
+    if (rc) return rc;
+    g->swap_scalars();
+    return ZQS_OK;
+}
+
+ZQS_API int zqs_stage_reinject(zqs_grid* g, void* stream) {
+    if (!g) return set_error("NULL grid"), ZQS_EINVAL;
+    int rc = g->ready();
+    if (rc) return rc;
+    LaunchCounter lc;
+    return launch_reinject(g->g, g->src, g->pick(stream), lc);
+}
+
+ZQS_API int zqs_grid_mac_to_regular4(zqs_grid* g, float* vel4, int dst_on_device, void* stream) {
+    if (!g || !vel4) return set_error("NULL argument"), ZQS_EINVAL;
+    const Layout& L = g->g.L;
+    cudaStream_t s = g->pick(stream);
+    LaunchCounter lc;
+    size_t bytes = (size_t)L.W * L.H * L.D * 16;
+    if (dst_on_device) return launch_reg4_dense(g->g, nullptr, (float4*)vel4, s, lc);
+    // stage through t4b's storage (large enough: elems*16 >= W*H*D*16)
+    int rc = launch_reg4_dense(g->g, nullptr, g->g.t4b, s, lc);
+    if (rc) return rc;
+    ZQS_CUDA_TRY(cudaMemcpyAsync(vel4, g->g.t4b, bytes, cudaMemcpyDeviceToHost, s));
+    return ZQS_OK;
+}
+
+ZQS_API int zqs_grid_stats(zqs_grid* g, zqs_stats* out, void* stream) {
+    if (!g || !out) return set_error("NULL argument"), ZQS_EINVAL;
+    int rc = g->ready();
+    if (rc) return rc;
+    cudaStream_t s = g->pick(stream);
+    memset(out, 0, sizeof(*out));
+    const float* p = g->p_last ? g->p_last : g->g.p;
+    rc = launch_stats(g->g, g->kp, p, out, s);
+    if (rc) return rc;
+    if (g->params.solver == ZQS_SOLVER_CLOSED) {
+        double m[2];
+        ZQS_CUDA_TRY(cudaMemcpy(m, g->g.red + g->g.red_len - 2, sizeof(m), cudaMemcpyDeviceToHost));
+        out->div_mean_removed = (double)(float)m[0];
+    }
+    return ZQS_OK;
+}
+
+ZQS_API int zqs_grid_synchronize(zqs_grid* g, void* stream) {
+    if (!g) return set_error("NULL grid"), ZQS_EINVAL;
+    ZQS_CUDA_TRY(cudaStreamSynchronize(g->pick(stream)));
+    return ZQS_OK;
+}
+
+ZQS_API int64_t zqs_grid_launch_count(const zqs_grid* g) { return g ? g->step_launches : 0; }
+
+}  // extern "C"

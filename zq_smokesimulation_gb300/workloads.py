@@ -1,0 +1,244 @@
+"""Seeded synthetic workloads of the smoke step (no dataset is involved).
+
+Inputs are drawn on the host with SplitMix64 so every consumer (the CUDA
+library, the CPU oracle, the C++ host API) sees identical bytes:
+    x_n = splitmix64(seed + n*0x9E3779B97F4A7C15), u_n = (x_n >> 40) * 2^-24 in [0,1)
+and U(a,b) = a + (b-a)*u_n in float32.
+
+Named configurations (cell units, y is up, gravity along -y):
+  plain64        64^3, closed walls + open top, sphere source r=6 at (32,8,32),
+                 alpha .1 beta .5 eps .2 Tamb 0, attenuation .99, dt .5,
+                 omega 1.9, K=200, noise +-1e-3 on live faces (seed 0)
+  plain128_obs   128^3, as plain64 plus the box obstacle [48,80]x[56,72]x[48,80]
+                 (inclusive), source r=10 at (64,12,64), K=400
+  plain256       256^3, walls as plain64, four seeded sphere sources: r~U[8,16],
+                 centre x,z~U[r+1, N-r-1], y~U[1, 0.1N], density and temperature
+                 ~U[.5,1]; K=600
+  plain512       the same at 512^3
+"Walls closed except an open top" = the open (Dirichlet p=0 outside) solver
+with an occupied layer at x=0, x=W-1, y=0, z=0, z=D-1: outside the top face the
+pressure is 0, every other side is a solid wall, like ZQ_InitFineGrid3D's
+closed layers (ZQ_SmokeSimulationUtils3D.cpp:1535-1584) minus the top one.
+Backtrace substeps: 20, the reference default (ZQ_SmokeSimulationUtils3D.cpp:46).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import capi
+
+_GOLD = np.uint64(0x9E3779B97F4A7C15)
+_M1 = np.uint64(0xBF58476D1CE4E5B9)
+_M2 = np.uint64(0x94D049BB133111EB)
+
+
+def splitmix64(seed: int, n: int, offset: int = 0) -> np.ndarray:
+    idx = np.arange(offset + 1, offset + n + 1, dtype=np.uint64)
+    with np.errstate(over="ignore"):
+        z = np.uint64(seed) + idx * _GOLD
+        z = (z ^ (z >> np.uint64(30))) * _M1
+        z = (z ^ (z >> np.uint64(27))) * _M2
+        z = z ^ (z >> np.uint64(31))
+    return z
+
+
+def uniform01(seed: int, n: int, offset: int = 0) -> np.ndarray:
+    z = splitmix64(seed, n, offset)
+    return (z >> np.uint64(40)).astype(np.float32) * np.float32(2.0 ** -24)
+
+
+def uniform(seed: int, n: int, lo: float, hi: float, offset: int = 0) -> np.ndarray:
+    u = uniform01(seed, n, offset)
+    lo32, span = np.float32(lo), np.float32(hi) - np.float32(lo)
+    return lo32 + span * u
+
+
+# ---------------------------------------------------------------------------
+# occupancy
+# ---------------------------------------------------------------------------
+
+def walls_open_top(W: int, H: int, D: int) -> np.ndarray:
+    occ = np.zeros((D, H, W), dtype=np.uint8)
+    occ[:, :, 0] = 1
+    occ[:, :, W - 1] = 1
+    occ[:, 0, :] = 1
+    occ[0, :, :] = 1
+    occ[D - 1, :, :] = 1
+    return occ
+
+
+def walls_closed(W: int, H: int, D: int) -> np.ndarray:
+    """ZQ_InitFineGrid3D's six border layers for the closed solvers (Utils3D:1535-1584)."""
+    occ = walls_open_top(W, H, D)
+    occ[:, H - 1, :] = 1
+    return occ
+
+
+def add_box(occ: np.ndarray, x0: int, x1: int, y0: int, y1: int, z0: int, z1: int) -> np.ndarray:
+    """Occupy cells [x0,x1]x[y0,y1]x[z0,z1] (inclusive bounds)."""
+    occ[z0:z1 + 1, y0:y1 + 1, x0:x1 + 1] = 1
+    return occ
+
+
+def live_faces(occ: np.ndarray):
+    """Open-rule live masks of the u, v, w faces (ZQ_CUDA_Advection3D.cu:471-575)."""
+    free = occ == 0
+    D, H, W = occ.shape
+    lu = np.zeros((D, H, W + 1), bool)
+    lu[:, :, 1:W] = free[:, :, 1:] & free[:, :, :-1]
+    lu[:, :, 0] = free[:, :, 0]
+    lu[:, :, W] = free[:, :, W - 1]
+    lv = np.zeros((D, H + 1, W), bool)
+    lv[:, 1:H, :] = free[:, 1:, :] & free[:, :-1, :]
+    lv[:, 0, :] = free[:, 0, :]
+    lv[:, H, :] = free[:, H - 1, :]
+    lw = np.zeros((D + 1, H, W), bool)
+    lw[1:D] = free[1:] & free[:-1]
+    lw[0] = free[0]
+    lw[D] = free[D - 1]
+    return lu, lv, lw
+
+
+# ---------------------------------------------------------------------------
+# configurations
+# ---------------------------------------------------------------------------
+
+@dataclass
+class Workload:
+    name: str
+    W: int
+    H: int
+    D: int
+    params: capi.Params
+    occ: np.ndarray
+    u: np.ndarray
+    v: np.ndarray
+    w: np.ndarray
+    T: np.ndarray
+    rho: np.ndarray
+    steps: int
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def cells(self) -> int:
+        return self.W * self.H * self.D
+
+    def state(self) -> dict:
+        return {"u": self.u.copy(), "v": self.v.copy(), "w": self.w.copy(), "T": self.T.copy(),
+                "rho": self.rho.copy()}
+
+
+def sphere(cx, cy, cz, r, density=1.0, temperature=1.0) -> capi.Source:
+    s = capi.Source()
+    s.shape = capi.SOURCE_SPHERE
+    s.cx, s.cy, s.cz = cx, cy, cz
+    s.hx = s.hy = s.hz = r
+    s.density, s.temperature = density, temperature
+    return s
+
+
+def box(cx, cy, cz, hx, hy, hz, density=1.0, temperature=1.0) -> capi.Source:
+    s = capi.Source()
+    s.shape = capi.SOURCE_BOX
+    s.cx, s.cy, s.cz = cx, cy, cz
+    s.hx, s.hy, s.hz = hx, hy, hz
+    s.density, s.temperature = density, temperature
+    return s
+
+
+def smoke_params(W: int, K: int, *, substeps: int = 20, omega: float = 1.9, vel_mode=capi.ADV_VEL_INMAC_OUTMAC,
+                 sca_mode=capi.ADV_SCA_MAC, solver=capi.SOLVER_OPEN) -> capi.Params:
+    p = capi.Params()
+    p.voxel_size = np.float32(1.0 / W)
+    p.step_time = 0.5
+    p.substeps = substeps
+    p.confine = 0.2
+    p.buoyancy = 0.5
+    p.gravity = 0.1
+    p.tamb = 0.0
+    p.vel_atten = p.temp_atten = p.dens_atten = 0.99
+    p.solver = solver
+    p.sor_iters = K
+    p.omega = omega
+    p.adv_vel_mode = vel_mode
+    p.adv_sca_mode = sca_mode
+    p.backtrace_full = 0
+    p.n_sources = 0
+    return p
+
+
+def initial_velocity(occ: np.ndarray, seed: int, amp: float = 1e-3):
+    D, H, W = occ.shape
+    lu, lv, lw = live_faces(occ)
+    nu, nv, nw = lu.size, lv.size, lw.size
+    u = uniform(seed, nu, -amp, amp, 0).reshape(lu.shape)
+    v = uniform(seed, nv, -amp, amp, nu).reshape(lv.shape)
+    w = uniform(seed, nw, -amp, amp, nu + nv).reshape(lw.shape)
+    u[~lu] = 0
+    v[~lv] = 0
+    w[~lw] = 0
+    return u, v, w
+
+
+def make(name: str, *, K: int | None = None, substeps: int = 20, steps: int | None = None, seed: int = 0,
+         vel_mode=capi.ADV_VEL_INMAC_OUTMAC, sca_mode=capi.ADV_SCA_MAC, omega: float = 1.9) -> Workload:
+    if name in ("plain64", "plain128_obs"):
+        N = 64 if name == "plain64" else 128
+        occ = walls_open_top(N, N, N)
+        if name == "plain64":
+            src = [sphere(32.0, 8.0, 32.0, 6.0)]
+            Kd, steps_d = 200, 100
+        else:
+            add_box(occ, 48, 80, 56, 72, 48, 80)
+            src = [sphere(64.0, 12.0, 64.0, 10.0)]
+            Kd, steps_d = 400, 500
+    elif name.startswith("plain") and name[5:].isdigit():
+        N = int(name[5:])
+        occ = walls_open_top(N, N, N)
+        rs = uniform(seed + 1000, 4, 8.0, 16.0)
+        src = []
+        for q in range(4):
+            r = float(rs[q])
+            u3 = uniform01(seed + 2000 + q, 5)
+            cx = float(np.float32(r + 1) + np.float32(N - 2 * r - 2) * u3[0])
+            cz = float(np.float32(r + 1) + np.float32(N - 2 * r - 2) * u3[1])
+            cy = float(np.float32(1.0) + np.float32(0.1 * N - 1.0) * u3[2])
+            den = float(np.float32(0.5) + np.float32(0.5) * u3[3])
+            tem = float(np.float32(0.5) + np.float32(0.5) * u3[4])
+            src.append(sphere(cx, cy, cz, r, den, tem))
+        Kd, steps_d = 600, 200
+    else:
+        raise KeyError(f"unknown workload {name!r}")
+    N = occ.shape[0]
+    p = smoke_params(N, K if K is not None else Kd, substeps=substeps, omega=omega, vel_mode=vel_mode,
+                     sca_mode=sca_mode)
+    p.set_sources(src)
+    u, v, w = initial_velocity(occ, seed)
+    T = np.zeros((N, N, N), np.float32)
+    rho = np.zeros((N, N, N), np.float32)
+    return Workload(name, N, N, N, p, occ, u, v, w, T, rho, steps if steps is not None else steps_d,
+                    {"seed": seed, "K": p.sor_iters, "substeps": substeps})
+
+
+def small_case(W: int, H: int, D: int, *, seed: int = 7, K: int = 20, substeps: int = 4, obstacle: bool = True,
+               closed: bool = False, vel_amp: float = 0.05, scalars: bool = True,
+               vel_mode=capi.ADV_VEL_INMAC_OUTMAC, sca_mode=capi.ADV_SCA_MAC, omega: float = 1.9) -> Workload:
+    """A small, irregular, fully seeded case for parity tests (odd sizes allowed)."""
+    occ = walls_closed(W, H, D) if closed else walls_open_top(W, H, D)
+    if obstacle and min(W, H, D) >= 6:
+        add_box(occ, W // 3, W // 3 + 1, H // 2, H // 2 + 1, D // 3, D // 2)
+    p = smoke_params(W, K, substeps=substeps, omega=omega, vel_mode=vel_mode, sca_mode=sca_mode,
+                     solver=capi.SOLVER_CLOSED if closed else capi.SOLVER_OPEN)
+    p.step_time = 0.05
+    p.set_sources([sphere(W / 2, min(2.5, H / 3), D / 2, max(1.5, W / 6)),
+                   box(W / 4, H / 4 + 0.5, D / 2, 1.0, 1.0, 1.5, 0.7, 0.4)])
+    u, v, w = initial_velocity(occ, seed, amp=vel_amp)
+    if scalars:
+        T = uniform(seed + 1, W * H * D, 0.0, 1.0).reshape(D, H, W)
+        rho = uniform(seed + 2, W * H * D, 0.0, 1.0).reshape(D, H, W)
+    else:
+        T = np.zeros((D, H, W), np.float32)
+        rho = np.zeros((D, H, W), np.float32)
+    return Workload(f"small{W}x{H}x{D}", W, H, D, p, occ, u, v, w, T, rho, 1, {"seed": seed})
