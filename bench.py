@@ -42,6 +42,8 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="plain256")
     ap.add_argument("--sor-depth", type=int, default=0, help="SOR iterations per fused pass (0 = default)")
+    ap.add_argument("--sor-variant", type=int, default=-1, help="fused SOR kernel variant (-1 = default)")
+    ap.add_argument("--zchunk", type=int, default=0, help="z planes per SOR CTA (0 = automatic)")
     ap.add_argument("--cpu-sample", default="plain128", help="grid of the bounded CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -185,9 +187,14 @@ def run_ours(args):
     g = capi.Grid(w.W, w.H, w.D)
     g.set_params(w.params)
     g.set_sor_config(args.sor_depth, False)
+    g.set_sor_variant(args.sor_variant, args.zchunk)
     g.load_state(w.occ, w.u, w.v, w.w, w.T, w.rho)
-    stream = torch.cuda.current_stream()
+    # An explicit stream: the library treats a NULL stream as the grid's own
+    # stream, so the events must sit on the stream the kernels run on.
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     sp = stream.cuda_stream
+    assert sp != 0
     cells = w.cells
 
     sampler = ClockSampler(local)
@@ -205,6 +212,8 @@ def run_ours(args):
 
     # -- dominant kernel (temporally blocked SOR): per-launch duration, live --
     depth = args.sor_depth if args.sor_depth > 0 else 2
+    if args.sor_variant >= 0:
+        depth = capi.sor_variants()[args.sor_variant].depth
     passes = math.ceil(2 * K / (2 * depth))
     reps = 3
     p0 = w.params.copy()

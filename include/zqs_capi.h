@@ -191,6 +191,19 @@ ZQS_API int zqs_grid_stats(zqs_grid* g, zqs_stats* out, void* stream);
  * runs the plain one-colour-per-launch kernel (the self-check path). */
 ZQS_API int zqs_grid_set_sor_config(zqs_grid* g, int temporal_depth, int split_colours);
 
+/* Fused SOR kernel variants (for tuning): iterations fused per HBM pass, xy
+ * tile, cell pairs per thread, threads and shared memory per CTA, CTAs that fit
+ * on one SM of the current device (0: does not fit). */
+typedef struct zqs_sor_variant {
+    int32_t depth, tile_x, tile_y, pairs_per_thread, threads, ctas_per_sm;
+    int64_t smem_bytes;
+} zqs_sor_variant;
+ZQS_API int zqs_sor_variant_count(void);
+ZQS_API int zqs_sor_variant_info(int index, zqs_sor_variant* out);
+/* Select a fused variant (-1: default for the configured depth) and the z
+ * planes each CTA streams (0: chosen from the grid and the device). */
+ZQS_API int zqs_grid_set_sor_variant(zqs_grid* g, int index, int zchunk);
+
 /* Wait for all work queued on the stream (NULL: the handle's own stream). */
 ZQS_API int zqs_grid_synchronize(zqs_grid* g, void* stream);
 

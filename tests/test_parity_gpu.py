@@ -190,18 +190,37 @@ def test_plain64_100_steps(zqs_lib, oracle32, oracle64):
     assert float(out["rho"].sum()) > 100.0   # smoke has risen and spread
 
 
-@pytest.mark.parametrize("depth", [1, 2, 3, 4])
-def test_sor_fused_equals_split_256(zqs_lib, depth):
-    """Colour-race self-check at a full configuration size: the temporally
-    blocked SOR reproduces one-colour-per-launch sweeps bit for bit."""
-    w = wl.make("plain256", K=11)
+def _variants():
+    from zq_smokesimulation_gb300 import capi as c
+    try:
+        return list(range(len(c.sor_variants())))
+    except Exception:
+        return list(range(10))
+
+
+@pytest.mark.parametrize("variant", _variants())
+@pytest.mark.parametrize("case", ["plain256", "odd"])
+def test_sor_fused_variants_equal_split(zqs_lib, variant, case):
+    """Colour-race self-check: every temporally blocked SOR variant reproduces
+    one-colour-per-launch sweeps bit for bit (K=11 also exercises the
+    shorter remainder pass), at full size and on an odd-sized obstacle grid."""
+    if case == "plain256":
+        w = wl.make("plain256", K=11)
+    else:
+        w = wl.small_case(37, 29, 23, K=11, vel_amp=0.3)
+    info = capi.sor_variants()[variant]
+    if info.ctas_per_sm < 1:
+        pytest.skip("variant does not fit this device")
     g1 = gpu_grid(w, sor=(1, True))
     g1.project()
-    g2 = gpu_grid(w, sor=(depth, False))
-    g2.project()
-    a = {k: g1.download(f) for k, f in (("p", capi.FIELD_PRESSURE), ("v", capi.FIELD_V))}
-    b = {k: g2.download(f) for k, f in (("p", capi.FIELD_PRESSURE), ("v", capi.FIELD_V))}
-    assert_same(b, a, keys=("p", "v"), what=f"depth {depth}")
+    g2 = gpu_grid(w, sor=(info.depth, False))
+    for zchunk in (0, 5):
+        g2.load_state(w.occ, w.u, w.v, w.w, w.T, w.rho)
+        g2.set_sor_variant(variant, zchunk)
+        g2.project()
+        a = {k: g1.download(f) for k, f in (("p", capi.FIELD_PRESSURE), ("v", capi.FIELD_V))}
+        b = {k: g2.download(f) for k, f in (("p", capi.FIELD_PRESSURE), ("v", capi.FIELD_V))}
+        assert_same(b, a, keys=("p", "v"), what=f"variant {variant} zchunk {zchunk}")
 
 
 def test_plain256_one_step_vs_oracle(zqs_lib, oracle32):

@@ -63,6 +63,12 @@ class Stats(C.Structure):
                 ("free_cells", C.c_int64)]
 
 
+class SorVariant(C.Structure):
+    _fields_ = [("depth", C.c_int32), ("tile_x", C.c_int32), ("tile_y", C.c_int32),
+                ("pairs_per_thread", C.c_int32), ("threads", C.c_int32), ("ctas_per_sm", C.c_int32),
+                ("smem_bytes", C.c_int64)]
+
+
 class Layout(C.Structure):
     _fields_ = [("W", C.c_int32), ("H", C.c_int32), ("D", C.c_int32), ("pitch_x", C.c_int32),
                 ("rows", C.c_int32), ("planes", C.c_int32), ("plane_elems", C.c_int64),
@@ -75,8 +81,8 @@ CAPI_SYMBOLS = [
     "zqs_grid_get_layout", "zqs_grid_set_params", "zqs_grid_get_params", "zqs_grid_upload",
     "zqs_grid_download", "zqs_grid_step", "zqs_grid_use_graph", "zqs_stage_add_force", "zqs_stage_attenuate",
     "zqs_stage_advect_velocity", "zqs_stage_project", "zqs_stage_advect_scalar", "zqs_stage_reinject",
-    "zqs_grid_mac_to_regular4", "zqs_grid_stats", "zqs_grid_set_sor_config", "zqs_grid_synchronize",
-    "zqs_grid_launch_count",
+    "zqs_grid_mac_to_regular4", "zqs_grid_stats", "zqs_grid_set_sor_config", "zqs_sor_variant_count",
+    "zqs_sor_variant_info", "zqs_grid_set_sor_variant", "zqs_grid_synchronize", "zqs_grid_launch_count",
 ]
 LEGACY_C_SYMBOLS = ["ZQ_Cuda_Prepare_Advection", "Advect_Velocity", "Advect_Scalar", "AddForce3D",
                     "Attenuation3D", "zqs_project_sor"]
@@ -133,6 +139,9 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.zqs_grid_launch_count.argtypes = [vp]
     lib.zqs_grid_launch_count.restype = C.c_int64
     lib.zqs_grid_synchronize.argtypes = [vp, vp]
+    lib.zqs_sor_variant_count.restype = i
+    lib.zqs_sor_variant_info.argtypes = [i, C.POINTER(SorVariant)]
+    lib.zqs_grid_set_sor_variant.argtypes = [vp, i, i]
     # legacy shims
     lib.ZQ_Cuda_Prepare_Advection.argtypes = [C.c_uint, C.c_uint, C.c_uint, f, C.c_uint, f]
     lib.ZQ_Cuda_Prepare_Advection.restype = None
@@ -164,6 +173,16 @@ def default_params(W: int, H: int, D: int) -> Params:
     p = Params()
     load().zqs_params_default(C.byref(p), W, H, D)
     return p
+
+
+def sor_variants() -> list[SorVariant]:
+    lib = load()
+    out = []
+    for i in range(lib.zqs_sor_variant_count()):
+        v = SorVariant()
+        check(lib.zqs_sor_variant_info(i, C.byref(v)), "zqs_sor_variant_info")
+        out.append(v)
+    return out
 
 
 def ptr(a: np.ndarray) -> int:
@@ -226,6 +245,9 @@ class Grid:
 
     def set_sor_config(self, temporal_depth: int = 0, split: bool = False):
         check(self.lib.zqs_grid_set_sor_config(self.h, temporal_depth, 1 if split else 0), "set_sor_config")
+
+    def set_sor_variant(self, index: int = -1, zchunk: int = 0):
+        check(self.lib.zqs_grid_set_sor_variant(self.h, index, zchunk), "set_sor_variant")
 
     def use_graph(self, enable: bool):
         check(self.lib.zqs_grid_use_graph(self.h, 1 if enable else 0), "use_graph")

@@ -496,6 +496,7 @@ ZQS_API int zqs_grid_set_sor_config(zqs_grid* g, int temporal_depth, int split_c
     }
     g->sor.temporal_depth = temporal_depth == 0 ? 2 : temporal_depth;
     g->sor.split = split_colours ? 1 : 0;
+    g->sor.variant = -1;
     g->drop_graphs();
     return ZQS_OK;
 }
@@ -639,6 +640,30 @@ ZQS_API int zqs_grid_stats(zqs_grid* g, zqs_stats* out, void* stream) {
         ZQS_CUDA_TRY(cudaMemcpy(m, g->g.red + g->g.red_len - 2, sizeof(m), cudaMemcpyDeviceToHost));
         out->div_mean_removed = (double)(float)m[0];
     }
+    return ZQS_OK;
+}
+
+ZQS_API int zqs_sor_variant_count(void) { return sor_variant_count(); }
+
+ZQS_API int zqs_sor_variant_info(int index, zqs_sor_variant* out) { return sor_variant_info(index, out); }
+
+ZQS_API int zqs_grid_set_sor_variant(zqs_grid* g, int index, int zchunk) {
+    if (!g || index < -1 || index >= sor_variant_count() || zchunk < 0) {
+        set_error("zqs_grid_set_sor_variant: bad arguments");
+        return ZQS_EINVAL;
+    }
+    if (index >= 0) {
+        zqs_sor_variant v;
+        int rc = sor_variant_info(index, &v);
+        if (rc) return rc;
+        if (v.ctas_per_sm < 1) {
+            set_error("zqs_grid_set_sor_variant: variant does not fit on this device");
+            return ZQS_EUNSUPPORTED;
+        }
+    }
+    g->sor.variant = index;
+    g->sor.zchunk = zchunk;
+    g->drop_graphs();
     return ZQS_OK;
 }
 

@@ -14,14 +14,18 @@
 // running sum that starts at +0 is never -0, and x + (+0) == x otherwise).
 //
 // Two SOR kernels:
-//   k_sor_colour   one launch per colour, in place (the plain form, also the
-//                  colour-race self-check of the fused kernel);
-//   k_sor_tb<S>    S half-sweeps per HBM pass (S/2 iterations): a CTA owns an
-//                  xy tile plus an S-cell halo and streams a z chunk through a
-//                  ring of S+2 shared-memory planes; half-sweep s runs on plane
-//                  t-s at time t over the tile grown by S-s cells, so every
-//                  value it reads is at the correct sweep.  Results are
-//                  identical to S/2 iterations of k_sor_colour.
+//   k_sor_colour  one launch per colour, in place: the plain form, and the
+//                 colour-race self-check of the fused kernel.
+//   k_sor_rb<S>   S half-sweeps (S/2 iterations) per HBM pass.  A CTA owns a
+//                 TX x TY tile plus an S-cell halo and streams a z chunk through
+//                 a ring of 2S+2 shared-memory planes.  One thread per (red,
+//                 black) cell pair along x; each plane is stored colour-
+//                 compressed (red cells and black cells in separate arrays), so
+//                 every neighbour read of a warp is contiguous.  Half-sweep s
+//                 runs on plane t-2s at step t over the tile grown by S-s cells:
+//                 the two-plane lag lets all S half-sweeps of a step run at once
+//                 with one barrier per step, and every value each reads is at the
+//                 right sweep.  Results equal S/2 iterations of k_sor_colour.
 #include "zqs_internal.h"
 
 #include <algorithm>
@@ -72,7 +76,7 @@ __global__ void k_divergence(Layout L, const float* __restrict__ u, const float*
     }
 }
 
-// Single block: sums the partials in a fixed order, stores mean (as double) in out[0].
+// Single block: sums the partials in a fixed order, stores the mean in out[0].
 __global__ void k_reduce_mean(const double* __restrict__ part, long long nblocks, double* __restrict__ out) {
     __shared__ double ss[256], sc[256];
     double s = 0.0, c = 0.0;
@@ -146,116 +150,331 @@ __global__ void k_sor_colour(Layout L, float* __restrict__ p, const float* __res
     p[c] = sor_update(p[c], s, __ldg(div + c), cnt, omega, om1);
 }
 
-template <int S, int TX, int TY>
-struct TbShape {
-    static constexpr int RW = TX + 2 * S;
-    static constexpr int RH = TY + 2 * S;
-    static constexpr int PL = RW * RH;
-    static constexpr int NP = S + 2;
-    static constexpr size_t smem = (size_t)NP * PL * (sizeof(float) * 2 + 1);
+template <int S, int TX, int TY, int PPT>
+struct RbShape {
+    static_assert(S % 2 == 0 && TX % 2 == 0, "S and TX must be even");
+    static constexpr int RW = TX + 2 * S;  // region width in cells
+    static constexpr int RH = TY + 2 * S;  // region height
+    static_assert(RH % PPT == 0, "region rows must split evenly over a thread's pairs");
+    static constexpr int PW = RW / 2;      // cell pairs per row
+    static constexpr int CA = PW * RH;     // pairs (= cells of one colour) per plane
+    static constexpr int NT = CA / PPT;    // threads per CTA; pair q of thread t is t + q*NT
+    static constexpr int NP = 2 * S + 2;   // ring planes
+    static constexpr size_t smem = (size_t)NP * 2 * CA * (4 + 4 + 1);
 };
 
-__device__ __forceinline__ int ring(int z, int np) {
-    int r = z % np;
-    return r < 0 ? r + np : r;
-}
-
-// Temporally blocked red-black SOR: S half-sweeps (S even, red first) per pass,
-// reading pin and writing pout.  Grid: (ceil(W/TX), ceil(H/TY), ceil(D/zc)).
-template <int S, int TX, int TY>
-__global__ void __launch_bounds__(256) k_sor_tb(Layout L, const float* __restrict__ pin, float* __restrict__ pout,
-                                                const float* __restrict__ div, const uint8_t* __restrict__ flags,
-                                                float omega, float om1, int zc) {
-    using Sh = TbShape<S, TX, TY>;
-    constexpr int RW = Sh::RW, RH = Sh::RH, PL = Sh::PL, NP = Sh::NP;
+// The t loop is unrolled by the ring size NP, so every shared-memory slot of a
+// step is a compile-time constant and each access is base + immediate.
+template <int S, int TX, int TY, int PPT>
+__global__ void __launch_bounds__(RbShape<S, TX, TY, PPT>::NT)
+    k_sor_rb(Layout L, const float* __restrict__ pin, float* __restrict__ pout, const float* __restrict__ div,
+             const uint8_t* __restrict__ flags, float omega, float om1, int zc) {
+    using Sh = RbShape<S, TX, TY, PPT>;
+    constexpr int PW = Sh::PW, NP = Sh::NP, CA = Sh::CA, NT = Sh::NT;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    float* sp = reinterpret_cast<float*>(smem_raw);
-    float* sd = sp + NP * PL;
-    uint8_t* sf = reinterpret_cast<uint8_t*>(sd + NP * PL);
+    float* sp = reinterpret_cast<float*>(smem_raw);              // [NP][2][CA] pressure, colour-compressed
+    float* sd = sp + NP * 2 * CA;                                  // [NP][2][CA] divergence
+    uint8_t* sf = reinterpret_cast<uint8_t*>(sd + NP * 2 * CA);    // [NP][2][CA] flags
+
     const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
     const int z0 = blockIdx.z * zc;
     const int z1 = min(z0 + zc, L.D);
-    const int tid = threadIdx.x;
-    const int nthr = blockDim.x;
+    const int plane = (int)L.plane;
 
-    for (int t = z0 - S; t < z1 + S; t++) {
-        {
-            const int slot = ring(t, NP);
-            float* P = sp + slot * PL;
-            float* Dv = sd + slot * PL;
-            uint8_t* F = sf + slot * PL;
-            const bool zin = (t >= 0 && t < L.D);
-            for (int idx = tid; idx < PL; idx += nthr) {
-                const int lj = idx / RW, li = idx - lj * RW;
-                const int i = x0 - S + li, j = y0 - S + lj;
-                float pv = 0.0f, dv = 0.0f;
-                uint8_t fv = 0;
-                if (zin && i >= 0 && i < L.W && j >= 0 && j < L.H) {
-                    const int c = lidx(L, i, j, t);
-                    fv = __ldg(flags + c);
-                    if (fv & F_FREE) {
-                        pv = pin[c];
-                        dv = __ldg(div + c);
+    int me[PPT], jrow[PPT], gaddr[PPT];
+    unsigned amask[PPT];
+    bool pin_ok[PPT], out_ok[PPT];
+#pragma unroll
+    for (int q = 0; q < PPT; q++) {
+        const int e = threadIdx.x + q * NT;
+        const int row = e / PW, m = e - row * PW;
+        me[q] = e;
+        const int xl = x0 - S + 2 * m;  // left cell of the pair (even)
+        const int j = y0 - S + row;
+        jrow[q] = j;
+        const int ly = row - S, lxl = 2 * m - S;
+        unsigned mk = 0;
+#pragma unroll
+        for (int r = 0; r < S; r++)
+#pragma unroll
+            for (int o = 0; o < 2; o++) {
+                const int lx = lxl + o;
+                if (lx >= -r && lx < TX + r && ly >= -r && ly < TY + r) mk |= 1u << (2 * r + o);
+            }
+        amask[q] = mk;
+        pin_ok[q] = xl >= 0 && xl < L.W && j >= 0 && j < L.H;
+        out_ok[q] = pin_ok[q] && ly >= 0 && ly < TY && lxl >= 0 && lxl < TX;
+        gaddr[q] = pin_ok[q] ? lidx(L, xl, j, z0 - S) : 0;  // dereferenced only for planes inside [0,D)
+    }
+
+    const int tbeg = z0 - S;
+    const int nsteps = (z1 - z0) + 3 * S + 1;  // t = z0-S .. z1+2S
+    const int flo = max(0, z0 - S), fhi = min(L.D, z1 + S);
+
+    float2 np_[PPT], nd[PPT];
+    unsigned nf[PPT];
+#pragma unroll
+    for (int q = 0; q < PPT; q++) {
+        np_[q] = make_float2(0.0f, 0.0f);
+        nd[q] = np_[q];
+        nf[q] = 0;
+        if (pin_ok[q] && tbeg >= flo && tbeg < fhi) {
+            np_[q] = __ldg(reinterpret_cast<const float2*>(pin + gaddr[q]));
+            nd[q] = __ldg(reinterpret_cast<const float2*>(div + gaddr[q]));
+            nf[q] = __ldg(reinterpret_cast<const unsigned short*>(flags + gaddr[q]));
+        }
+    }
+
+    for (int g = 0; g < nsteps; g += NP) {
+#pragma unroll
+        for (int qs = 0; qs < NP; qs++) {
+            if (g + qs < nsteps) {
+                const int t = tbeg + g + qs;  // plane t lives in slot qs
+                // 1. the prefetched plane t into its slot
+#pragma unroll
+                for (int q = 0; q < PPT; q++) {
+                    const int lc = (jrow[q] + t) & 1;  // colour of the left cell
+                    const int a0 = lc ? CA : 0, a1 = CA - a0;
+                    float* P = sp + qs * 2 * CA + me[q];
+                    float* Dv = sd + qs * 2 * CA + me[q];
+                    uint8_t* F = sf + qs * 2 * CA + me[q];
+                    P[a0] = np_[q].x;
+                    P[a1] = np_[q].y;
+                    Dv[a0] = nd[q].x;
+                    Dv[a1] = nd[q].y;
+                    F[a0] = (uint8_t)(nf[q] & 0xffu);
+                    F[a1] = (uint8_t)(nf[q] >> 8);
+                }
+                // 2. prefetch plane t+1 (in flight during the half-sweeps)
+#pragma unroll
+                for (int q = 0; q < PPT; q++) {
+                    gaddr[q] += plane;
+                    np_[q] = make_float2(0.0f, 0.0f);
+                    nd[q] = np_[q];
+                    nf[q] = 0;
+                    if (pin_ok[q] && t + 1 >= flo && t + 1 < fhi) {
+                        np_[q] = __ldg(reinterpret_cast<const float2*>(pin + gaddr[q]));
+                        nd[q] = __ldg(reinterpret_cast<const float2*>(div + gaddr[q]));
+                        nf[q] = __ldg(reinterpret_cast<const unsigned short*>(flags + gaddr[q]));
                     }
                 }
-                P[idx] = pv;
-                Dv[idx] = dv;
-                F[idx] = fv;
-            }
-        }
-        __syncthreads();
+                // 3. half-sweep s on plane t-2s (all S at once; they touch disjoint data)
 #pragma unroll
-        for (int s = 1; s <= S; s++) {
-            const int z = t - s;
-            const int r = S - s;
-            if (z >= max(z0 - r, 0) && z < min(z1 + r, L.D)) {
-                const int colour = (s - 1) & 1;
-                float* Pc = sp + ring(z, NP) * PL;
-                const float* Pm = sp + ring(z - 1, NP) * PL;
-                const float* Pp = sp + ring(z + 1, NP) * PL;
-                const float* Dc = sd + ring(z, NP) * PL;
-                const uint8_t* Fc = sf + ring(z, NP) * PL;
-                const int rw = TX + 2 * r;
-                const int halfw = rw >> 1;
-                const int nupd = halfw * (TY + 2 * r);
-                for (int q = tid; q < nupd; q += nthr) {
-                    const int row = q / halfw;
-                    const int m = q - row * halfw;
-                    const int ly = row - r;
-                    const int j = y0 + ly;
-                    const int base = x0 - r + 2 * m;
-                    const int i = base + ((base + j + z + colour) & 1);
-                    const int si = (ly + S) * RW + (i - x0 + S);
-                    const uint8_t f = Fc[si];
-                    const int cnt = (f & F_CNT_MASK) >> F_CNT_SHIFT;
-                    if (!(f & F_FREE) || cnt == 0) continue;
-                    float sum = 0.0f;
-                    sum = sum + Pc[si - 1];
-                    sum = sum + Pc[si + 1];
-                    sum = sum + Pc[si - RW];
-                    sum = sum + Pc[si + RW];
-                    sum = sum + Pm[si];
-                    sum = sum + Pp[si];
-                    Pc[si] = sor_update(Pc[si], sum, Dc[si], cnt, omega, om1);
+                for (int s = 1; s <= S; s++) {
+                    const int z = t - 2 * s;
+                    const int r = S - s;
+                    if (z >= max(z0 - r, 0) && z < min(z1 + r, L.D)) {
+                        const int c = (s - 1) & 1;  // red first
+                        const int sz = (qs - 2 * s + 2 * NP) % NP;
+                        const int szm = (sz + NP - 1) % NP;
+                        const int szp = (sz + 1) % NP;
+#pragma unroll
+                        for (int q = 0; q < PPT; q++) {
+                            const int o = ((jrow[q] + t) & 1) ^ c;  // parity of z equals parity of t
+                            if ((amask[q] >> (2 * r + o)) & 1u) {
+                                const int cnt = (sf[(sz * 2 + c) * CA + me[q]] >> F_CNT_SHIFT) & 7;
+                                if (cnt) {  // zero for cells that are not free
+                                    const float* Po = sp + (sz * 2 + (c ^ 1)) * CA + me[q];
+                                    float sum = 0.0f;
+                                    sum = sum + Po[o - 1];
+                                    sum = sum + Po[o];
+                                    sum = sum + Po[-PW];
+                                    sum = sum + Po[PW];
+                                    sum = sum + sp[(szm * 2 + (c ^ 1)) * CA + me[q]];
+                                    sum = sum + sp[(szp * 2 + (c ^ 1)) * CA + me[q]];
+                                    float* Pc = sp + (sz * 2 + c) * CA + me[q];
+                                    *Pc = sor_update(*Pc, sum, sd[(sz * 2 + c) * CA + me[q]], cnt, omega, om1);
+                                }
+                            }
+                        }
+                    }
                 }
-            }
-            __syncthreads();
-        }
-        const int zo = t - S;
-        if (zo >= z0 && zo < z1) {
-            const float* P = sp + ring(zo, NP) * PL;
-            const uint8_t* F = sf + ring(zo, NP) * PL;
-            for (int idx = tid; idx < TX * TY; idx += nthr) {
-                const int ly = idx / TX, lx = idx - ly * TX;
-                const int i = x0 + lx, j = y0 + ly;
-                if (i < L.W && j < L.H) {
-                    const int si = (ly + S) * RW + (lx + S);
-                    if (F[si] & F_FREE) pout[lidx(L, i, j, zo)] = P[si];
+                // 4. plane t-2S-1 finished its last half-sweep in the previous step
+                const int zo = t - 2 * S - 1;
+                if (zo >= z0 && zo < z1) {
+                    const int so = (qs - 2 * S - 1 + 2 * NP) % NP;
+#pragma unroll
+                    for (int q = 0; q < PPT; q++) {
+                        if (out_ok[q]) {
+                            const int lc = (jrow[q] + zo) & 1;
+                            const float a = sp[(so * 2 + lc) * CA + me[q]];
+                            const float b = sp[(so * 2 + (lc ^ 1)) * CA + me[q]];
+                            *reinterpret_cast<float2*>(pout + gaddr[q] - (2 * S + 2) * plane) = make_float2(a, b);
+                        }
+                    }
                 }
+                __syncthreads();
             }
         }
-        // The next load writes the slot of plane t+1-NP = t-S-1, whose last
-        // reader (half-sweep S at this step) finished before the barrier above.
+    }
+}
+
+// Register-column form of k_sor_rb: each thread keeps its pair's pressure
+// (both colours, every plane in flight) and flags in registers, so the self,
+// same-pair x and both z neighbours never touch shared memory.  Shared memory
+// holds the published pressure (for the x neighbour in the adjacent pair and
+// the y neighbours) and the divergence.  Same schedule, same results.
+template <int S, int TX, int TY, int PPT>
+struct RegShape {
+    static_assert(S % 2 == 0 && TX % 2 == 0, "S and TX must be even");
+    static constexpr int RW = TX + 2 * S;
+    static constexpr int RH = TY + 2 * S;
+    static_assert(RH % PPT == 0, "region rows must split evenly over a thread's pairs");
+    static constexpr int PW = RW / 2;
+    static constexpr int CA = PW * RH;
+    static constexpr int NT = CA / PPT;
+    static constexpr int NP = 2 * S + 2;
+    static constexpr size_t smem = (size_t)NP * 2 * CA * (4 + 4);
+};
+
+template <int S, int TX, int TY, int PPT>
+__global__ void __launch_bounds__(RegShape<S, TX, TY, PPT>::NT)
+    k_sor_reg(Layout L, const float* __restrict__ pin, float* __restrict__ pout, const float* __restrict__ div,
+              const uint8_t* __restrict__ flags, float omega, float om1, int zc) {
+    using Sh = RegShape<S, TX, TY, PPT>;
+    constexpr int PW = Sh::PW, NP = Sh::NP, CA = Sh::CA, NT = Sh::NT;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float* sp = reinterpret_cast<float*>(smem_raw);  // [NP][2][CA] published pressure
+    float* sd = sp + NP * 2 * CA;                      // [NP][2][CA] divergence
+
+    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
+    const int z0 = blockIdx.z * zc;
+    const int z1 = min(z0 + zc, L.D);
+    const int plane = (int)L.plane;
+
+    int me[PPT], jrow[PPT], gaddr[PPT];
+    unsigned amask[PPT];
+    bool pin_ok[PPT], out_ok[PPT];
+#pragma unroll
+    for (int q = 0; q < PPT; q++) {
+        const int e = threadIdx.x + q * NT;
+        const int row = e / PW, m = e - row * PW;
+        me[q] = e;
+        const int xl = x0 - S + 2 * m;
+        const int j = y0 - S + row;
+        jrow[q] = j;
+        const int ly = row - S, lxl = 2 * m - S;
+        unsigned mk = 0;
+#pragma unroll
+        for (int r = 0; r < S; r++)
+#pragma unroll
+            for (int o = 0; o < 2; o++) {
+                const int lx = lxl + o;
+                if (lx >= -r && lx < TX + r && ly >= -r && ly < TY + r) mk |= 1u << (2 * r + o);
+            }
+        amask[q] = mk;
+        pin_ok[q] = xl >= 0 && xl < L.W && j >= 0 && j < L.H;
+        out_ok[q] = pin_ok[q] && ly >= 0 && ly < TY && lxl >= 0 && lxl < TX;
+        gaddr[q] = pin_ok[q] ? lidx(L, xl, j, z0 - S) : 0;
+    }
+
+    const int tbeg = z0 - S;
+    const int nsteps = (z1 - z0) + 3 * S + 1;
+    const int flo = max(0, z0 - S), fhi = min(L.D, z1 + S);
+
+    float P[PPT][NP][2];     // pressure by colour, ring of planes
+    unsigned F[PPT][NP];     // flags by colour: byte c = flags of the colour-c cell
+    float2 np_[PPT], nd[PPT];
+    unsigned nf[PPT];
+#pragma unroll
+    for (int q = 0; q < PPT; q++) {
+#pragma unroll
+        for (int a = 0; a < NP; a++) {
+            P[q][a][0] = P[q][a][1] = 0.0f;
+            F[q][a] = 0u;
+        }
+        np_[q] = make_float2(0.0f, 0.0f);
+        nd[q] = np_[q];
+        nf[q] = 0;
+        if (pin_ok[q] && tbeg >= flo && tbeg < fhi) {
+            np_[q] = __ldg(reinterpret_cast<const float2*>(pin + gaddr[q]));
+            nd[q] = __ldg(reinterpret_cast<const float2*>(div + gaddr[q]));
+            nf[q] = __ldg(reinterpret_cast<const unsigned short*>(flags + gaddr[q]));
+        }
+    }
+
+    for (int g = 0; g < nsteps; g += NP) {
+#pragma unroll
+        for (int qs = 0; qs < NP; qs++) {
+            if (g + qs < nsteps) {
+                const int t = tbeg + g + qs;
+                // 1. plane t: registers by colour, and publish
+#pragma unroll
+                for (int q = 0; q < PPT; q++) {
+                    const bool lc = ((jrow[q] + t) & 1) != 0;  // the left cell is black
+                    P[q][qs][0] = lc ? np_[q].y : np_[q].x;
+                    P[q][qs][1] = lc ? np_[q].x : np_[q].y;
+                    F[q][qs] = lc ? (((nf[q] & 0xffu) << 8) | (nf[q] >> 8)) : nf[q];
+                    float* Pp = sp + qs * 2 * CA + me[q];
+                    float* Dp = sd + qs * 2 * CA + me[q];
+                    Pp[0] = P[q][qs][0];
+                    Pp[CA] = P[q][qs][1];
+                    Dp[0] = lc ? nd[q].y : nd[q].x;
+                    Dp[CA] = lc ? nd[q].x : nd[q].y;
+                }
+                // 2. prefetch plane t+1
+#pragma unroll
+                for (int q = 0; q < PPT; q++) {
+                    gaddr[q] += plane;
+                    np_[q] = make_float2(0.0f, 0.0f);
+                    nd[q] = np_[q];
+                    nf[q] = 0;
+                    if (pin_ok[q] && t + 1 >= flo && t + 1 < fhi) {
+                        np_[q] = __ldg(reinterpret_cast<const float2*>(pin + gaddr[q]));
+                        nd[q] = __ldg(reinterpret_cast<const float2*>(div + gaddr[q]));
+                        nf[q] = __ldg(reinterpret_cast<const unsigned short*>(flags + gaddr[q]));
+                    }
+                }
+                // 3. half-sweeps
+#pragma unroll
+                for (int s = 1; s <= S; s++) {
+                    const int z = t - 2 * s;
+                    const int r = S - s;
+                    if (z >= max(z0 - r, 0) && z < min(z1 + r, L.D)) {
+                        const int c = (s - 1) & 1;
+                        const int sz = (qs - 2 * s + 2 * NP) % NP;
+                        const int szm = (sz + NP - 1) % NP;
+                        const int szp = (sz + 1) % NP;
+#pragma unroll
+                        for (int q = 0; q < PPT; q++) {
+                            const int o = ((jrow[q] + t) & 1) ^ c;
+                            const int cnt = (F[q][sz] >> (8 * c + F_CNT_SHIFT)) & 7;
+                            if (((amask[q] >> (2 * r + o)) & 1u) && cnt) {
+                                const float* Po = sp + (sz * 2 + (c ^ 1)) * CA + me[q];
+                                const float own = P[q][sz][c ^ 1];
+                                const float adj = o ? Po[1] : Po[-1];
+                                float sum = 0.0f;
+                                sum = sum + (o ? own : adj);
+                                sum = sum + (o ? adj : own);
+                                sum = sum + Po[-PW];
+                                sum = sum + Po[PW];
+                                sum = sum + P[q][szm][c ^ 1];
+                                sum = sum + P[q][szp][c ^ 1];
+                                const float nv = sor_update(P[q][sz][c], sum, sd[(sz * 2 + c) * CA + me[q]], cnt,
+                                                            omega, om1);
+                                P[q][sz][c] = nv;
+                                sp[(sz * 2 + c) * CA + me[q]] = nv;
+                            }
+                        }
+                    }
+                }
+                // 4. output plane t-2S-1
+                const int zo = t - 2 * S - 1;
+                if (zo >= z0 && zo < z1) {
+                    const int so = (qs - 2 * S - 1 + 2 * NP) % NP;
+#pragma unroll
+                    for (int q = 0; q < PPT; q++) {
+                        if (out_ok[q]) {
+                            const bool lc = ((jrow[q] + zo) & 1) != 0;
+                            const float a = lc ? P[q][so][1] : P[q][so][0];
+                            const float b = lc ? P[q][so][0] : P[q][so][1];
+                            *reinterpret_cast<float2*>(pout + gaddr[q] - (2 * S + 2) * plane) = make_float2(a, b);
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        }
     }
 }
 
@@ -343,46 +562,149 @@ __global__ void k_stats(Layout L, const float* __restrict__ u, const float* __re
     }
 }
 
-template <int S, int TX, int TY>
-int prepare_tb() {
-    using Sh = TbShape<S, TX, TY>;
-    cudaError_t e = cudaFuncSetAttribute(k_sor_tb<S, TX, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)Sh::smem);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(k_sor_tb)");
-    return ZQS_OK;
+// ---------------------------------------------------------------- host side
+
+struct RbVariant {
+    int S, TX, TY, ppt, nt;
+    size_t smem;
+    int ctas_per_sm;
+    cudaError_t (*launch)(dim3, const Layout&, const float*, float*, const float*, const uint8_t*, float, float, int,
+                          cudaStream_t);
+    const void* fn;
+};
+
+template <int S, int TX, int TY, int PPT>
+cudaError_t rb_launch(dim3 gr, const Layout& L, const float* pin, float* pout, const float* div,
+                      const uint8_t* flags, float omega, float om1, int zc, cudaStream_t st) {
+    using Sh = RbShape<S, TX, TY, PPT>;
+    k_sor_rb<S, TX, TY, PPT><<<gr, Sh::NT, Sh::smem, st>>>(L, pin, pout, div, flags, omega, om1, zc);
+    return cudaGetLastError();
 }
 
-template <int S, int TX, int TY>
-int launch_tb(const DevGrid& g, const float* pin, float* pout, const KParams& kp, int zc, cudaStream_t st) {
-    using Sh = TbShape<S, TX, TY>;
-    const Layout& L = g.L;
-    dim3 gr((L.W + TX - 1) / TX, (L.H + TY - 1) / TY, (L.D + zc - 1) / zc);
-    k_sor_tb<S, TX, TY><<<gr, 256, Sh::smem, st>>>(L, pin, pout, g.div, g.flags, kp.omega, kp.om1, zc);
-    return ZQS_OK;
+template <int S, int TX, int TY, int PPT>
+RbVariant rb_variant() {
+    using Sh = RbShape<S, TX, TY, PPT>;
+    RbVariant v;
+    v.S = S;
+    v.TX = TX;
+    v.TY = TY;
+    v.ppt = PPT;
+    v.nt = Sh::NT;
+    v.smem = Sh::smem;
+    v.ctas_per_sm = 0;
+    v.launch = &rb_launch<S, TX, TY, PPT>;
+    v.fn = (const void*)k_sor_rb<S, TX, TY, PPT>;
+    return v;
 }
 
-int launch_tb_depth(int S, const DevGrid& g, const float* pin, float* pout, const KParams& kp, int zc,
-                    cudaStream_t st) {
-    switch (S) {
-        case 2: return launch_tb<2, 32, 16>(g, pin, pout, kp, zc, st);
-        case 4: return launch_tb<4, 32, 16>(g, pin, pout, kp, zc, st);
-        case 6: return launch_tb<6, 32, 16>(g, pin, pout, kp, zc, st);
-        case 8: return launch_tb<8, 32, 16>(g, pin, pout, kp, zc, st);
-        default: set_error("SOR temporal depth must be 1..4 iterations"); return ZQS_EINVAL;
+template <int S, int TX, int TY, int PPT>
+cudaError_t reg_launch(dim3 gr, const Layout& L, const float* pin, float* pout, const float* div,
+                       const uint8_t* flags, float omega, float om1, int zc, cudaStream_t st) {
+    using Sh = RegShape<S, TX, TY, PPT>;
+    k_sor_reg<S, TX, TY, PPT><<<gr, Sh::NT, Sh::smem, st>>>(L, pin, pout, div, flags, omega, om1, zc);
+    return cudaGetLastError();
+}
+
+template <int S, int TX, int TY, int PPT>
+RbVariant reg_variant() {
+    using Sh = RegShape<S, TX, TY, PPT>;
+    RbVariant v;
+    v.S = S;
+    v.TX = TX;
+    v.TY = TY;
+    v.ppt = PPT;
+    v.nt = Sh::NT;
+    v.smem = Sh::smem;
+    v.ctas_per_sm = 0;
+    v.launch = &reg_launch<S, TX, TY, PPT>;
+    v.fn = (const void*)k_sor_reg<S, TX, TY, PPT>;
+    return v;
+}
+
+// The registry of fused SOR variants (temporal depth S/2, tile, pairs per thread);
+// 0-9 keep every plane in shared memory (k_sor_rb), 10-17 keep the thread's own
+// column in registers (k_sor_reg).
+constexpr int kNumVariants = 18;
+RbVariant g_var[kNumVariants];
+// default variant per depth 1..4
+// (measured at 256^3 on GB300: register-column 64x16 at depth 2 is fastest)
+const int kDefaultVariant[5] = {-1, 16, 13, 15, 7};
+int g_num_sms = 0;
+int g_prepared = 0;
+
+// z chunk minimising the estimated pass time: waves x (chunk + pipeline fill)
+int choose_zc(const Layout& L, const RbVariant& v) {
+    const long long tiles = (long long)((L.W + v.TX - 1) / v.TX) * ((L.H + v.TY - 1) / v.TY);
+    const long long slots = (long long)std::max(1, g_num_sms) * std::max(1, v.ctas_per_sm);
+    int best = L.D;
+    double best_cost = 1e300;
+    for (int zc = L.D;; zc = (zc + 1) / 2) {
+        long long ctas = tiles * ((L.D + zc - 1) / zc);
+        long long waves = (ctas + slots - 1) / slots;
+        double cost = (double)waves * (zc + 3 * v.S + 1);
+        if (cost < best_cost - 1e-9) {
+            best_cost = cost;
+            best = zc;
+        }
+        if (zc <= 8) break;
     }
+    return best;
 }
 
 }  // namespace
 
 int sor_prepare() {
-    static int done = 0;  // per process; one device
-    if (done) return ZQS_OK;
-    int rc = prepare_tb<2, 32, 16>();
-    if (!rc) rc = prepare_tb<4, 32, 16>();
-    if (!rc) rc = prepare_tb<6, 32, 16>();
-    if (!rc) rc = prepare_tb<8, 32, 16>();
-    if (!rc) done = 1;
-    return rc;
+    if (g_prepared) return ZQS_OK;  // per process; one device
+    g_var[0] = rb_variant<2, 32, 16, 1>();
+    g_var[1] = rb_variant<2, 32, 16, 2>();
+    g_var[2] = rb_variant<2, 64, 16, 2>();
+    g_var[3] = rb_variant<4, 32, 16, 1>();
+    g_var[4] = rb_variant<4, 32, 16, 2>();
+    g_var[5] = rb_variant<4, 64, 16, 2>();
+    g_var[6] = rb_variant<6, 32, 16, 2>();
+    g_var[7] = rb_variant<8, 32, 8, 2>();
+    g_var[8] = rb_variant<2, 32, 32, 2>();
+    g_var[9] = rb_variant<4, 32, 32, 2>();
+    g_var[10] = reg_variant<2, 32, 16, 1>();
+    g_var[11] = reg_variant<2, 64, 16, 1>();
+    g_var[12] = reg_variant<4, 32, 16, 1>();
+    g_var[13] = reg_variant<4, 64, 16, 1>();
+    g_var[14] = reg_variant<4, 32, 32, 1>();
+    g_var[15] = reg_variant<6, 32, 16, 1>();
+    g_var[16] = reg_variant<2, 32, 16, 2>();
+    g_var[17] = reg_variant<4, 32, 16, 2>();
+    int dev = 0;
+    ZQS_CUDA_TRY(cudaGetDevice(&dev));
+    ZQS_CUDA_TRY(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
+    for (int i = 0; i < kNumVariants; i++) {
+        RbVariant& v = g_var[i];
+        ZQS_CUDA_TRY(cudaFuncSetAttribute(v.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)v.smem));
+        int n = 0;
+        ZQS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, v.fn, v.nt, v.smem));
+        v.ctas_per_sm = n;  // 0: does not fit (never selected)
+    }
+    g_prepared = 1;
+    return ZQS_OK;
+}
+
+int sor_variant_count() { return kNumVariants; }
+
+int sor_variant_info(int i, zqs_sor_variant* out) {
+    if (i < 0 || i >= kNumVariants || !out) {
+        set_error("sor variant index out of range");
+        return ZQS_EINVAL;
+    }
+    int rc = sor_prepare();
+    if (rc) return rc;
+    const RbVariant& v = g_var[i];
+    out->depth = v.S / 2;
+    out->tile_x = v.TX;
+    out->tile_y = v.TY;
+    out->pairs_per_thread = v.ppt;
+    out->threads = v.nt;
+    out->ctas_per_sm = v.ctas_per_sm;
+    out->smem_bytes = (int64_t)v.smem;
+    return ZQS_OK;
 }
 
 int launch_project(DevGrid& g, const KParams& kp, int K, const SorConfig& cfg, cudaStream_t s, LaunchCounter& lc,
@@ -416,21 +738,26 @@ int launch_project(DevGrid& g, const KParams& kp, int K, const SorConfig& cfg, c
         }
         ZQS_LAUNCH_CHECK("k_sor_colour");
     } else {
-        const int Smain = 2 * std::min(cfg.temporal_depth, 4);
-        int remaining = 2 * K;
-        // z chunk: keep a few waves of CTAs in flight
-        const int tiles = ((L.W + 31) / 32) * ((L.H + 15) / 16);
-        int zc = L.D;
-        while (zc > 16 && (long long)tiles * ((L.D + zc - 1) / zc) < 2 * 152) zc = (zc + 1) / 2;
+        int rc = sor_prepare();
+        if (rc) return rc;
+        int vmain = cfg.variant >= 0 ? cfg.variant : kDefaultVariant[std::min(std::max(cfg.temporal_depth, 1), 4)];
+        if (vmain >= kNumVariants || g_var[vmain].ctas_per_sm < 1) {
+            set_error("SOR variant does not fit this device");
+            return ZQS_EUNSUPPORTED;
+        }
+        const int dmain = g_var[vmain].S / 2;
+        int remaining = K;
         while (remaining > 0) {
-            int S = std::min(Smain, remaining);
-            int rc = launch_tb_depth(S, g, cur, nxt, kp, zc, s);
-            if (rc) return rc;
+            const int d = std::min(dmain, remaining);
+            const RbVariant& v = (d == dmain) ? g_var[vmain] : g_var[kDefaultVariant[d]];
+            const int zc = (d == dmain && cfg.zchunk > 0) ? std::min(cfg.zchunk, L.D) : choose_zc(L, v);
+            dim3 gr((L.W + v.TX - 1) / v.TX, (L.H + v.TY - 1) / v.TY, (L.D + zc - 1) / zc);
+            cudaError_t e = v.launch(gr, L, cur, nxt, g.div, g.flags, kp.omega, kp.om1, zc, s);
+            if (e != cudaSuccess) return cuda_fail(e, "k_sor_rb");
             lc.n++;
             std::swap(cur, nxt);
-            remaining -= S;
+            remaining -= d;
         }
-        ZQS_LAUNCH_CHECK("k_sor_tb");
     }
     dim3 gf((L.W + 1 + 31) / 32, (L.H + 1 + 7) / 8, L.D + 1);
     k_gradient<<<gf, b, 0, s>>>(L, g.u, g.v, g.w, cur, g.flags, closed ? 0 : 1);

@@ -120,9 +120,13 @@ int launch_advect_scalar(const DevGrid& g, const KParams& kp, int mode, bool fol
 int launch_reinject(const DevGrid& g, const SourceList& src, cudaStream_t s, LaunchCounter& lc);
 
 struct SorConfig {
-    int temporal_depth;   // iterations per fused pass (>=1)
-    int split;            // 1: one launch per colour (plain kernel)
+    int temporal_depth = 2;  // iterations per fused pass (>=1)
+    int split = 0;           // 1: one launch per colour (plain kernel)
+    int variant = -1;        // fused kernel variant (-1: default for the depth)
+    int zchunk = 0;          // z planes per CTA (0: chosen from the grid)
 };
+int sor_variant_count();
+int sor_variant_info(int i, zqs_sor_variant* out);
 int launch_project(DevGrid& g, const KParams& kp, int K, const SorConfig& cfg, cudaStream_t s,
                    LaunchCounter& lc, float** p_final);
 int sor_prepare();  // sets kernel attributes once per process (outside any capture)
