@@ -104,6 +104,23 @@ extern "C" {
 ZQS_API int zqs_project_sor(float* mac_u, float* mac_v, float* mac_w, const uint8_t* occupy, int width, int height,
                             int depth, int solver, int maxIter, float omega);
 
+/* No counterpart in the reference.  The same projection for callers that
+ * must not allocate GPU memory (a pre-reserved memory pool, code that runs
+ * while a CUDA graph is being captured, runtimes without an allocator):
+ * DEVICE pointers in the reference layouts, updated in place, asynchronous on
+ * `stream` (NULL: the default stream).  It calls no cudaMalloc/cudaFree: its
+ * working fields live in one fixed array compiled into the library (about
+ * 7.6 MB, held by every GPU that loads the library until the process exits),
+ * which limits the grid to ZQS_NOALLOC_MAX_ELEMS padded elements per field,
+ * (W+1 rounded up to 4)*(H+1)*(D+3); 64x64x64 fits.  Larger grids return
+ * ZQS_EINVAL.  The first call on each device looks up the array's device
+ * address; make that first call before any stream capture.  All calls share
+ * the array, so calls that overlap on the GPU (different streams, or
+ * concurrent host threads) race; serialise them.  Returns zqs_status. */
+#define ZQS_NOALLOC_MAX_ELEMS 300000
+ZQS_API int zqs_project_sor_noalloc(float* d_u, float* d_v, float* d_w, const uint8_t* d_occupy, int width,
+                                    int height, int depth, int solver, int maxIter, float omega, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

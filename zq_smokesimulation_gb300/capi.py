@@ -85,7 +85,7 @@ CAPI_SYMBOLS = [
     "zqs_sor_variant_info", "zqs_grid_set_sor_variant", "zqs_grid_synchronize", "zqs_grid_launch_count",
 ]
 LEGACY_C_SYMBOLS = ["ZQ_Cuda_Prepare_Advection", "Advect_Velocity", "Advect_Scalar", "AddForce3D",
-                    "Attenuation3D", "zqs_project_sor"]
+                    "Attenuation3D", "zqs_project_sor", "zqs_project_sor_noalloc"]
 LEGACY_CXX_SYMBOLS = [
     "_ZN20ZQ_CUDA_MACtoRegular18cu_MAC_to_Regular4EPKfS1_S1_P6float4iii",
     "_ZN20ZQ_CUDA_MACtoRegular18cu_Regular4_to_MACEPK6float4PfS3_S3_iii",
@@ -155,6 +155,8 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.Attenuation3D.restype = f
     lib.zqs_project_sor.argtypes = [vp, vp, vp, vp, i, i, i, i, i, f]
     lib.zqs_project_sor.restype = i
+    lib.zqs_project_sor_noalloc.argtypes = [vp, vp, vp, vp, i, i, i, i, i, f, vp]
+    lib.zqs_project_sor_noalloc.restype = i
     if path is None:
         _lib = lib
     return lib
