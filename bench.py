@@ -237,7 +237,7 @@ def run_ours(args):
     alg_bytes = SOR_BYTES_PER_CELL_ITER * depth * cells
     peak, peak_kind = load_peaks()
     achieved = alg_bytes / (sor_ms_per_launch * 1e-3) / 1e9
-    traffic = profile_traffic(f"k_sor_tb_{args.workload}")
+    traffic = profile_traffic(f"k_sor_{args.workload}") if args.sor_variant < 0 and args.sor_depth in (0, 2) else None
 
     # -- end to end through the C ABI with pinned host buffers --
     e2e = None
@@ -294,7 +294,7 @@ def run_ours(args):
                        "advection": "inMAC_outMAC + MAC scalar", "sor_depth": depth, "graph": True,
                        "l2": "working set %.2f GB > 129 MB L2, no flush" % (g.layout().field_elems * 4 * 21.25 / 1e9),
                        "parallelism": "replicas" if world > 1 else "single"},
-            "roofline": {"bound": "hbm", "kernel": "k_sor_tb", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "roofline": {"bound": "hbm", "kernel": "k_sor_reg", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "alg_bytes_per_launch": alg_bytes, "ms_per_launch": sor_ms_per_launch,
                          "step_alg_gbs": step_alg / (ms / args.steps * 1e-3) / 1e9,
