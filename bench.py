@@ -47,6 +47,10 @@ def parse():
     ap.add_argument("--cpu-sample", default="plain128", help="grid of the bounded CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--batch", default="batch64", help="mixed-size batch measured beside the plain step ('' = skip)")
+    ap.add_argument("--batch-steps", type=int, default=10)
+    ap.add_argument("--batch-variant", type=int, default=-1)
+    ap.add_argument("--batch-zchunk", type=int, default=0)
     return ap.parse_args()
 
 
@@ -163,6 +167,87 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def measure_batch(args, stream, rel_check: bool = True):
+    """The mixed-size batch: batched step (one persistent launch per stage,
+    one CUDA graph) against the same instances stepped one at a time
+    (zqs_grid_step per instance, each a CUDA graph of its own)."""
+    import numpy as np
+    import torch
+
+    from zq_smokesimulation_gb300 import capi
+    from zq_smokesimulation_gb300 import workloads as wl
+
+    n = int(args.batch[5:]) if args.batch.startswith("batch") and args.batch[5:].isdigit() else 64
+    cases = wl.batch_mixed(n)
+    sp = stream.cuda_stream
+    cells = sum(w.cells for w in cases)
+    K = cases[0].params.sor_iters
+
+    def grids():
+        out = []
+        for w in cases:
+            g = capi.Grid(w.W, w.H, w.D)
+            g.set_params(w.params)
+            g.load_state(w.occ, w.u, w.v, w.w, w.T, w.rho)
+            out.append(g)
+        return out
+
+    def timed(fn, steps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(stream)
+        for _ in range(steps):
+            fn()
+        b.record(stream)
+        b.synchronize()
+        return a.elapsed_time(b)
+
+    gb = grids()
+    batch = capi.Batch(gb)
+    batch.set_sor_variant(args.batch_variant, args.batch_zchunk)
+    batch.step(max(3, args.warmup), sp)
+    steps = max(1, args.batch_steps)
+    ms_b = timed(lambda: batch.step(1, sp), steps)
+    launches = batch.launch_count()
+    batch.sync(sp)
+
+    gs = grids()
+    for g in gs:
+        g.step(max(3, args.warmup), sp)
+    steps1 = max(1, min(steps, 5))
+    ms_1 = timed(lambda: [g.step(1, sp) for g in gs], steps1)
+    launches_1 = sum(g.launch_count() for g in gs)
+    torch.cuda.synchronize()
+    # both ran warmup + a different number of timed steps: compare members after
+    # bringing the one-at-a-time set to the same step count
+    extra = steps - steps1
+    for g in gs:
+        g.step(extra, sp)
+    torch.cuda.synchronize()
+    worst = 0.0
+    mism = 0
+    if rel_check:
+        for ga, gb_ in zip(gs, gb):
+            for f in (capi.FIELD_U, capi.FIELD_V, capi.FIELD_W, capi.FIELD_DENSITY):
+                x, y = ga.download(f), gb_.download(f)
+                den = float(np.linalg.norm(x.astype(np.float64)))
+                err = float(np.linalg.norm((x.astype(np.float64) - y))) / den if den > 0 else 0.0
+                worst = max(worst, err)
+                mism += int(np.count_nonzero(x != y))
+    batch.close()
+    for g in gb + gs:
+        g.close()
+    v_b = cells * steps / (ms_b * 1e-3) / 1e9
+    v_1 = cells * steps1 / (ms_1 * 1e-3) / 1e9
+    step_alg = (STEP_BYTES_FIXED + SOR_BYTES_PER_CELL_ITER * K) * cells
+    return {"workload": args.batch, "instances": n, "cells": cells, "sor_iters": K, "steps": steps,
+            "value": v_b, "unit": UNIT, "ms_per_step": ms_b / steps, "gpu_launches_per_step": launches,
+            "one_at_a_time": {"value": v_1, "ms_per_step": ms_1 / steps1, "steps": steps1,
+                              "gpu_launches_per_step": launches_1},
+            "speedup": v_b / v_1, "max_rel_l2_vs_one_at_a_time": worst, "mismatched_values": mism,
+            "step_alg_gbs": step_alg / (ms_b / steps * 1e-3) / 1e9}
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -270,6 +355,9 @@ def run_ours(args):
         e2e = {"value": world * cells * e2e_steps / (e2e_ms * 1e-3) / 1e9, "unit": UNIT,
                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                "path": "zqs_grid_upload x5 (pinned host) + zqs_grid_step + zqs_grid_download x5"}
+    batch = None
+    if args.batch and world == 1:
+        batch = measure_batch(args, stream)
     clocks = sampler.stop()
 
     if dist is not None:
@@ -300,6 +388,7 @@ def run_ours(args):
                          "step_alg_gbs": step_alg / (ms / args.steps * 1e-3) / 1e9,
                          "step_frac": step_alg / (ms / args.steps * 1e-3) / 1e9 / peak},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches_per_step * args.steps, "clocks": clocks,
+            "batch": batch,
         }
         print(json.dumps(line), flush=True)
     g.close()

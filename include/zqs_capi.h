@@ -210,6 +210,40 @@ ZQS_API int zqs_grid_synchronize(zqs_grid* g, void* stream);
 /* Kernel launches issued by the last zqs_grid_step call (for accounting). */
 ZQS_API int64_t zqs_grid_launch_count(const zqs_grid* g);
 
+/* ---- batched mixed-size instances -------------------------------------------
+ * A batch advances many independent grids together: each stage of the step is
+ * ONE persistent launch whose tile work list spans every member grid (sizes may
+ * differ), and the whole batched step is replayed as one CUDA graph.  No
+ * counterpart in the reference, which runs one grid per solver object
+ * (ZQ_SmokeSimulation3D.cpp:156, UpdateOneFrame steps a single fineGrid).
+ *
+ * The batch refers to the grids; it does not own them and they must outlive it.
+ * Every member must be ready (parameters and occupancy set), use the MAC
+ * velocity advection (ZQS_ADV_VEL_INMAC_OUTMAC) and MAC scalar advection
+ * (ZQS_ADV_SCA_MAC), and share sor_iters (ZQS_EUNSUPPORTED otherwise); other
+ * parameters (dt, forces, solver, sources, sizes) may differ per grid.  Each
+ * member ends in exactly the state zqs_grid_step would leave it in, bit for
+ * bit, and can be read back with zqs_grid_download.  Parameter, occupancy or
+ * SOR changes on a member, and steps taken on it alone, are picked up by the
+ * next zqs_batch_step. */
+typedef struct zqs_batch zqs_batch;
+
+ZQS_API int zqs_batch_create(zqs_batch** out, zqs_grid* const* grids, int n);
+ZQS_API int zqs_batch_destroy(zqs_batch* b);
+
+/* Advance every member nsteps steps on the stream (NULL: the batch's own). */
+ZQS_API int zqs_batch_step(zqs_batch* b, int nsteps, void* stream);
+ZQS_API int zqs_batch_use_graph(zqs_batch* b, int enable);
+
+/* Fused SOR variant of the batch (-1: default); it must be a register-column
+ * variant (ZQS_EUNSUPPORTED otherwise).  zchunk 0 lets the batch pick each
+ * member's z chunk for load balance; >0 forces it (clamped to each depth). */
+ZQS_API int zqs_batch_set_sor_variant(zqs_batch* b, int index, int zchunk);
+
+/* Kernel launches of one batched step (for accounting). */
+ZQS_API int64_t zqs_batch_launch_count(const zqs_batch* b);
+ZQS_API int zqs_batch_synchronize(zqs_batch* b, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

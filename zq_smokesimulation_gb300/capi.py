@@ -83,6 +83,8 @@ CAPI_SYMBOLS = [
     "zqs_stage_advect_velocity", "zqs_stage_project", "zqs_stage_advect_scalar", "zqs_stage_reinject",
     "zqs_grid_mac_to_regular4", "zqs_grid_stats", "zqs_grid_set_sor_config", "zqs_sor_variant_count",
     "zqs_sor_variant_info", "zqs_grid_set_sor_variant", "zqs_grid_synchronize", "zqs_grid_launch_count",
+    "zqs_batch_create", "zqs_batch_destroy", "zqs_batch_step", "zqs_batch_use_graph", "zqs_batch_set_sor_variant",
+    "zqs_batch_launch_count", "zqs_batch_synchronize",
 ]
 LEGACY_C_SYMBOLS = ["ZQ_Cuda_Prepare_Advection", "Advect_Velocity", "Advect_Scalar", "AddForce3D",
                     "Attenuation3D", "zqs_project_sor", "zqs_project_sor_noalloc"]
@@ -142,6 +144,14 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.zqs_sor_variant_count.restype = i
     lib.zqs_sor_variant_info.argtypes = [i, C.POINTER(SorVariant)]
     lib.zqs_grid_set_sor_variant.argtypes = [vp, i, i]
+    lib.zqs_batch_create.argtypes = [C.POINTER(vp), C.POINTER(vp), i]
+    lib.zqs_batch_destroy.argtypes = [vp]
+    lib.zqs_batch_step.argtypes = [vp, i, vp]
+    lib.zqs_batch_use_graph.argtypes = [vp, i]
+    lib.zqs_batch_set_sor_variant.argtypes = [vp, i, i]
+    lib.zqs_batch_launch_count.argtypes = [vp]
+    lib.zqs_batch_launch_count.restype = C.c_int64
+    lib.zqs_batch_synchronize.argtypes = [vp, vp]
     # legacy shims
     lib.ZQ_Cuda_Prepare_Advection.argtypes = [C.c_uint, C.c_uint, C.c_uint, f, C.c_uint, f]
     lib.ZQ_Cuda_Prepare_Advection.restype = None
@@ -337,3 +347,50 @@ class Grid:
 
     def launch_count(self) -> int:
         return int(self.lib.zqs_grid_launch_count(self.h))
+
+
+class Batch:
+    """Many grids advanced together (a zqs_batch handle): one persistent launch
+    per stage over all members' tiles, replayed as a CUDA graph.  The members
+    stay usable as Grid objects; after step() call sync() (or pass the stream
+    the members are read on) before downloading them."""
+
+    def __init__(self, grids: list[Grid]):
+        self.lib = load()
+        self.grids = list(grids)  # the handles must outlive the batch
+        arr = (C.c_void_p * len(self.grids))(*[g.h.value for g in self.grids])
+        h = C.c_void_p()
+        check(self.lib.zqs_batch_create(C.byref(h), arr, len(self.grids)), "zqs_batch_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            self.lib.zqs_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def step(self, n: int = 1, stream: int | None = None):
+        check(self.lib.zqs_batch_step(self.h, n, C.c_void_p(stream or 0)), "zqs_batch_step")
+
+    def use_graph(self, enable: bool):
+        check(self.lib.zqs_batch_use_graph(self.h, 1 if enable else 0), "zqs_batch_use_graph")
+
+    def set_sor_variant(self, index: int = -1, zchunk: int = 0):
+        check(self.lib.zqs_batch_set_sor_variant(self.h, index, zchunk), "zqs_batch_set_sor_variant")
+
+    def sync(self, stream: int | None = None):
+        check(self.lib.zqs_batch_synchronize(self.h, C.c_void_p(stream or 0)), "zqs_batch_synchronize")
+
+    def launch_count(self) -> int:
+        return int(self.lib.zqs_batch_launch_count(self.h))

@@ -14,7 +14,7 @@
 #include <string>
 #include <utility>
 
-#include "zqs_internal.h"
+#include "zqs_grid.h"
 
 namespace zqs {
 
@@ -97,71 +97,6 @@ int validate_params(const zqs_params& p) {
 }  // namespace zqs
 
 using namespace zqs;
-
-struct zqs_grid {
-    DevGrid g{};
-    void* base = nullptr;
-    uint8_t* occ_dense = nullptr;
-    cudaStream_t own = nullptr;
-    zqs_params params{};
-    bool has_params = false;
-    bool has_occ = false;
-    KParams kp{};
-    SourceList src{};
-    SorConfig sor{2, 0};
-    float* p_last = nullptr;
-    bool use_graph = true;
-    cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};
-    int vel_par = 0, sca_par = 0;   // which buffer of each ping-pong pair is current
-    long long step_launches = 0;
-    long long graph_launches[4] = {0, 0, 0, 0};
-    float* graph_p_last[4] = {nullptr, nullptr, nullptr, nullptr};
-
-    cudaStream_t pick(void* s) const { return s ? (cudaStream_t)s : own; }
-
-    void drop_graphs() {
-        for (int q = 0; q < 4; q++) {
-            if (graph[q]) cudaGraphExecDestroy(graph[q]);
-            graph[q] = nullptr;
-        }
-    }
-    void swap_velocity() {
-        std::swap(g.u, g.u2);
-        std::swap(g.v, g.v2);
-        std::swap(g.w, g.w2);
-        vel_par ^= 1;
-    }
-    void swap_scalars() {
-        std::swap(g.T, g.T2);
-        std::swap(g.rho, g.rho2);
-        sca_par ^= 1;
-    }
-    int ready() const {
-        if (!has_params) {
-            set_error("grid has no parameters (call zqs_grid_set_params)");
-            return ZQS_ENOTREADY;
-        }
-        if (!has_occ) {
-            set_error("grid has no occupancy (upload ZQS_FIELD_OCCUPANCY)");
-            return ZQS_ENOTREADY;
-        }
-        return ZQS_OK;
-    }
-    // The launches of one step, issued on stream s (captured or direct).
-    int issue_step(cudaStream_t s, LaunchCounter& lc) {
-        int rc = launch_force(g, kp, true, s, lc);
-        if (rc) return rc;
-        rc = launch_advect_velocity(g, kp, params.adv_vel_mode, true, s, lc);
-        if (rc) return rc;
-        swap_velocity();
-        rc = launch_project(g, kp, params.sor_iters, sor, s, lc, &p_last);
-        if (rc) return rc;
-        rc = launch_advect_scalar(g, kp, params.adv_sca_mode, true, &src, s, lc);
-        if (rc) return rc;
-        swap_scalars();
-        return ZQS_OK;
-    }
-};
 
 namespace zqs {
 // Internal hooks for the legacy shims (same library).

@@ -13,7 +13,9 @@
 // density attenuation factors (multiplying each interpolation corner, which is
 // what attenuating the field first computes) and the source reinjection of
 // ZQ_ReinjectTemperatureDensity3D (ZQ_SmokeSimulationUtils3D.cpp:3842-3882).
-#include "zqs_internal.h"
+#include <algorithm>
+
+#include "zqs_batch.h"
 
 namespace zqs {
 
@@ -188,20 +190,20 @@ __device__ __forceinline__ bool face_live(uint8_t fl, uint8_t bit, int idx, int 
     return open || (idx > 0 && idx < n);
 }
 
-// One thread per face: blockIdx.z = comp*(D+1) + k, comp 0/1/2 = u/v/w.
+// One thread per face: bz = comp*(D+1) + k, comp 0/1/2 = u/v/w.
 // REGIN selects the regular (cell-centre float4) velocity for both the
 // backtrace and the final sample (inRegular_outMAC), else MAC (inMAC_outMAC).
 template <bool REGIN>
-__global__ void __launch_bounds__(256) k_advect_vel_macout(Layout L, const float* __restrict__ u,
-                                                           const float* __restrict__ v, const float* __restrict__ w,
-                                                           const float4* __restrict__ vel4,
-                                                           const uint8_t* __restrict__ flags, float* __restrict__ u2,
-                                                           float* __restrict__ v2, float* __restrict__ w2, KParams kp,
-                                                           int open) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int comp = blockIdx.z / (L.D + 1);
-    const int k = blockIdx.z - comp * (L.D + 1);
+__device__ __forceinline__ void advect_vel_macout_tile(const Layout& L, const float* __restrict__ u,
+                                                       const float* __restrict__ v, const float* __restrict__ w,
+                                                       const float4* __restrict__ vel4,
+                                                       const uint8_t* __restrict__ flags, float* __restrict__ u2,
+                                                       float* __restrict__ v2, float* __restrict__ w2,
+                                                       const KParams& kp, int open, int bx, int by, int bz) {
+    const int i = bx * 32 + threadIdx.x;
+    const int j = by * 8 + threadIdx.y;
+    const int comp = bz / (L.D + 1);
+    const int k = bz - comp * (L.D + 1);
     int nx = L.W, ny = L.H, nz = L.D;
     if (comp == 0) nx++;
     else if (comp == 1) ny++;
@@ -232,6 +234,16 @@ __global__ void __launch_bounds__(256) k_advect_vel_macout(Layout L, const float
         }
     }
     dst[c] = out;
+}
+
+template <bool REGIN>
+__global__ void __launch_bounds__(256) k_advect_vel_macout(Layout L, const float* __restrict__ u,
+                                                           const float* __restrict__ v, const float* __restrict__ w,
+                                                           const float4* __restrict__ vel4,
+                                                           const uint8_t* __restrict__ flags, float* __restrict__ u2,
+                                                           float* __restrict__ v2, float* __restrict__ w2, KParams kp,
+                                                           int open) {
+    advect_vel_macout_tile<REGIN>(L, u, v, w, vel4, flags, u2, v2, w2, kp, open, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 // Advect_Velocity_inRegular_outRegular_Kernel (Adv3D:76-113): per cell.
@@ -310,16 +322,16 @@ __device__ __forceinline__ void reinject_cell(const SourceList& src, int i, int 
 // attenuation factors applied to the interpolation corners and the sources
 // reinjected in the epilogue.
 template <bool REGIN>
-__global__ void __launch_bounds__(256) k_advect_scalar(Layout L, const float* __restrict__ u,
-                                                       const float* __restrict__ v, const float* __restrict__ w,
-                                                       const float4* __restrict__ vel4,
-                                                       const uint8_t* __restrict__ flags,
-                                                       const float* __restrict__ T, const float* __restrict__ rho,
-                                                       float* __restrict__ T2, float* __restrict__ rho2, KParams kp,
-                                                       float aT, float aD, SourceList src) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = blockIdx.z;
+__device__ __forceinline__ void advect_scalar_tile(const Layout& L, const float* __restrict__ u,
+                                                   const float* __restrict__ v, const float* __restrict__ w,
+                                                   const float4* __restrict__ vel4, const uint8_t* __restrict__ flags,
+                                                   const float* __restrict__ T, const float* __restrict__ rho,
+                                                   float* __restrict__ T2, float* __restrict__ rho2,
+                                                   const KParams& kp, float aT, float aD, const SourceList& src,
+                                                   int bx, int by, int bz) {
+    const int i = bx * 32 + threadIdx.x;
+    const int j = by * 8 + threadIdx.y;
+    const int k = bz;
     if (i >= L.W || j >= L.H || k >= L.D) return;
     float px = (float)i + 0.5f, py = (float)j + 0.5f, pz = (float)k + 0.5f;
     if (REGIN) {
@@ -336,6 +348,49 @@ __global__ void __launch_bounds__(256) k_advect_scalar(Layout L, const float* __
     const int c = lidx(L, i, j, k);
     T2[c] = t;
     rho2[c] = d;
+}
+
+template <bool REGIN>
+__global__ void __launch_bounds__(256) k_advect_scalar(Layout L, const float* __restrict__ u,
+                                                       const float* __restrict__ v, const float* __restrict__ w,
+                                                       const float4* __restrict__ vel4,
+                                                       const uint8_t* __restrict__ flags,
+                                                       const float* __restrict__ T, const float* __restrict__ rho,
+                                                       float* __restrict__ T2, float* __restrict__ rho2, KParams kp,
+                                                       float aT, float aD, SourceList src) {
+    advect_scalar_tile<REGIN>(L, u, v, w, vel4, flags, T, rho, T2, rho2, kp, aT, aD, src, blockIdx.x, blockIdx.y,
+                              blockIdx.z);
+}
+
+// ---- batched forms (MAC velocity) ----
+
+__global__ void __launch_bounds__(256) k_advect_vel_batch(BatchLaunch B, int vcur) {
+    for (int t = blockIdx.x; t < B.total; t += gridDim.x) {
+        const int i = batch_find(B.pre, B.n, t);
+        const InstDesc& d = B.desc[i];
+        const int lt = t - __ldg(B.pre + i);
+        const int gx = (d.L.W + 1 + 31) / 32, gy = (d.L.H + 1 + 7) / 8;
+        const int bx = lt % gx, r = lt / gx, by = r % gy, bz = r / gy;
+        const KParams kp = d.kp;
+        const int nxt = vcur ^ 1;
+        advect_vel_macout_tile<false>(d.L, d.vel[vcur][0], d.vel[vcur][1], d.vel[vcur][2], d.t4a, d.flags,
+                                      d.vel[nxt][0], d.vel[nxt][1], d.vel[nxt][2], kp, 1, bx, by, bz);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_advect_scalar_batch(BatchLaunch B, int vcur, int scur) {
+    for (int t = blockIdx.x; t < B.total; t += gridDim.x) {
+        const int i = batch_find(B.pre, B.n, t);
+        const InstDesc& d = B.desc[i];
+        const int lt = t - __ldg(B.pre + i);
+        const int gx = (d.L.W + 31) / 32, gy = (d.L.H + 7) / 8;
+        const int bx = lt % gx, r = lt / gx, by = r % gy, bz = r / gy;
+        const KParams kp = d.kp;
+        const int nxt = scur ^ 1;
+        advect_scalar_tile<false>(d.L, d.vel[vcur][0], d.vel[vcur][1], d.vel[vcur][2], d.t4a, d.flags,
+                                  d.sca[scur][0], d.sca[scur][1], d.sca[nxt][0], d.sca[nxt][1], kp, kp.temp_atten,
+                                  kp.dens_atten, d.src, bx, by, bz);
+    }
 }
 
 __global__ void k_reinject(Layout L, float* __restrict__ T, float* __restrict__ rho, SourceList src) {
@@ -409,6 +464,23 @@ int launch_advect_scalar(const DevGrid& g, const KParams& kp, int mode, bool fol
     }
     lc.n++;
     ZQS_LAUNCH_CHECK("k_advect_scalar");
+    return ZQS_OK;
+}
+
+int launch_advect_velocity_batch(const BatchLaunch& advf, int vcur, int blocks, cudaStream_t s, LaunchCounter& lc) {
+    dim3 b(32, 8, 1);
+    k_advect_vel_batch<<<std::min(blocks, advf.total), b, 0, s>>>(advf, vcur);
+    lc.n++;
+    ZQS_LAUNCH_CHECK("k_advect_vel_batch");
+    return ZQS_OK;
+}
+
+int launch_advect_scalar_batch(const BatchLaunch& cell, int vcur, int scur, int blocks, cudaStream_t s,
+                               LaunchCounter& lc) {
+    dim3 b(32, 8, 1);
+    k_advect_scalar_batch<<<std::min(blocks, cell.total), b, 0, s>>>(cell, vcur, scur);
+    lc.n++;
+    ZQS_LAUNCH_CHECK("k_advect_scalar_batch");
     return ZQS_OK;
 }
 

@@ -3,12 +3,16 @@
 // Restates cu_AddForce3D (ZQ_CUDA_AddForce3D.cu:510-556) and Attenuation3D
 // (ZQ_CUDA_Attenuation3D.cu:8-116) on the padded device layout.  Three
 // launches replace the reference's five kernels and seven allocations:
-//   k_vorticity    faces -> (wx, wy, wz, |w|) per cell        (:11-34)
-//   k_force_cell   |w| halo + w + T + rho -> force per cell    (:64-111, :161-184)
-//   k_force_faces  force -> face update, velocity attenuation fused (:211-385)
+//   vorticity    faces -> (wx, wy, wz, |w|) per cell        (:11-34)
+//   force_cell   |w| halo + w + T + rho -> force per cell    (:64-111, :161-184)
+//   force_faces  force -> face update, velocity attenuation fused (:211-385)
 // The expression order of every float operation matches the oracle
 // (oracle/zqs_oracle.cpp, add_force/attenuate) so FP32 results agree exactly.
-#include "zqs_internal.h"
+// Each stage is a tile function over one 32x8 block of (i,j) at plane k,
+// launched directly for one grid or through the batch work list.
+#include <algorithm>
+
+#include "zqs_batch.h"
 
 namespace zqs {
 
@@ -26,11 +30,12 @@ __device__ __forceinline__ float ctr_w(const float* __restrict__ w, int c, int p
 
 // Vorticity of the cell-centre velocity on cells with every index in [1,N-2]
 // (ZQ_CUDA_AddForce3D.cu:11-34); other cells get 0 as the reference memsets.
-__global__ void k_vorticity(Layout L, const float* __restrict__ u, const float* __restrict__ v,
-                            const float* __restrict__ w, float4* __restrict__ vort, float twoh) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    int j = blockIdx.y * blockDim.y + threadIdx.y;
-    int k = blockIdx.z;
+__device__ __forceinline__ void vorticity_tile(const Layout& L, const float* __restrict__ u,
+                                               const float* __restrict__ v, const float* __restrict__ w,
+                                               float4* __restrict__ vort, float twoh, int bx, int by, int bz) {
+    int i = bx * 32 + threadIdx.x;
+    int j = by * 8 + threadIdx.y;
+    int k = bz;
     if (i >= L.W || j >= L.H || k >= L.D) return;
     const int c = lidx(L, i, j, k);
     const int px = L.px, pl = (int)L.plane;
@@ -49,11 +54,13 @@ __global__ void k_vorticity(Layout L, const float* __restrict__ u, const float* 
 
 // N = normalised gradient of |w| (ZQ_CUDA_AddForce3D.cu:64-111) and
 // f = (eps*h)*(N x w); f_y += beta*(T-Tamb); f_y -= alpha*rho (:161-184).
-__global__ void k_force_cell(Layout L, const float4* __restrict__ vort, const float* __restrict__ T,
-                             const float* __restrict__ rho, float4* __restrict__ force, KParams kp) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    int j = blockIdx.y * blockDim.y + threadIdx.y;
-    int k = blockIdx.z;
+__device__ __forceinline__ void force_cell_tile(const Layout& L, const float4* __restrict__ vort,
+                                                const float* __restrict__ T, const float* __restrict__ rho,
+                                                float4* __restrict__ force, const KParams& kp, int bx, int by,
+                                                int bz) {
+    int i = bx * 32 + threadIdx.x;
+    int j = by * 8 + threadIdx.y;
+    int k = bz;
     if (i >= L.W || j >= L.H || k >= L.D) return;
     const int c = lidx(L, i, j, k);
     const int px = L.px, pl = (int)L.plane;
@@ -87,11 +94,13 @@ __global__ void k_force_cell(Layout L, const float4* __restrict__ vort, const fl
 // ATTEN also multiplies live faces by vel_atten, which is the next stage of
 // the reference step (ZQ_CUDA_Attenuation3D.cu:8-98) applied to the same faces.
 template <bool ATTEN>
-__global__ void k_force_faces(Layout L, float* __restrict__ u, float* __restrict__ v, float* __restrict__ w,
-                              const uint8_t* __restrict__ flags, const float4* __restrict__ force, KParams kp) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    int j = blockIdx.y * blockDim.y + threadIdx.y;
-    int k = blockIdx.z;
+__device__ __forceinline__ void force_faces_tile(const Layout& L, float* __restrict__ u, float* __restrict__ v,
+                                                 float* __restrict__ w, const uint8_t* __restrict__ flags,
+                                                 const float4* __restrict__ force, const KParams& kp, int bx,
+                                                 int by, int bz) {
+    int i = bx * 32 + threadIdx.x;
+    int j = by * 8 + threadIdx.y;
+    int k = bz;
     if (i > L.W || j > L.H || k > L.D) return;
     const int c = lidx(L, i, j, k);
     const int px = L.px, pl = (int)L.plane;
@@ -124,6 +133,22 @@ __global__ void k_force_faces(Layout L, float* __restrict__ u, float* __restrict
     }
 }
 
+__global__ void k_vorticity(Layout L, const float* __restrict__ u, const float* __restrict__ v,
+                            const float* __restrict__ w, float4* __restrict__ vort, float twoh) {
+    vorticity_tile(L, u, v, w, vort, twoh, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+__global__ void k_force_cell(Layout L, const float4* __restrict__ vort, const float* __restrict__ T,
+                             const float* __restrict__ rho, float4* __restrict__ force, KParams kp) {
+    force_cell_tile(L, vort, T, rho, force, kp, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+template <bool ATTEN>
+__global__ void k_force_faces(Layout L, float* __restrict__ u, float* __restrict__ v, float* __restrict__ w,
+                              const uint8_t* __restrict__ flags, const float4* __restrict__ force, KParams kp) {
+    force_faces_tile<ATTEN>(L, u, v, w, flags, force, kp, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
 // Attenuation3D as a stage of its own (ZQ_CUDA_Attenuation3D.cu:8-116).
 __global__ void k_attenuate(Layout L, float* __restrict__ u, float* __restrict__ v, float* __restrict__ w,
                             float* __restrict__ T, float* __restrict__ rho, const uint8_t* __restrict__ flags,
@@ -140,6 +165,49 @@ __global__ void k_attenuate(Layout L, float* __restrict__ u, float* __restrict__
     if (i < L.W && j < L.H && k < L.D) {
         T[c] = T[c] * kp.temp_atten;
         rho[c] = rho[c] * kp.dens_atten;
+    }
+}
+
+// ---- batched forms: one persistent launch over every instance's tiles ----
+
+__device__ __forceinline__ void tile_coords(const Layout& L, int lt, int wx, int wy, int& bx, int& by, int& bz) {
+    const int gx = (wx + 31) / 32, gy = (wy + 7) / 8;
+    bx = lt % gx;
+    const int r = lt / gx;
+    by = r % gy;
+    bz = r / gy;
+}
+
+__global__ void k_vorticity_batch(BatchLaunch B, int vcur) {
+    for (int t = blockIdx.x; t < B.total; t += gridDim.x) {
+        const int i = batch_find(B.pre, B.n, t);
+        const InstDesc& d = B.desc[i];
+        int bx, by, bz;
+        tile_coords(d.L, t - __ldg(B.pre + i), d.L.W, d.L.H, bx, by, bz);
+        vorticity_tile(d.L, d.vel[vcur][0], d.vel[vcur][1], d.vel[vcur][2], d.t4a, d.kp.twoh, bx, by, bz);
+    }
+}
+
+__global__ void k_force_cell_batch(BatchLaunch B, int scur) {
+    for (int t = blockIdx.x; t < B.total; t += gridDim.x) {
+        const int i = batch_find(B.pre, B.n, t);
+        const InstDesc& d = B.desc[i];
+        int bx, by, bz;
+        tile_coords(d.L, t - __ldg(B.pre + i), d.L.W, d.L.H, bx, by, bz);
+        const KParams kp = d.kp;
+        force_cell_tile(d.L, d.t4a, d.sca[scur][0], d.sca[scur][1], d.t4b, kp, bx, by, bz);
+    }
+}
+
+__global__ void k_force_faces_batch(BatchLaunch B, int vcur) {
+    for (int t = blockIdx.x; t < B.total; t += gridDim.x) {
+        const int i = batch_find(B.pre, B.n, t);
+        const InstDesc& d = B.desc[i];
+        int bx, by, bz;
+        tile_coords(d.L, t - __ldg(B.pre + i), d.L.W + 1, d.L.H + 1, bx, by, bz);
+        const KParams kp = d.kp;
+        force_faces_tile<true>(d.L, d.vel[vcur][0], d.vel[vcur][1], d.vel[vcur][2], d.flags, d.t4b, kp, bx, by,
+                               bz);
     }
 }
 
@@ -166,6 +234,17 @@ int launch_attenuate(const DevGrid& g, const KParams& kp, cudaStream_t s, Launch
     k_attenuate<<<gf, b, 0, s>>>(L, g.u, g.v, g.w, g.T, g.rho, g.flags, kp);
     lc.n++;
     ZQS_LAUNCH_CHECK("k_attenuate");
+    return ZQS_OK;
+}
+
+int launch_force_batch(const BatchLaunch& cell, const BatchLaunch& face, int vcur, int scur, int blocks,
+                       cudaStream_t s, LaunchCounter& lc) {
+    dim3 b(32, 8, 1);
+    k_vorticity_batch<<<std::min(blocks, cell.total), b, 0, s>>>(cell, vcur);
+    k_force_cell_batch<<<std::min(blocks, cell.total), b, 0, s>>>(cell, scur);
+    k_force_faces_batch<<<std::min(blocks, face.total), b, 0, s>>>(face, vcur);
+    lc.n += 3;
+    ZQS_LAUNCH_CHECK("batched force kernels");
     return ZQS_OK;
 }
 

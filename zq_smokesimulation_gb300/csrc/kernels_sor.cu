@@ -26,7 +26,7 @@
 //                 the two-plane lag lets all S half-sweeps of a step run at once
 //                 with one barrier per step, and every value each reads is at the
 //                 right sweep.  Results equal S/2 iterations of k_sor_colour.
-#include "zqs_internal.h"
+#include "zqs_batch.h"
 
 #include <algorithm>
 #include <vector>
@@ -35,12 +35,16 @@ namespace zqs {
 
 namespace {
 
-__global__ void k_divergence(Layout L, const float* __restrict__ u, const float* __restrict__ v,
-                             const float* __restrict__ w, const uint8_t* __restrict__ flags, float* __restrict__ div,
-                             float* __restrict__ p, double* __restrict__ part, int want_partials) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = blockIdx.z;
+// Divergence of one 32x8 block at plane bz; with want_partials the block's FP64
+// sum and free-cell count go to part[2*blk], part[2*blk+1].
+__device__ __forceinline__ void divergence_tile(const Layout& L, const float* __restrict__ u,
+                                                const float* __restrict__ v, const float* __restrict__ w,
+                                                const uint8_t* __restrict__ flags, float* __restrict__ div,
+                                                float* __restrict__ p, double* __restrict__ part, int want_partials,
+                                                int bx, int by, int bz, long long blk) {
+    const int i = bx * 32 + threadIdx.x;
+    const int j = by * 8 + threadIdx.y;
+    const int k = bz;
     double sum = 0.0, cnt = 0.0;
     if (i < L.W && j < L.H && k < L.D) {
         const int c = lidx(L, i, j, k);
@@ -69,11 +73,18 @@ __global__ void k_divergence(Layout L, const float* __restrict__ u, const float*
             __syncthreads();
         }
         if (t == 0) {
-            long long b = ((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
-            part[2 * b] = ss[0];
-            part[2 * b + 1] = sc[0];
+            part[2 * blk] = ss[0];
+            part[2 * blk + 1] = sc[0];
         }
+        __syncthreads();  // the shared partials are reused by the next tile of a persistent block
     }
+}
+
+__global__ void k_divergence(Layout L, const float* __restrict__ u, const float* __restrict__ v,
+                             const float* __restrict__ w, const uint8_t* __restrict__ flags, float* __restrict__ div,
+                             float* __restrict__ p, double* __restrict__ part, int want_partials) {
+    const long long blk = ((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+    divergence_tile(L, u, v, w, flags, div, p, part, want_partials, blockIdx.x, blockIdx.y, blockIdx.z, blk);
 }
 
 // Single block: sums the partials in a fixed order, stores the mean in out[0].
@@ -327,18 +338,22 @@ struct RegShape {
     static constexpr size_t smem = (size_t)NP * 2 * CA * (4 + 4);
 };
 
+// One CTA tile (bx, by) of TX x TY columns and z chunk bz; every thread of the
+// block takes part (barriers inside), and the last step ends with a barrier,
+// so a persistent block may run the next tile on the same shared memory.
 template <int S, int TX, int TY, int PPT>
-__global__ void __launch_bounds__(RegShape<S, TX, TY, PPT>::NT)
-    k_sor_reg(Layout L, const float* __restrict__ pin, float* __restrict__ pout, const float* __restrict__ div,
-              const uint8_t* __restrict__ flags, float omega, float om1, int zc) {
+__device__ __forceinline__ void sor_reg_tile(const Layout& L, const float* __restrict__ pin,
+                                             float* __restrict__ pout, const float* __restrict__ div,
+                                             const uint8_t* __restrict__ flags, float omega, float om1, int zc,
+                                             int bx, int by, int bz) {
     using Sh = RegShape<S, TX, TY, PPT>;
     constexpr int PW = Sh::PW, NP = Sh::NP, CA = Sh::CA, NT = Sh::NT;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float* sp = reinterpret_cast<float*>(smem_raw);  // [NP][2][CA] published pressure
     float* sd = sp + NP * 2 * CA;                      // [NP][2][CA] divergence
 
-    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
-    const int z0 = blockIdx.z * zc;
+    const int x0 = bx * TX, y0 = by * TY;
+    const int z0 = bz * zc;
     const int z1 = min(z0 + zc, L.D);
     const int plane = (int)L.plane;
 
@@ -475,6 +490,31 @@ __global__ void __launch_bounds__(RegShape<S, TX, TY, PPT>::NT)
                 __syncthreads();
             }
         }
+    }
+}
+
+template <int S, int TX, int TY, int PPT>
+__global__ void __launch_bounds__(RegShape<S, TX, TY, PPT>::NT)
+    k_sor_reg(Layout L, const float* __restrict__ pin, float* __restrict__ pout, const float* __restrict__ div,
+              const uint8_t* __restrict__ flags, float omega, float om1, int zc) {
+    sor_reg_tile<S, TX, TY, PPT>(L, pin, pout, div, flags, omega, om1, zc, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+// Persistent batched pass: tile t of the flat SOR tile space belongs to the
+// instance found in the prefix array; pressure goes p[pcur] -> p[pcur^1], z
+// chunk zc[which].
+template <int S, int TX, int TY, int PPT>
+__global__ void __launch_bounds__(RegShape<S, TX, TY, PPT>::NT)
+    k_sor_reg_batch(BatchLaunch B, int pcur, int which) {
+    for (int t = blockIdx.x; t < B.total; t += gridDim.x) {
+        const int i = batch_find(B.pre, B.n, t);
+        const InstDesc& d = B.desc[i];
+        const int local = t - __ldg(B.pre + i);
+        const int tx = (d.L.W + TX - 1) / TX, ty = (d.L.H + TY - 1) / TY;
+        const int bx = local % tx, r = local / tx;
+        const int by = r % ty, bz = r / ty;
+        sor_reg_tile<S, TX, TY, PPT>(d.L, d.p[pcur], d.p[pcur ^ 1], d.div, d.flags, d.kp.omega, d.kp.om1,
+                                     d.zc[which], bx, by, bz);
     }
 }
 
@@ -696,11 +736,12 @@ __global__ void __launch_bounds__(QuadShape<S, TX, TY>::NT)
 }
 
 // u -= p_R - p_L on live faces; OPEN also updates domain faces with p = 0 outside.
-__global__ void k_gradient(Layout L, float* __restrict__ u, float* __restrict__ v, float* __restrict__ w,
-                           const float* __restrict__ p, const uint8_t* __restrict__ flags, int open) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = blockIdx.z;
+__device__ __forceinline__ void gradient_tile(const Layout& L, float* __restrict__ u, float* __restrict__ v,
+                                              float* __restrict__ w, const float* __restrict__ p,
+                                              const uint8_t* __restrict__ flags, int open, int bx, int by, int bz) {
+    const int i = bx * 32 + threadIdx.x;
+    const int j = by * 8 + threadIdx.y;
+    const int k = bz;
     if (i > L.W || j > L.H || k > L.D) return;
     const int c = lidx(L, i, j, k);
     const int px = L.px, pl = (int)L.plane;
@@ -779,6 +820,93 @@ __global__ void k_stats(Layout L, const float* __restrict__ u, const float* __re
     }
 }
 
+__global__ void k_gradient(Layout L, float* __restrict__ u, float* __restrict__ v, float* __restrict__ w,
+                           const float* __restrict__ p, const uint8_t* __restrict__ flags, int open) {
+    gradient_tile(L, u, v, w, p, flags, open, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+// ---- batched forms: one persistent launch over every instance's tiles ----
+
+__device__ __forceinline__ void block_coords(int lt, int wx, int wy, int& bx, int& by, int& bz) {
+    const int gx = (wx + 31) / 32, gy = (wy + 7) / 8;
+    bx = lt % gx;
+    const int r = lt / gx;
+    by = r % gy;
+    bz = r / gy;
+}
+
+// Divergence of every instance into div and p[0] = 0; closed instances write
+// their block partials to red in the single-grid block order.
+__global__ void k_divergence_batch(BatchLaunch B, int vcur) {
+    for (int t = blockIdx.x; t < B.total; t += gridDim.x) {
+        const int i = batch_find(B.pre, B.n, t);
+        const InstDesc& d = B.desc[i];
+        const int lt = t - __ldg(B.pre + i);
+        int bx, by, bz;
+        block_coords(lt, d.L.W, d.L.H, bx, by, bz);
+        divergence_tile(d.L, d.vel[vcur][0], d.vel[vcur][1], d.vel[vcur][2], d.flags, d.div, d.p[0], d.red,
+                        d.closed, bx, by, bz, lt);
+    }
+}
+
+// One block per instance: the closed-solver mean of its partials (the
+// reduction k_reduce_mean performs, same order).
+__global__ void k_reduce_mean_batch(const InstDesc* __restrict__ desc, const int* __restrict__ cell_pre) {
+    const InstDesc& d = desc[blockIdx.x];
+    if (!d.closed || d.kp.mean_override) return;
+    const long long nblocks = cell_pre[blockIdx.x + 1] - cell_pre[blockIdx.x];
+    const double* part = d.red;
+    __shared__ double ss[256], sc[256];
+    double s = 0.0, c = 0.0;
+    for (long long b = threadIdx.x; b < nblocks; b += 256) {
+        s += part[2 * b];
+        c += part[2 * b + 1];
+    }
+    ss[threadIdx.x] = s;
+    sc[threadIdx.x] = c;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) {
+            ss[threadIdx.x] += ss[threadIdx.x + o];
+            sc[threadIdx.x] += sc[threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        double* out = d.red + d.red_len - 2;
+        out[0] = sc[0] > 0.0 ? ss[0] / sc[0] : 0.0;
+        out[1] = sc[0];
+    }
+}
+
+__global__ void k_div_subtract_batch(BatchLaunch B) {
+    for (int t = blockIdx.x; t < B.total; t += gridDim.x) {
+        const int n = batch_find(B.pre, B.n, t);
+        const InstDesc& d = B.desc[n];
+        if (!d.closed) continue;
+        int bx, by, bz;
+        block_coords(t - __ldg(B.pre + n), d.L.W, d.L.H, bx, by, bz);
+        const int i = bx * 32 + threadIdx.x, j = by * 8 + threadIdx.y, k = bz;
+        if (i >= d.L.W || j >= d.L.H || k >= d.L.D) continue;
+        const int c = lidx(d.L, i, j, k);
+        if (__ldg(d.flags + c) & F_FREE) {
+            const float m = d.kp.mean_override ? d.kp.mean_value : (float)d.red[d.red_len - 2];
+            d.div[c] = d.div[c] - m;
+        }
+    }
+}
+
+__global__ void k_gradient_batch(BatchLaunch B, int vcur, int pfin) {
+    for (int t = blockIdx.x; t < B.total; t += gridDim.x) {
+        const int i = batch_find(B.pre, B.n, t);
+        const InstDesc& d = B.desc[i];
+        int bx, by, bz;
+        block_coords(t - __ldg(B.pre + i), d.L.W + 1, d.L.H + 1, bx, by, bz);
+        gradient_tile(d.L, d.vel[vcur][0], d.vel[vcur][1], d.vel[vcur][2], d.p[pfin], d.flags, d.closed ? 0 : 1, bx,
+                      by, bz);
+    }
+}
+
 // ---------------------------------------------------------------- host side
 
 struct RbVariant {
@@ -788,6 +916,10 @@ struct RbVariant {
     cudaError_t (*launch)(dim3, const Layout&, const float*, float*, const float*, const uint8_t*, float, float, int,
                           cudaStream_t);
     const void* fn;
+    // batched persistent form (register-column variants only)
+    cudaError_t (*launch_batch)(int, const BatchLaunch&, int, int, cudaStream_t);
+    const void* fn_batch;
+    int ctas_per_sm_batch;
 };
 
 template <int S, int TX, int TY, int PPT>
@@ -810,6 +942,9 @@ RbVariant rb_variant() {
     v.smem = Sh::smem;
     v.ctas_per_sm = 0;
     v.launch = &rb_launch<S, TX, TY, PPT>;
+    v.launch_batch = nullptr;
+    v.fn_batch = nullptr;
+    v.ctas_per_sm_batch = 0;
     v.fn = (const void*)k_sor_rb<S, TX, TY, PPT>;
     return v;
 }
@@ -819,6 +954,13 @@ cudaError_t reg_launch(dim3 gr, const Layout& L, const float* pin, float* pout, 
                        const uint8_t* flags, float omega, float om1, int zc, cudaStream_t st) {
     using Sh = RegShape<S, TX, TY, PPT>;
     k_sor_reg<S, TX, TY, PPT><<<gr, Sh::NT, Sh::smem, st>>>(L, pin, pout, div, flags, omega, om1, zc);
+    return cudaGetLastError();
+}
+
+template <int S, int TX, int TY, int PPT>
+cudaError_t reg_launch_batch(int blocks, const BatchLaunch& B, int pcur, int which, cudaStream_t st) {
+    using Sh = RegShape<S, TX, TY, PPT>;
+    k_sor_reg_batch<S, TX, TY, PPT><<<blocks, Sh::NT, Sh::smem, st>>>(B, pcur, which);
     return cudaGetLastError();
 }
 
@@ -835,6 +977,9 @@ RbVariant reg_variant() {
     v.ctas_per_sm = 0;
     v.launch = &reg_launch<S, TX, TY, PPT>;
     v.fn = (const void*)k_sor_reg<S, TX, TY, PPT>;
+    v.launch_batch = &reg_launch_batch<S, TX, TY, PPT>;
+    v.fn_batch = (const void*)k_sor_reg_batch<S, TX, TY, PPT>;
+    v.ctas_per_sm_batch = 0;
     return v;
 }
 
@@ -858,6 +1003,9 @@ RbVariant quad_variant() {
     v.smem = Sh::smem;
     v.ctas_per_sm = 0;
     v.launch = &quad_launch<S, TX, TY>;
+    v.launch_batch = nullptr;
+    v.fn_batch = nullptr;
+    v.ctas_per_sm_batch = 0;
     v.fn = (const void*)k_sor_quad<S, TX, TY>;
     return v;
 }
@@ -870,6 +1018,8 @@ RbVariant g_var[kNumVariants];
 // default variant per depth 1..4
 // (measured at 256^3 on GB300: register-column 64x16 at depth 2 is fastest)
 const int kDefaultVariant[5] = {-1, 16, 13, 15, 7};
+// batched default: register-column 32x16 at depth 2 (small tiles suit 32..128 edges)
+const int kBatchDefaultVariant = 12;
 int g_num_sms = 0;
 int g_prepared = 0;
 
@@ -929,6 +1079,13 @@ int sor_prepare() {
         int n = 0;
         ZQS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, v.fn, v.nt, v.smem));
         v.ctas_per_sm = n;  // 0: does not fit (never selected)
+        if (v.fn_batch) {
+            ZQS_CUDA_TRY(
+                cudaFuncSetAttribute(v.fn_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)v.smem));
+            n = 0;
+            ZQS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, v.fn_batch, v.nt, v.smem));
+            v.ctas_per_sm_batch = n;
+        }
     }
     g_prepared = 1;
     return ZQS_OK;
@@ -1011,6 +1168,77 @@ int launch_project(DevGrid& g, const KParams& kp, int K, const SorConfig& cfg, c
     lc.n++;
     ZQS_LAUNCH_CHECK("k_gradient");
     if (p_final) *p_final = cur;
+    return ZQS_OK;
+}
+
+bool sor_variant_batchable(int variant) {
+    if (sor_prepare() != ZQS_OK) return false;
+    return variant >= 0 && variant < kNumVariants && g_var[variant].launch_batch &&
+           g_var[variant].ctas_per_sm_batch > 0;
+}
+
+int sor_batch_plan(int variant, SorBatchPlan& out) {
+    int rc = sor_prepare();
+    if (rc) return rc;
+    const int vm = variant >= 0 ? variant : kBatchDefaultVariant;
+    if (!sor_variant_batchable(vm)) {
+        set_error("SOR variant " + std::to_string(vm) + " has no batched form on this device");
+        return ZQS_EUNSUPPORTED;
+    }
+    // remainder: the depth-1 register-column variant with the same tile, else the first depth-1 one
+    int vr = -1;
+    for (int i = 0; i < kNumVariants && vr < 0; i++)
+        if (sor_variant_batchable(i) && g_var[i].S == 2 && g_var[i].TX == g_var[vm].TX &&
+            g_var[i].TY == g_var[vm].TY && g_var[i].ppt == g_var[vm].ppt)
+            vr = i;
+    for (int i = 0; i < kNumVariants && vr < 0; i++)
+        if (sor_variant_batchable(i) && g_var[i].S == 2) vr = i;
+    if (vr < 0) {
+        set_error("no depth-1 batched SOR variant fits this device");
+        return ZQS_EUNSUPPORTED;
+    }
+    out.vmain = vm;
+    out.vrem = vr;
+    const int v2[2] = {vm, vr};
+    for (int q = 0; q < 2; q++) {
+        out.S[q] = g_var[v2[q]].S;
+        out.TX[q] = g_var[v2[q]].TX;
+        out.TY[q] = g_var[v2[q]].TY;
+        out.slots[q] = g_num_sms * g_var[v2[q]].ctas_per_sm_batch;
+    }
+    return ZQS_OK;
+}
+
+int launch_project_batch(const BatchLaunch& cell, const BatchLaunch& face, const BatchLaunch& sorm,
+                         const BatchLaunch& sorr, const SorBatchPlan& plan, int K, bool any_closed, int vcur,
+                         int blocks, cudaStream_t s, LaunchCounter& lc, int* pfin) {
+    dim3 b(32, 8, 1);
+    k_divergence_batch<<<std::min(blocks, cell.total), b, 0, s>>>(cell, vcur);
+    lc.n++;
+    if (any_closed) {
+        k_reduce_mean_batch<<<cell.n, 256, 0, s>>>(cell.desc, cell.pre);
+        k_div_subtract_batch<<<std::min(blocks, cell.total), b, 0, s>>>(cell);
+        lc.n += 2;
+    }
+    ZQS_LAUNCH_CHECK("batched divergence");
+    int pcur = 0;
+    const int dmain = plan.S[0] / 2;
+    int remaining = K;
+    while (remaining > 0) {
+        const int which = remaining >= dmain ? 0 : 1;
+        const RbVariant& v = g_var[which == 0 ? plan.vmain : plan.vrem];
+        const BatchLaunch& B = which == 0 ? sorm : sorr;
+        const int d = which == 0 ? dmain : 1;
+        cudaError_t e = v.launch_batch(std::min(plan.slots[which], B.total), B, pcur, which, s);
+        if (e != cudaSuccess) return cuda_fail(e, "k_sor_reg_batch");
+        lc.n++;
+        pcur ^= 1;
+        remaining -= d;
+    }
+    k_gradient_batch<<<std::min(blocks, face.total), b, 0, s>>>(face, vcur, pcur);
+    lc.n++;
+    ZQS_LAUNCH_CHECK("k_gradient_batch");
+    if (pfin) *pfin = pcur;
     return ZQS_OK;
 }
 

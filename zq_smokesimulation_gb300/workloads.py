@@ -15,6 +15,11 @@ Named configurations (cell units, y is up, gravity along -y):
                  centre x,z~U[r+1, N-r-1], y~U[1, 0.1N], density and temperature
                  ~U[.5,1]; K=600
   plain512       the same at 512^3
+  batch64        64 independent instances, edges from {32,48,64,96,128}, each
+                 cubic or with one axis doubled; per instance a seeded sphere
+                 source (r ~ U[.06,.12] x the shortest edge, in the bottom 15%),
+                 alpha ~ U[.05,.2], beta ~ U[.2,.8], eps ~ U[0,.3],
+                 dt ~ U[.25,.75]; K=200, 100 steps (batch_mixed())
 "Walls closed except an open top" = the open (Dirichlet p=0 outside) solver
 with an occupied layer at x=0, x=W-1, y=0, z=0, z=D-1: outside the top face the
 pressure is 0, every other side is a solid wall, like ZQ_InitFineGrid3D's
@@ -242,3 +247,36 @@ def small_case(W: int, H: int, D: int, *, seed: int = 7, K: int = 20, substeps: 
         T = np.zeros((D, H, W), np.float32)
         rho = np.zeros((D, H, W), np.float32)
     return Workload(f"small{W}x{H}x{D}", W, H, D, p, occ, u, v, w, T, rho, 1, {"seed": seed})
+
+
+def batch_member(idx: int, *, seed: int = 0, K: int = 200, edges=(32, 48, 64, 96, 128)) -> Workload:
+    """Instance idx of the mixed-size batch (all draws seeded by seed and idx)."""
+    base = seed * 1_000_003 + 7919 * (idx + 1)
+    u = uniform01(base, 16)
+    e = int(edges[min(len(edges) - 1, int(u[0] * len(edges)))])
+    dims = [e, e, e]
+    if u[1] >= 0.5:                        # one axis doubled
+        dims[min(2, int(u[2] * 3))] *= 2
+    W, H, D = dims
+    occ = walls_open_top(W, H, D)
+    m = min(W, H, D)
+    r = float(np.float32(m) * (np.float32(0.06) + np.float32(0.06) * u[3]))
+    cx = float(np.float32(r + 1) + np.float32(W - 2 * r - 2) * u[4])
+    cz = float(np.float32(r + 1) + np.float32(D - 2 * r - 2) * u[5])
+    cy = float(np.float32(1.0) + np.float32(max(0.15 * H - 1.0, 0.0)) * u[6])
+    p = smoke_params(W, K)
+    p.gravity = float(np.float32(0.05) + np.float32(0.15) * u[7])      # alpha (density)
+    p.buoyancy = float(np.float32(0.2) + np.float32(0.6) * u[8])       # beta (temperature)
+    p.confine = float(np.float32(0.3) * u[9])                          # eps
+    p.step_time = float(np.float32(0.25) + np.float32(0.5) * u[10])    # dt
+    p.set_sources([sphere(cx, cy, cz, r)])
+    uu, vv, ww = initial_velocity(occ, base + 17)
+    T = np.zeros((D, H, W), np.float32)
+    rho = np.zeros((D, H, W), np.float32)
+    return Workload(f"batch[{idx}]{W}x{H}x{D}", W, H, D, p, occ, uu, vv, ww, T, rho, 100,
+                    {"seed": seed, "index": idx, "K": K})
+
+
+def batch_mixed(n: int = 64, *, seed: int = 0, K: int = 200, edges=(32, 48, 64, 96, 128)) -> list[Workload]:
+    """The mixed-size batch: n seeded instances (batch_member(0..n-1))."""
+    return [batch_member(i, seed=seed, K=K, edges=edges) for i in range(n)]
