@@ -100,6 +100,62 @@ class Oracle:
                              C.byref(params), nsteps, _p(p))
         return rc, p
 
+    # -- control problem and reverse mode ------------------------------------------
+    def step_ctrl(self, W, H, D, st, occ, params, F, nsteps=1):
+        """nsteps steps with the external per-cell force F (3, D, H, W)."""
+        return self._f("step_ctrl")(W, H, D, _p(st["u"]), _p(st["v"]), _p(st["w"]), _p(st["T"]), _p(st["rho"]),
+                                    _p(occ), C.byref(params), nsteps, _p(self.arr(F)))
+
+    def add_force_ctrl(self, W, H, D, st, occ, params, F):
+        self._f("add_force_ctrl")(W, H, D, _p(st["u"]), _p(st["v"]), _p(st["w"]), _p(occ), _p(st["T"]),
+                                  _p(st["rho"]), C.byref(params), _p(self.arr(F)))
+
+    def project_adjoint(self, W, H, D, g, occ, params):
+        """In place on g = {u, v, w}: adjoint of the projected velocity -> of the input."""
+        self._f("project_adjoint")(W, H, D, _p(g["u"]), _p(g["v"]), _p(g["w"]), _p(occ), C.byref(params))
+
+    def advect_scalar_adjoint(self, W, H, D, vel, occ, Tin, Din, gT, gD, params):
+        """Returns (gTin, gDin, gvel) for the MAC-velocity scalar advection."""
+        gTin = np.zeros((D, H, W), self.dtype)
+        gDin = np.zeros((D, H, W), self.dtype)
+        gv = {k: np.zeros_like(self.arr(vel[k])) for k in ("u", "v", "w")}
+        self._f("advect_scalar_adjoint")(W, H, D, _p(vel["u"]), _p(vel["v"]), _p(vel["w"]), _p(occ),
+                                         _p(self.arr(Tin)), _p(self.arr(Din)), _p(self.arr(gT)), _p(self.arr(gD)),
+                                         _p(gTin), _p(gDin), _p(gv["u"]), _p(gv["v"]), _p(gv["w"]), C.byref(params))
+        return gTin, gDin, gv
+
+    def advect_velocity_adjoint(self, W, H, D, vel, occ, params, g3):
+        g2 = {k: np.zeros_like(self.arr(vel[k])) for k in ("u", "v", "w")}
+        self._f("advect_velocity_adjoint")(W, H, D, _p(vel["u"]), _p(vel["v"]), _p(vel["w"]), _p(occ),
+                                           C.byref(params), _p(self.arr(g3["u"])), _p(self.arr(g3["v"])),
+                                           _p(self.arr(g3["w"])), _p(g2["u"]), _p(g2["v"]), _p(g2["w"]))
+        return g2
+
+    def add_force_adjoint(self, W, H, D, vel, occ, params, g, gT, grho, gF=None):
+        """In place on g (velocity); adds into gT, grho and gF (3, D, H, W) when given."""
+        self._f("add_force_adjoint")(W, H, D, _p(vel["u"]), _p(vel["v"]), _p(vel["w"]), _p(occ), C.byref(params),
+                                     _p(g["u"]), _p(g["v"]), _p(g["w"]), _p(gT), _p(grho), _p(gF))
+
+    def step_adjoint(self, W, H, D, st, occ, params, F, g, gF):
+        """Adjoint of one step(F) from state st; g (state adjoint) in place, gF += dL/dF."""
+        return self._f("step_adjoint")(W, H, D, _p(st["u"]), _p(st["v"]), _p(st["w"]), _p(st["T"]), _p(st["rho"]),
+                                       _p(occ), C.byref(params), _p(None if F is None else self.arr(F)),
+                                       _p(g["u"]), _p(g["v"]), _p(g["w"]), _p(g["T"]), _p(g["rho"]), _p(gF))
+
+    def control_loss(self, W, H, D, st, occ, params, nsteps, F, target, grad=False):
+        """L = sum (rho_n - target)^2 after nsteps steps with force F; with grad,
+        also dL/dF (3, D, H, W) and the adjoint of the initial state."""
+        loss = C.c_double(0.0)
+        gF = np.zeros((3, D, H, W), self.dtype) if grad else None
+        n0 = sum(st[k].size for k in ("u", "v", "w", "T", "rho"))
+        g0 = np.zeros(n0, self.dtype) if grad else None
+        rc = self._f("control_loss")(W, H, D, _p(self.arr(st["u"])), _p(self.arr(st["v"])), _p(self.arr(st["w"])),
+                                     _p(self.arr(st["T"])), _p(self.arr(st["rho"])), _p(occ), C.byref(params),
+                                     nsteps, _p(self.arr(F)), _p(self.arr(target)), C.byref(loss), _p(gF), _p(g0))
+        if rc != 0:
+            raise RuntimeError(f"oracle control_loss failed: {rc}")
+        return (loss.value, gF, g0) if grad else loss.value
+
     def state(self, wl):
         """Copy of a workload's state in this oracle's dtype."""
         return {k: self.arr(getattr(wl, k)).copy() for k in ("u", "v", "w", "T", "rho")}

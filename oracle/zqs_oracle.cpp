@@ -233,9 +233,12 @@ void vorticity(const Dims& d, const R* u, const R* v, const R* w, R h, R* vort, 
             }
 }
 
+/* F (optional): an external per-cell force added to f after the buoyancy
+ * terms, component-major dense (F[q*ncell + cell], q = x, y, z); the control
+ * of the adjoint problem (no counterpart in the reference). */
 template <class R>
 void add_force(const Dims& d, R* u, R* v, R* w, const uint8_t* occ, const R* T, const R* rho,
-               const zqs_params& P) {
+               const zqs_params& P, const R* F = nullptr) {
     const size_t n = d.ncell();
     const int W = d.W, H = d.H, D = d.D;
     const size_t sy = (size_t)W, sz = (size_t)W * H;
@@ -278,6 +281,11 @@ void add_force(const Dims& d, R* u, R* v, R* w, const uint8_t* occ, const R* T, 
         R fz = cc * (gx * oy - gy * ox);
         fy = fy + beta * (T[c] - tamb);
         fy = fy - alpha * rho[c];
+        if (F) {
+            fx = fx + F[c];
+            fy = fy + F[n + c];
+            fz = fz + F[2 * n + c];
+        }
         force[c * 3 + 0] = fx;
         force[c * 3 + 1] = fy;
         force[c * 3 + 2] = fz;
@@ -732,8 +740,9 @@ void project(const Dims& d, R* u, R* v, R* w, const uint8_t* occ, const zqs_para
  * (always with the open write-back, Utils3D:2163), projection, scalar
  * advection (in place, Utils3D:3835), reinjection. */
 template <class R>
-int step(const Dims& d, R* u, R* v, R* w, R* T, R* rho, const uint8_t* occ, const zqs_params& P, R* p_out) {
-    add_force(d, u, v, w, occ, T, rho, P);
+int step(const Dims& d, R* u, R* v, R* w, R* T, R* rho, const uint8_t* occ, const zqs_params& P, R* p_out,
+         const R* F = nullptr) {
+    add_force(d, u, v, w, occ, T, rho, P, F);
     attenuate(d, u, v, w, T, rho, occ, P);
     int rc = advect_velocity(d, u, v, w, occ, P, P.adv_vel_mode, true);
     if (rc) return rc;
@@ -741,6 +750,628 @@ int step(const Dims& d, R* u, R* v, R* w, R* T, R* rho, const uint8_t* occ, cons
     rc = advect_scalar(d, u, v, w, occ, T, rho, T, rho, P, P.adv_sca_mode);
     if (rc) return rc;
     reinject(d, T, rho, P);
+    return ZQS_OK;
+}
+
+/* ====================================================================== */
+/* Reverse mode (adjoint) of the step, for the force-field control problem */
+/* ====================================================================== */
+/* No counterpart in the reference: the differentiable path is new.  The
+ * forward map is step() with the control F; its adjoint is written stage by
+ * stage in reverse order, in the arithmetic type R (double for the FP64
+ * gradient).  Discrete decisions (the backtrace's occupancy/domain break,
+ * clamping, floor cells, the zero-length normal of the confinement force) are
+ * held at their forward values: this is the derivative almost everywhere.
+ * Stage rules (each the transpose of the forward rule restated above):
+ *   reinjection       adjoint zeroed on source cells (values overwritten)
+ *   advection         the final trilinear sample scattered back to its 8
+ *                     corners (transposed trilinear), and the position chain
+ *                     x_{s+1} = x_s - (dt/h) vel(x_s) reversed substep by
+ *                     substep: g_vel(x_s) = -(dt/h) g_x is scattered into the
+ *                     MAC velocity, g_x += J_vel(x_s)^T g_vel(x_s)
+ *   projection        G^T, then the 2K half-sweeps transposed in reverse
+ *                     order (black then red), then div^T (closed: minus the
+ *                     free-cell mean first)
+ *   attenuation       the same factors on the same live faces / cells
+ *   force             face averaging transposed into cell forces; buoyancy
+ *                     into T and rho; confinement through N = g/|g|, the
+ *                     one-sided/central gradient of |w|, the curl stencil and
+ *                     the MAC-to-centre average. */
+
+template <class R> static inline bool bt_ok(const Dims& d, const uint8_t* occ, R x, R y, R z) {
+    if (!(x >= R(0) && x <= (R)d.W && y >= R(0) && y <= (R)d.H && z >= R(0) && z <= (R)d.D)) return false;
+    int i = clampi((int)std::floor(x), 0, d.W - 1);
+    int j = clampi((int)std::floor(y), 0, d.H - 1);
+    int k = clampi((int)std::floor(z), 0, d.D - 1);
+    return occ[d.cell(i, j, k)] == 0;
+}
+
+/* backtrace() with every position kept: xs[3s..3s+2] = x_s; returns m, the
+ * index of the point backtrace() returns. */
+template <class R, class VelF>
+static inline int backtrace_record(const Dims& d, const uint8_t* occ, const VelF& vel, int steps, R dt, R h,
+                                   bool full, R px, R py, R pz, R* xs) {
+    R vx, vy, vz;
+    vel(px, py, pz, vx, vy, vz);
+    xs[0] = px;
+    xs[1] = py;
+    xs[2] = pz;
+    int m = 0, istep = 0;
+    bool broke = false;
+    do {
+        if (!bt_ok(d, occ, px, py, pz)) {
+            broke = true;
+            break;
+        }
+        m = istep;
+        px = px - (vx * dt) / h;
+        py = py - (vy * dt) / h;
+        pz = pz - (vz * dt) / h;
+        vel(px, py, pz, vx, vy, vz);
+        istep++;
+        xs[3 * istep + 0] = px;
+        xs[3 * istep + 1] = py;
+        xs[3 * istep + 2] = pz;
+    } while (istep < steps);
+    if (full && !broke && bt_ok(d, occ, px, py, pz)) m = istep;
+    return m;
+}
+
+/* Trilinear value and its gradient with respect to (gx, gy, gz); clamped
+ * axes have equal corners and so a zero derivative. */
+template <class R, class S>
+static inline R trilinear_grad(const S* base, int nx, int ny, int nz, R gx, R gy, R gz, R g[3]) {
+    Axis<R> ax = axis(gx, nx), ay = axis(gy, ny), az = axis(gz, nz);
+    auto at = [&](int i, int j, int k) -> R { return (R)base[(((size_t)k * ny) + j) * nx + i]; };
+    R c000 = at(ax.i0, ay.i0, az.i0), c100 = at(ax.i1, ay.i0, az.i0);
+    R c010 = at(ax.i0, ay.i1, az.i0), c110 = at(ax.i1, ay.i1, az.i0);
+    R c001 = at(ax.i0, ay.i0, az.i1), c101 = at(ax.i1, ay.i0, az.i1);
+    R c011 = at(ax.i0, ay.i1, az.i1), c111 = at(ax.i1, ay.i1, az.i1);
+    R c00 = lerp(c000, c100, ax.t), c10 = lerp(c010, c110, ax.t);
+    R c01 = lerp(c001, c101, ax.t), c11 = lerp(c011, c111, ax.t);
+    R c0 = lerp(c00, c10, ay.t), c1 = lerp(c01, c11, ay.t);
+    g[0] = lerp(lerp(c100 - c000, c110 - c010, ay.t), lerp(c101 - c001, c111 - c011, ay.t), az.t);
+    g[1] = lerp(c10 - c00, c11 - c01, az.t);
+    g[2] = c1 - c0;
+    return lerp(c0, c1, az.t);
+}
+
+template <class R> static inline void atomic_add(R* p, R v) {
+#pragma omp atomic
+    *p += v;
+}
+
+/* Transposed trilinear: val times each corner weight added to the corners. */
+template <class R>
+static inline void trilinear_scatter(R* base, int nx, int ny, int nz, R gx, R gy, R gz, R val) {
+    if (val == R(0)) return;
+    Axis<R> ax = axis(gx, nx), ay = axis(gy, ny), az = axis(gz, nz);
+    const R wx[2] = {R(1) - ax.t, ax.t}, wy[2] = {R(1) - ay.t, ay.t}, wz[2] = {R(1) - az.t, az.t};
+    const int ix[2] = {ax.i0, ax.i1}, iy[2] = {ay.i0, ay.i1}, iz[2] = {az.i0, az.i1};
+    for (int c = 0; c < 2; c++)
+        for (int b = 0; b < 2; b++)
+            for (int a = 0; a < 2; a++)
+                atomic_add(base + ((((size_t)iz[c] * ny) + iy[b]) * nx + ix[a]), ((wx[a] * wy[b]) * wz[c]) * val);
+}
+
+/* MAC velocity: Jacobian rows J[a] = grad vel_a, and the transposed sample. */
+template <class R> struct MacAdj {
+    Dims d;
+    const R *u, *v, *w;
+    void jac(R px, R py, R pz, R J[3][3]) const {
+        const R hf = R(0.5);
+        trilinear_grad<R>(u, d.W + 1, d.H, d.D, px, py - hf, pz - hf, J[0]);
+        trilinear_grad<R>(v, d.W, d.H + 1, d.D, px - hf, py, pz - hf, J[1]);
+        trilinear_grad<R>(w, d.W, d.H, d.D + 1, px - hf, py - hf, pz, J[2]);
+    }
+    void scatter(R* gu, R* gv, R* gw, R px, R py, R pz, const R g[3]) const {
+        const R hf = R(0.5);
+        trilinear_scatter<R>(gu, d.W + 1, d.H, d.D, px, py - hf, pz - hf, g[0]);
+        trilinear_scatter<R>(gv, d.W, d.H + 1, d.D, px - hf, py, pz - hf, g[1]);
+        trilinear_scatter<R>(gw, d.W, d.H, d.D + 1, px - hf, py - hf, pz, g[2]);
+    }
+};
+
+/* Reverse the position chain of a recorded backtrace: gx (adjoint of x_m) in,
+ * velocity adjoint scattered into (gu, gv, gw). */
+template <class R>
+static inline void backtrace_adjoint(const MacAdj<R>& V, R* gu, R* gv, R* gw, const R* xs, int m, R dt, R h,
+                                     R gx[3]) {
+    const R c = dt / h;
+    for (int s = m - 1; s >= 0; s--) {
+        const R* x = xs + 3 * s;
+        R gvel[3] = {-c * gx[0], -c * gx[1], -c * gx[2]};
+        V.scatter(gu, gv, gw, x[0], x[1], x[2], gvel);
+        R J[3][3];
+        V.jac(x[0], x[1], x[2], J);
+        for (int b = 0; b < 3; b++) gx[b] += (J[0][b] * gvel[0] + J[1][b] * gvel[1]) + J[2][b] * gvel[2];
+    }
+}
+
+/* Adjoint of advect_scalar (MAC velocity): (gTout, gDout) in; adjoints of the
+ * advected fields added to (gTin, gDin) and of the velocity to (gu, gv, gw). */
+template <class R>
+void advect_scalar_adjoint(const Dims& d, const R* u, const R* v, const R* w, const uint8_t* occ, const R* Tin,
+                           const R* Din, const R* gTout, const R* gDout, R* gTin, R* gDin, R* gu, R* gv, R* gw,
+                           const zqs_params& P) {
+    AdvCtx<R> a = adv_ctx<R>(P);
+    const R hf = R(0.5);
+    MacSampler<R> ms{d, u, v, w};
+    MacAdj<R> V{d, u, v, w};
+#pragma omp parallel
+    {
+        std::vector<R> xs(3 * (a.steps + 1));
+#pragma omp for schedule(dynamic, 1)
+        for (int k = 0; k < d.D; k++)
+            for (int j = 0; j < d.H; j++)
+                for (int i = 0; i < d.W; i++) {
+                    size_t c = d.cell(i, j, k);
+                    R gT = gTout[c], gD = gDout[c];
+                    if (gT == R(0) && gD == R(0)) continue;
+                    int m = backtrace_record(d, occ, ms, a.steps, a.dt, a.h, a.full, (R)i + hf, (R)j + hf,
+                                             (R)k + hf, xs.data());
+                    R* x = xs.data() + 3 * m;
+                    trilinear_scatter<R>(gTin, d.W, d.H, d.D, x[0] - hf, x[1] - hf, x[2] - hf, gT);
+                    trilinear_scatter<R>(gDin, d.W, d.H, d.D, x[0] - hf, x[1] - hf, x[2] - hf, gD);
+                    R g1[3], g2[3];
+                    trilinear_grad<R>(Tin, d.W, d.H, d.D, x[0] - hf, x[1] - hf, x[2] - hf, g1);
+                    trilinear_grad<R>(Din, d.W, d.H, d.D, x[0] - hf, x[1] - hf, x[2] - hf, g2);
+                    R gx[3] = {gT * g1[0] + gD * g2[0], gT * g1[1] + gD * g2[1], gT * g1[2] + gD * g2[2]};
+                    backtrace_adjoint(V, gu, gv, gw, xs.data(), m, a.dt, a.h, gx);
+                }
+    }
+}
+
+/* Adjoint of advect_velocity (inMAC_outMAC, open write-back): the adjoint of
+ * the output (gu3..) in, the adjoint of the input velocity (gu2..) ASSIGNED. */
+template <class R>
+void advect_velocity_adjoint(const Dims& d, const R* u, const R* v, const R* w, const uint8_t* occ,
+                             const zqs_params& P, const R* gu3, const R* gv3, const R* gw3, R* gu2, R* gv2, R* gw2) {
+    AdvCtx<R> a = adv_ctx<R>(P);
+    const R hf = R(0.5);
+    std::fill(gu2, gu2 + d.nu(), R(0));
+    std::fill(gv2, gv2 + d.nv(), R(0));
+    std::fill(gw2, gw2 + d.nw(), R(0));
+    MacSampler<R> ms{d, u, v, w};
+    MacAdj<R> V{d, u, v, w};
+#pragma omp parallel
+    {
+        std::vector<R> xs(3 * (a.steps + 1));
+#pragma omp for schedule(dynamic, 1)
+        for (int k = 0; k <= d.D; k++)
+            for (int j = 0; j <= d.H; j++)
+                for (int i = 0; i <= d.W; i++) {
+                    for (int q = 0; q < 3; q++) {
+                        bool in, live;
+                        R px = (R)i + hf, py = (R)j + hf, pz = (R)k + hf;
+                        size_t f;
+                        const R* gin;
+                        R* gout;
+                        if (q == 0) {
+                            in = j < d.H && k < d.D;
+                            if (!in) continue;
+                            live = u_live(d, occ, i, j, k, true);
+                            px = (R)i;
+                            f = d.uix(i, j, k);
+                            gin = gu3;
+                            gout = gu2;
+                        } else if (q == 1) {
+                            in = i < d.W && k < d.D;
+                            if (!in) continue;
+                            live = v_live(d, occ, i, j, k, true);
+                            py = (R)j;
+                            f = d.vix(i, j, k);
+                            gin = gv3;
+                            gout = gv2;
+                        } else {
+                            in = i < d.W && j < d.H;
+                            if (!in) continue;
+                            live = w_live(d, occ, i, j, k, true);
+                            pz = (R)k;
+                            f = d.wix(i, j, k);
+                            gin = gw3;
+                            gout = gw2;
+                        }
+                        const R g = gin[f];
+                        if (g == R(0)) continue;
+                        if (!live) {
+                            atomic_add(gout + f, g);
+                            continue;
+                        }
+                        int m = backtrace_record(d, occ, ms, a.steps, a.dt, a.h, a.full, px, py, pz, xs.data());
+                        R* x = xs.data() + 3 * m;
+                        R gx[3];
+                        if (q == 0) {
+                            trilinear_scatter<R>(gu2, d.W + 1, d.H, d.D, x[0], x[1] - hf, x[2] - hf, g);
+                            trilinear_grad<R>(u, d.W + 1, d.H, d.D, x[0], x[1] - hf, x[2] - hf, gx);
+                        } else if (q == 1) {
+                            trilinear_scatter<R>(gv2, d.W, d.H + 1, d.D, x[0] - hf, x[1], x[2] - hf, g);
+                            trilinear_grad<R>(v, d.W, d.H + 1, d.D, x[0] - hf, x[1], x[2] - hf, gx);
+                        } else {
+                            trilinear_scatter<R>(gw2, d.W, d.H, d.D + 1, x[0] - hf, x[1] - hf, x[2], g);
+                            trilinear_grad<R>(w, d.W, d.H, d.D + 1, x[0] - hf, x[1] - hf, x[2], gx);
+                        }
+                        for (int b = 0; b < 3; b++) gx[b] = gx[b] * g;
+                        backtrace_adjoint(V, gu2, gv2, gw2, xs.data(), m, a.dt, a.h, gx);
+                    }
+                }
+    }
+}
+
+/* SOR stencil weight of each cell (0 for occupied cells), as project(). */
+template <class R> static void sor_counts(const Dims& d, const uint8_t* occ, bool open, std::vector<R>& cnt) {
+    cnt.assign(d.ncell(), R(0));
+    for (int k = 0; k < d.D; k++)
+        for (int j = 0; j < d.H; j++)
+            for (int i = 0; i < d.W; i++) {
+                size_t c = d.cell(i, j, k);
+                if (occ[c]) continue;
+                int nin = 0, nfree = 0;
+                const int di[6] = {-1, 1, 0, 0, 0, 0}, dj[6] = {0, 0, -1, 1, 0, 0}, dk[6] = {0, 0, 0, 0, -1, 1};
+                for (int q = 0; q < 6; q++) {
+                    int a = i + di[q], b = j + dj[q], e = k + dk[q];
+                    if (a < 0 || a >= d.W || b < 0 || b >= d.H || e < 0 || e >= d.D) continue;
+                    nin++;
+                    if (!occ[d.cell(a, b, e)]) nfree++;
+                }
+                cnt[c] = open ? (R)(6 - (nin - nfree)) : (R)nfree;
+            }
+}
+
+/* Adjoint of project(): (gu, gv, gw) = adjoint of the projected velocity in,
+ * adjoint of the velocity before projection out (in place). */
+template <class R>
+void project_adjoint(const Dims& d, R* gu, R* gv, R* gw, const uint8_t* occ, const zqs_params& P) {
+    const int W = d.W, H = d.H, D = d.D;
+    const size_t n = d.ncell();
+    const bool open = P.solver == ZQS_SOLVER_OPEN;
+    std::vector<R> cnt;
+    sor_counts(d, occ, open, cnt);
+    std::vector<R> gp(n, R(0)), gd(n, R(0));
+    /* G^T: u_f -= p_R - p_L  =>  gp_R -= g_f, gp_L += g_f */
+    for (int k = 0; k <= D; k++)
+        for (int j = 0; j <= H; j++)
+            for (int i = 0; i <= W; i++) {
+                if (j < H && k < D && u_live(d, occ, i, j, k, open)) {
+                    R g = gu[d.uix(i, j, k)];
+                    if (i < W) gp[d.cell(i, j, k)] -= g;
+                    if (i > 0) gp[d.cell(i - 1, j, k)] += g;
+                }
+                if (i < W && k < D && v_live(d, occ, i, j, k, open)) {
+                    R g = gv[d.vix(i, j, k)];
+                    if (j < H) gp[d.cell(i, j, k)] -= g;
+                    if (j > 0) gp[d.cell(i, j - 1, k)] += g;
+                }
+                if (i < W && j < H && w_live(d, occ, i, j, k, open)) {
+                    R g = gw[d.wix(i, j, k)];
+                    if (k < D) gp[d.cell(i, j, k)] -= g;
+                    if (k > 0) gp[d.cell(i, j, k - 1)] += g;
+                }
+            }
+    /* SOR^T: half-sweeps in reverse order; for the half-sweep of colour c,
+     * z_c = (omega/cnt_c) gp_c goes to every free in-domain neighbour and
+     * (negated) to gd_c, then gp_c *= (1-omega). */
+    const R omega = (R)P.omega, om1 = R(1) - omega;
+    const size_t sy = (size_t)W, sz = (size_t)W * H;
+    auto upd = [&](size_t c) { return !occ[c] && cnt[c] != R(0); };
+    for (int it = P.sor_iters - 1; it >= 0; it--) {
+        for (int colour = 1; colour >= 0; colour--) {
+            /* gather into the other colour from this colour's cells */
+#pragma omp parallel for schedule(static)
+            for (int k = 0; k < D; k++)
+                for (int j = 0; j < H; j++)
+                    for (int i = (j + k + colour + 1) & 1; i < W; i += 2) {
+                        size_t c = d.cell(i, j, k);
+                        if (occ[c]) continue;
+                        R s = R(0);
+                        if (i > 0 && upd(c - 1)) s += (omega / cnt[c - 1]) * gp[c - 1];
+                        if (i < W - 1 && upd(c + 1)) s += (omega / cnt[c + 1]) * gp[c + 1];
+                        if (j > 0 && upd(c - sy)) s += (omega / cnt[c - sy]) * gp[c - sy];
+                        if (j < H - 1 && upd(c + sy)) s += (omega / cnt[c + sy]) * gp[c + sy];
+                        if (k > 0 && upd(c - sz)) s += (omega / cnt[c - sz]) * gp[c - sz];
+                        if (k < D - 1 && upd(c + sz)) s += (omega / cnt[c + sz]) * gp[c + sz];
+                        gp[c] += s;
+                    }
+#pragma omp parallel for schedule(static)
+            for (int k = 0; k < D; k++)
+                for (int j = 0; j < H; j++)
+                    for (int i = (j + k + colour) & 1; i < W; i += 2) {
+                        size_t c = d.cell(i, j, k);
+                        if (!upd(c)) continue;
+                        gd[c] -= (omega / cnt[c]) * gp[c];
+                        gp[c] = om1 * gp[c];
+                    }
+        }
+    }
+    if (!open) {
+        /* d -= mean_free(d) is its own transpose (an orthogonal projection) */
+        double s = 0.0;
+        int64_t nf = 0;
+        for (size_t c = 0; c < n; c++)
+            if (!occ[c]) {
+                s += (double)gd[c];
+                nf++;
+            }
+        if (nf > 0) {
+            R mean = (R)(s / (double)nf);
+            for (size_t c = 0; c < n; c++)
+                if (!occ[c]) gd[c] -= mean;
+        }
+    }
+    /* div^T: d_c = u[i+1]-u[i] + v[j+1]-v[j] + w[k+1]-w[k] on free cells */
+    auto gdc = [&](int i, int j, int k) -> R {
+        if (i < 0 || i >= W || j < 0 || j >= H || k < 0 || k >= D) return R(0);
+        size_t c = d.cell(i, j, k);
+        return occ[c] ? R(0) : gd[c];
+    };
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k <= D; k++)
+        for (int j = 0; j <= H; j++)
+            for (int i = 0; i <= W; i++) {
+                if (j < H && k < D) gu[d.uix(i, j, k)] += gdc(i - 1, j, k) - gdc(i, j, k);
+                if (i < W && k < D) gv[d.vix(i, j, k)] += gdc(i, j - 1, k) - gdc(i, j, k);
+                if (i < W && j < H) gw[d.wix(i, j, k)] += gdc(i, j, k - 1) - gdc(i, j, k);
+            }
+}
+
+/* Adjoint of add_force (F included): (gu, gv, gw) = adjoint of the velocity
+ * after the face update in, adjoint of the velocity before it out (in place);
+ * adjoints of T, rho and F are ADDED (gF may be null). */
+template <class R>
+void add_force_adjoint(const Dims& d, const R* u, const R* v, const R* w, const uint8_t* occ, const zqs_params& P,
+                       R* gu, R* gv, R* gw, R* gT, R* grho, R* gF) {
+    const size_t n = d.ncell();
+    const int W = d.W, H = d.H, D = d.D;
+    const size_t sy = (size_t)W, sz = (size_t)W * H;
+    const R h = (R)P.voxel_size;
+    std::vector<R> vort(n * 3, R(0)), vs(n, R(0)), gf(n * 3, R(0));
+    vorticity(d, u, v, w, h, vort.data(), vs.data());
+    const R dt = (R)P.step_time, hdt = dt * R(0.5);
+    /* face averaging transposed */
+    for (int k = 0; k <= D; k++)
+        for (int j = 0; j <= H; j++)
+            for (int i = 0; i <= W; i++) {
+                if (j < H && k < D && u_live(d, occ, i, j, k, true)) {
+                    R g = gu[d.uix(i, j, k)];
+                    if (i == 0) gf[d.cell(0, j, k) * 3 + 0] += dt * g;
+                    else if (i == W) gf[d.cell(W - 1, j, k) * 3 + 0] += dt * g;
+                    else {
+                        gf[d.cell(i, j, k) * 3 + 0] += hdt * g;
+                        gf[d.cell(i - 1, j, k) * 3 + 0] += hdt * g;
+                    }
+                }
+                if (i < W && k < D && v_live(d, occ, i, j, k, true)) {
+                    R g = gv[d.vix(i, j, k)];
+                    if (j == 0) gf[d.cell(i, 0, k) * 3 + 1] += dt * g;
+                    else if (j == H) gf[d.cell(i, H - 1, k) * 3 + 1] += dt * g;
+                    else {
+                        gf[d.cell(i, j, k) * 3 + 1] += hdt * g;
+                        gf[d.cell(i, j - 1, k) * 3 + 1] += hdt * g;
+                    }
+                }
+                if (i < W && j < H && w_live(d, occ, i, j, k, true)) {
+                    R g = gw[d.wix(i, j, k)];
+                    if (k == 0) gf[d.cell(i, j, 0) * 3 + 2] += dt * g;
+                    else if (k == D) gf[d.cell(i, j, D - 1) * 3 + 2] += dt * g;
+                    else {
+                        gf[d.cell(i, j, k) * 3 + 2] += hdt * g;
+                        gf[d.cell(i, j, k - 1) * 3 + 2] += hdt * g;
+                    }
+                }
+            }
+    const R cc = (R)P.confine * h;
+    const R beta = (R)P.buoyancy, alpha = (R)P.gravity;
+    std::vector<R> gvs(n, R(0)), gom(n * 3, R(0)), gg(n * 3, R(0));
+    for (int k = 0; k < D; k++)
+        for (int j = 0; j < H; j++)
+            for (int i = 0; i < W; i++) {
+                size_t c = d.cell(i, j, k);
+                R fx = gf[c * 3 + 0], fy = gf[c * 3 + 1], fz = gf[c * 3 + 2];
+                if (gF) {
+                    gF[c] += fx;
+                    gF[n + c] += fy;
+                    gF[2 * n + c] += fz;
+                }
+                gT[c] += beta * fy;
+                grho[c] -= alpha * fy;
+                /* recompute the normal of this cell as add_force() does */
+                R gx, gy, gz;
+                if (i == 0) gx = vs[c + 1] - vs[c];
+                else if (i == W - 1) gx = vs[c] - vs[c - 1];
+                else gx = R(0.5) * (vs[c + 1] - vs[c - 1]);
+                if (j == 0) gy = vs[c + sy] - vs[c];
+                else if (j == H - 1) gy = vs[c] - vs[c - sy];
+                else gy = R(0.5) * (vs[c + sy] - vs[c - sy]);
+                if (k == 0) gz = vs[c + sz] - vs[c];
+                else if (k == D - 1) gz = vs[c] - vs[c - sz];
+                else gz = R(0.5) * (vs[c + sz] - vs[c - sz]);
+                R len = std::sqrt((gx * gx + gy * gy) + gz * gz);
+                R Nx = gx, Ny = gy, Nz = gz;
+                if (len != R(0)) {
+                    Nx = gx / len;
+                    Ny = gy / len;
+                    Nz = gz / len;
+                }
+                const R ox = vort[c * 3 + 0], oy = vort[c * 3 + 1], oz = vort[c * 3 + 2];
+                /* f = cc * (N x w) */
+                R gNx = cc * (oy * fz - oz * fy), gNy = cc * (oz * fx - ox * fz), gNz = cc * (ox * fy - oy * fx);
+                gom[c * 3 + 0] = cc * (Nz * fy - Ny * fz);
+                gom[c * 3 + 1] = cc * (Nx * fz - Nz * fx);
+                gom[c * 3 + 2] = cc * (Ny * fx - Nx * fy);
+                if (len != R(0)) {
+                    R dot = (Nx * gNx + Ny * gNy) + Nz * gNz;
+                    gg[c * 3 + 0] = (gNx - Nx * dot) / len;
+                    gg[c * 3 + 1] = (gNy - Ny * dot) / len;
+                    gg[c * 3 + 2] = (gNz - Nz * dot) / len;
+                }
+            }
+    /* gradient of |w| transposed (central x0.5 inside, one-sided at the boundary) */
+    for (int k = 0; k < D; k++)
+        for (int j = 0; j < H; j++)
+            for (int i = 0; i < W; i++) {
+                size_t c = d.cell(i, j, k);
+                R g = gg[c * 3 + 0];
+                if (i == 0) { gvs[c + 1] += g; gvs[c] -= g; }
+                else if (i == W - 1) { gvs[c] += g; gvs[c - 1] -= g; }
+                else { gvs[c + 1] += R(0.5) * g; gvs[c - 1] -= R(0.5) * g; }
+                g = gg[c * 3 + 1];
+                if (j == 0) { gvs[c + sy] += g; gvs[c] -= g; }
+                else if (j == H - 1) { gvs[c] += g; gvs[c - sy] -= g; }
+                else { gvs[c + sy] += R(0.5) * g; gvs[c - sy] -= R(0.5) * g; }
+                g = gg[c * 3 + 2];
+                if (k == 0) { gvs[c + sz] += g; gvs[c] -= g; }
+                else if (k == D - 1) { gvs[c] += g; gvs[c - sz] -= g; }
+                else { gvs[c + sz] += R(0.5) * g; gvs[c - sz] -= R(0.5) * g; }
+            }
+    /* |w| and the curl stencil, interior cells only */
+    std::vector<R> gU(n, R(0)), gV(n, R(0)), gW(n, R(0));
+    const R twoh = R(2) * h;
+    for (int k = 1; k < D - 1; k++)
+        for (int j = 1; j < H - 1; j++)
+            for (int i = 1; i < W - 1; i++) {
+                size_t c = d.cell(i, j, k);
+                R ox = vort[c * 3 + 0], oy = vort[c * 3 + 1], oz = vort[c * 3 + 2];
+                R gox = gom[c * 3 + 0], goy = gom[c * 3 + 1], goz = gom[c * 3 + 2];
+                if (vs[c] != R(0)) {
+                    gox += ox / vs[c] * gvs[c];
+                    goy += oy / vs[c] * gvs[c];
+                    goz += oz / vs[c] * gvs[c];
+                }
+                gox = gox / twoh;
+                goy = goy / twoh;
+                goz = goz / twoh;
+                gW[c + sy] += gox; gW[c - sy] -= gox; gV[c + sz] -= gox; gV[c - sz] += gox;
+                gU[c + sz] += goy; gU[c - sz] -= goy; gW[c + 1] -= goy; gW[c - 1] += goy;
+                gV[c + 1] += goz; gV[c - 1] -= goz; gU[c + sy] -= goz; gU[c - sy] += goz;
+            }
+    /* centre = 0.5*(lo + hi) transposed */
+    for (int k = 0; k < D; k++)
+        for (int j = 0; j < H; j++)
+            for (int i = 0; i < W; i++) {
+                size_t c = d.cell(i, j, k);
+                gu[d.uix(i, j, k)] += R(0.5) * gU[c];
+                gu[d.uix(i + 1, j, k)] += R(0.5) * gU[c];
+                gv[d.vix(i, j, k)] += R(0.5) * gV[c];
+                gv[d.vix(i, j + 1, k)] += R(0.5) * gV[c];
+                gw[d.wix(i, j, k)] += R(0.5) * gW[c];
+                gw[d.wix(i, j, k + 1)] += R(0.5) * gW[c];
+            }
+}
+
+/* Cells a source overwrites (reinject()'s test). */
+template <class R> static void source_mask(const Dims& d, const zqs_params& P, std::vector<uint8_t>& m) {
+    m.assign(d.ncell(), 0);
+    std::vector<R> T(d.ncell(), R(0)), rho(d.ncell(), R(0));
+    zqs_params Q = P;
+    for (int s = 0; s < Q.n_sources; s++) Q.sources[s].density = 1.0f;
+    reinject(d, T.data(), rho.data(), Q);
+    for (size_t c = 0; c < d.ncell(); c++) m[c] = rho[c] != R(0);
+}
+
+/* Adjoint of one step(F) from the state s0 at its start.  (gu..grho) = the
+ * adjoint of the state after the step in, of s0 out; gF (nullable) += the
+ * adjoint of F. */
+template <class R>
+int step_adjoint(const Dims& d, const R* u0, const R* v0, const R* w0, const R* T0, const R* rho0,
+                 const uint8_t* occ, const zqs_params& P, const R* F, R* gu, R* gv, R* gw, R* gT, R* grho, R* gF) {
+    if (P.adv_vel_mode != ZQS_ADV_VEL_INMAC_OUTMAC || P.adv_sca_mode != ZQS_ADV_SCA_MAC) return ZQS_EUNSUPPORTED;
+    const size_t n = d.ncell();
+    /* forward intermediates */
+    std::vector<R> u2(u0, u0 + d.nu()), v2(v0, v0 + d.nv()), w2(w0, w0 + d.nw());
+    std::vector<R> T1(T0, T0 + n), D1(rho0, rho0 + n);
+    add_force(d, u2.data(), v2.data(), w2.data(), occ, T0, rho0, P, F);
+    attenuate(d, u2.data(), v2.data(), w2.data(), T1.data(), D1.data(), occ, P);
+    std::vector<R> u4(u2), v4(v2), w4(w2);
+    int rc = advect_velocity(d, u4.data(), v4.data(), w4.data(), occ, P, P.adv_vel_mode, true);
+    if (rc) return rc;
+    project(d, u4.data(), v4.data(), w4.data(), occ, P, (R*)nullptr, (R*)nullptr, (zqs_stats*)nullptr);
+    /* reinjection */
+    std::vector<uint8_t> src;
+    source_mask<R>(d, P, src);
+    for (size_t c = 0; c < n; c++)
+        if (src[c]) {
+            gT[c] = R(0);
+            grho[c] = R(0);
+        }
+    /* scalar advection: velocity u4, fields T1, D1 */
+    std::vector<R> gT1(n, R(0)), gD1(n, R(0));
+    advect_scalar_adjoint(d, u4.data(), v4.data(), w4.data(), occ, T1.data(), D1.data(), gT, grho, gT1.data(),
+                          gD1.data(), gu, gv, gw, P);
+    /* projection */
+    project_adjoint(d, gu, gv, gw, occ, P);
+    /* velocity advection */
+    std::vector<R> gu2(d.nu()), gv2(d.nv()), gw2(d.nw());
+    advect_velocity_adjoint(d, u2.data(), v2.data(), w2.data(), occ, P, gu, gv, gw, gu2.data(), gv2.data(),
+                            gw2.data());
+    /* attenuation */
+    const R av = (R)P.vel_atten, at = (R)P.temp_atten, ad = (R)P.dens_atten;
+    for (int k = 0; k <= d.D; k++)
+        for (int j = 0; j <= d.H; j++)
+            for (int i = 0; i <= d.W; i++) {
+                if (j < d.H && k < d.D) {
+                    size_t f = d.uix(i, j, k);
+                    gu[f] = u_live(d, occ, i, j, k, true) ? av * gu2[f] : gu2[f];
+                }
+                if (i < d.W && k < d.D) {
+                    size_t f = d.vix(i, j, k);
+                    gv[f] = v_live(d, occ, i, j, k, true) ? av * gv2[f] : gv2[f];
+                }
+                if (i < d.W && j < d.H) {
+                    size_t f = d.wix(i, j, k);
+                    gw[f] = w_live(d, occ, i, j, k, true) ? av * gw2[f] : gw2[f];
+                }
+            }
+    for (size_t c = 0; c < n; c++) {
+        gT[c] = at * gT1[c];
+        grho[c] = ad * gD1[c];
+    }
+    /* forces */
+    add_force_adjoint(d, u0, v0, w0, occ, P, gu, gv, gw, gT, grho, gF);
+    return ZQS_OK;
+}
+
+/* The control problem: L(F) = sum_c (rho_n[c] - target[c])^2 after nsteps
+ * steps of step(F) from the given state.  With gF non-null, the gradient
+ * dL/dF is stored there (every step state is kept; test sizes only) and,
+ * when g0 is non-null, the adjoint of the initial state (u,v,w,T,rho packed
+ * in that order) too. */
+template <class R>
+int control_loss(const Dims& d, const R* u, const R* v, const R* w, const R* T, const R* rho, const uint8_t* occ,
+                 const zqs_params& P, int nsteps, const R* F, const R* target, double* loss, R* gF, R* g0) {
+    const size_t n = d.ncell(), nu = d.nu(), nv = d.nv(), nw = d.nw();
+    const size_t ns = nu + nv + nw + 2 * n;
+    std::vector<R> s(u, u + nu);
+    s.insert(s.end(), v, v + nv);
+    s.insert(s.end(), w, w + nw);
+    s.insert(s.end(), T, T + n);
+    s.insert(s.end(), rho, rho + n);
+    std::vector<R> hist;
+    if (gF) hist.resize(ns * (size_t)nsteps);
+    for (int t = 0; t < nsteps; t++) {
+        if (gF) std::copy(s.begin(), s.end(), hist.begin() + ns * (size_t)t);
+        R* p = s.data();
+        int rc = step(d, p, p + nu, p + nu + nv, p + nu + nv + nw, p + nu + nv + nw + n, occ, P, (R*)nullptr, F);
+        if (rc) return rc;
+    }
+    const R* rn = s.data() + nu + nv + nw + n;
+    double L = 0.0;
+    for (size_t c = 0; c < n; c++) {
+        double e = (double)rn[c] - (double)target[c];
+        L += e * e;
+    }
+    *loss = L;
+    if (!gF) return ZQS_OK;
+    std::fill(gF, gF + 3 * n, R(0));
+    std::vector<R> g(ns, R(0));
+    for (size_t c = 0; c < n; c++) g[nu + nv + nw + n + c] = R(2) * (rn[c] - target[c]);
+    for (int t = nsteps - 1; t >= 0; t--) {
+        const R* p = hist.data() + ns * (size_t)t;
+        R* q = g.data();
+        int rc = step_adjoint(d, p, p + nu, p + nu + nv, p + nu + nv + nw, p + nu + nv + nw + n, occ, P, F, q,
+                              q + nu, q + nu + nv, q + nu + nv + nw, q + nu + nv + nw + n, gF);
+        if (rc) return rc;
+    }
+    if (g0) std::copy(g.begin(), g.end(), g0);
     return ZQS_OK;
 }
 
@@ -792,6 +1423,54 @@ int step(const Dims& d, R* u, R* v, R* w, R* T, R* rho, const uint8_t* occ, cons
                                                const R* av, const R* aw, R* u, R* v, R* w,              \
                                                int is_open) {                                           \
         zqo::apply_advect_result<R>(zqo::Dims{W, H, D}, occ, au, av, aw, u, v, w, is_open != 0);        \
+    }                                                                                                   \
+    ZQO_API int zqo_step_ctrl_##SFX(int W, int H, int D, R* u, R* v, R* w, R* T, R* rho,                \
+                                    const uint8_t* occ, const zqs_params* P, int nsteps, const R* F) {  \
+        for (int s = 0; s < nsteps; s++) {                                                              \
+            int rc = zqo::step<R>(zqo::Dims{W, H, D}, u, v, w, T, rho, occ, *P, (R*)nullptr, F);         \
+            if (rc) return rc;                                                                          \
+        }                                                                                               \
+        return 0;                                                                                       \
+    }                                                                                                   \
+    ZQO_API void zqo_project_adjoint_##SFX(int W, int H, int D, R* gu, R* gv, R* gw, const uint8_t* occ, \
+                                           const zqs_params* P) {                                       \
+        zqo::project_adjoint<R>(zqo::Dims{W, H, D}, gu, gv, gw, occ, *P);                               \
+    }                                                                                                   \
+    ZQO_API void zqo_advect_scalar_adjoint_##SFX(int W, int H, int D, const R* u, const R* v, const R* w, \
+                                                 const uint8_t* occ, const R* Tin, const R* Din,        \
+                                                 const R* gTout, const R* gDout, R* gTin, R* gDin,      \
+                                                 R* gu, R* gv, R* gw, const zqs_params* P) {            \
+        zqo::advect_scalar_adjoint<R>(zqo::Dims{W, H, D}, u, v, w, occ, Tin, Din, gTout, gDout, gTin,   \
+                                      gDin, gu, gv, gw, *P);                                            \
+    }                                                                                                   \
+    ZQO_API void zqo_advect_velocity_adjoint_##SFX(int W, int H, int D, const R* u, const R* v,          \
+                                                   const R* w, const uint8_t* occ, const zqs_params* P, \
+                                                   const R* gu3, const R* gv3, const R* gw3, R* gu2,    \
+                                                   R* gv2, R* gw2) {                                    \
+        zqo::advect_velocity_adjoint<R>(zqo::Dims{W, H, D}, u, v, w, occ, *P, gu3, gv3, gw3, gu2, gv2,  \
+                                        gw2);                                                           \
+    }                                                                                                   \
+    ZQO_API void zqo_add_force_ctrl_##SFX(int W, int H, int D, R* u, R* v, R* w, const uint8_t* occ,     \
+                                          const R* T, const R* rho, const zqs_params* P, const R* F) {  \
+        zqo::add_force<R>(zqo::Dims{W, H, D}, u, v, w, occ, T, rho, *P, F);                              \
+    }                                                                                                   \
+    ZQO_API void zqo_add_force_adjoint_##SFX(int W, int H, int D, const R* u, const R* v, const R* w,    \
+                                             const uint8_t* occ, const zqs_params* P, R* gu, R* gv,     \
+                                             R* gw, R* gT, R* grho, R* gF) {                            \
+        zqo::add_force_adjoint<R>(zqo::Dims{W, H, D}, u, v, w, occ, *P, gu, gv, gw, gT, grho, gF);      \
+    }                                                                                                   \
+    ZQO_API int zqo_step_adjoint_##SFX(int W, int H, int D, const R* u, const R* v, const R* w,          \
+                                       const R* T, const R* rho, const uint8_t* occ, const zqs_params* P, \
+                                       const R* F, R* gu, R* gv, R* gw, R* gT, R* grho, R* gF) {        \
+        return zqo::step_adjoint<R>(zqo::Dims{W, H, D}, u, v, w, T, rho, occ, *P, F, gu, gv, gw, gT,    \
+                                    grho, gF);                                                          \
+    }                                                                                                   \
+    ZQO_API int zqo_control_loss_##SFX(int W, int H, int D, const R* u, const R* v, const R* w,          \
+                                       const R* T, const R* rho, const uint8_t* occ, const zqs_params* P, \
+                                       int nsteps, const R* F, const R* target, double* loss, R* gF,    \
+                                       R* g0) {                                                         \
+        return zqo::control_loss<R>(zqo::Dims{W, H, D}, u, v, w, T, rho, occ, *P, nsteps, F, target,    \
+                                    loss, gF, g0);                                                      \
     }                                                                                                   \
     ZQO_API int zqo_step_##SFX(int W, int H, int D, R* u, R* v, R* w, R* T, R* rho,                     \
                                const uint8_t* occ, const zqs_params* P, int nsteps, R* p_out) {         \
