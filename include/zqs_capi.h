@@ -244,6 +244,50 @@ ZQS_API int zqs_batch_set_sor_variant(zqs_batch* b, int index, int zchunk);
 ZQS_API int64_t zqs_batch_launch_count(const zqs_batch* b);
 ZQS_API int zqs_batch_synchronize(zqs_batch* b, void* stream);
 
+/* ---- external force and reverse mode ----------------------------------------
+ * No counterpart in the reference.  An external per-cell force F is added to
+ * the cell force of every step after the buoyancy terms (force stage, before
+ * the face averaging).  F holds 3*W*H*D floats, component-major (x, y, z),
+ * each component dense with x fastest; NULL removes it. */
+ZQS_API int zqs_grid_set_force(zqs_grid* g, const float* F, int src_on_device, void* stream);
+
+/* A reverse-mode session over nsteps steps of a grid with a control force F,
+ * for losses on the final density.  The forward pass keeps the state every
+ * checkpoint_every steps; the backward pass recomputes each segment from its
+ * checkpoint and runs the adjoint kernels of every stage in reverse order
+ * (transposed-trilinear scatters with FP32 atomics for the advections, the
+ * transposed force stencil, the red-black SOR transposed half-sweep by
+ * half-sweep).  Requires MAC velocity and scalar advection and at most 32
+ * backtrace substeps (ZQS_EUNSUPPORTED otherwise).  Results of the backward
+ * pass vary in the last bits from run to run (atomic accumulation order). */
+typedef struct zqs_adjoint zqs_adjoint;
+
+typedef struct zqs_adjoint_info {
+    int64_t device_bytes;       /* memory the session holds (checkpoints, segment, adjoint fields, work grid) */
+    int64_t launches_forward;   /* kernel launches of the last forward pass */
+    int64_t launches_backward;  /* kernel launches of the last backward pass */
+    int32_t nsteps, checkpoint_every, checkpoints;
+    int32_t pad;
+} zqs_adjoint_info;
+
+ZQS_API int zqs_adjoint_create(zqs_adjoint** out, zqs_grid* g, int nsteps, int checkpoint_every);
+ZQS_API int zqs_adjoint_destroy(zqs_adjoint* a);
+
+/* Sets F (as zqs_grid_set_force) and advances the grid nsteps steps from its
+ * current state, keeping the checkpoints; the grid ends in the final state. */
+ZQS_API int zqs_adjoint_forward(zqs_adjoint* a, const float* F, int src_on_device, void* stream);
+
+/* g_density: dL/d(final density), W*H*D floats dense (e.g. 2*(rho - target)
+ * for L = sum (rho - target)^2).  grad_F receives dL/dF (3*W*H*D floats, the
+ * layout of F).  The grid is not modified. */
+ZQS_API int zqs_adjoint_backward(zqs_adjoint* a, const float* g_density, float* grad_F, int on_device,
+                                 void* stream);
+
+/* After zqs_adjoint_backward: dL/d(initial state) for ZQS_FIELD_U/V/W,
+ * ZQS_FIELD_TEMPERATURE or ZQS_FIELD_DENSITY, in the field's dense layout. */
+ZQS_API int zqs_adjoint_download(zqs_adjoint* a, int field, void* dst, int dst_on_device, void* stream);
+ZQS_API int zqs_adjoint_get_info(const zqs_adjoint* a, zqs_adjoint_info* out);
+
 #ifdef __cplusplus
 }
 #endif

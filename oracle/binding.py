@@ -56,13 +56,15 @@ class Oracle:
         u = np.empty((D, H, W + 1), self.dtype)
         v = np.empty((D, H + 1, W), self.dtype)
         w = np.empty((D + 1, H, W), self.dtype)
-        self._f("regular4_to_mac")(W, H, D, _p(self.arr(vel4)), _p(u), _p(v), _p(w))
+        v4 = self.arr(vel4)  # held: a converted temporary must outlive the call
+        self._f("regular4_to_mac")(W, H, D, _p(v4), _p(u), _p(v), _p(w))
         return u, v, w
 
     def vorticity(self, W, H, D, u, v, w, h):
         vort = np.empty((D, H, W, 3), self.dtype)
         vs = np.empty((D, H, W), self.dtype)
-        self._f("vorticity")(W, H, D, _p(self.arr(u)), _p(self.arr(v)), _p(self.arr(w)),
+        u, v, w = self.arr(u), self.arr(v), self.arr(w)
+        self._f("vorticity")(W, H, D, _p(u), _p(v), _p(w),
                              (C.c_float if self.sfx == "f32" else C.c_double)(h), _p(vort), _p(vs))
         return vort, vs
 
@@ -103,12 +105,14 @@ class Oracle:
     # -- control problem and reverse mode ------------------------------------------
     def step_ctrl(self, W, H, D, st, occ, params, F, nsteps=1):
         """nsteps steps with the external per-cell force F (3, D, H, W)."""
+        Fa = self.arr(F)
         return self._f("step_ctrl")(W, H, D, _p(st["u"]), _p(st["v"]), _p(st["w"]), _p(st["T"]), _p(st["rho"]),
-                                    _p(occ), C.byref(params), nsteps, _p(self.arr(F)))
+                                    _p(occ), C.byref(params), nsteps, _p(Fa))
 
     def add_force_ctrl(self, W, H, D, st, occ, params, F):
+        Fa = self.arr(F)
         self._f("add_force_ctrl")(W, H, D, _p(st["u"]), _p(st["v"]), _p(st["w"]), _p(occ), _p(st["T"]),
-                                  _p(st["rho"]), C.byref(params), _p(self.arr(F)))
+                                  _p(st["rho"]), C.byref(params), _p(Fa))
 
     def project_adjoint(self, W, H, D, g, occ, params):
         """In place on g = {u, v, w}: adjoint of the projected velocity -> of the input."""
@@ -119,16 +123,18 @@ class Oracle:
         gTin = np.zeros((D, H, W), self.dtype)
         gDin = np.zeros((D, H, W), self.dtype)
         gv = {k: np.zeros_like(self.arr(vel[k])) for k in ("u", "v", "w")}
+        Tin, Din, gT, gD = self.arr(Tin), self.arr(Din), self.arr(gT), self.arr(gD)
         self._f("advect_scalar_adjoint")(W, H, D, _p(vel["u"]), _p(vel["v"]), _p(vel["w"]), _p(occ),
-                                         _p(self.arr(Tin)), _p(self.arr(Din)), _p(self.arr(gT)), _p(self.arr(gD)),
+                                         _p(Tin), _p(Din), _p(gT), _p(gD),
                                          _p(gTin), _p(gDin), _p(gv["u"]), _p(gv["v"]), _p(gv["w"]), C.byref(params))
         return gTin, gDin, gv
 
     def advect_velocity_adjoint(self, W, H, D, vel, occ, params, g3):
         g2 = {k: np.zeros_like(self.arr(vel[k])) for k in ("u", "v", "w")}
+        a3 = {k: self.arr(g3[k]) for k in ("u", "v", "w")}
         self._f("advect_velocity_adjoint")(W, H, D, _p(vel["u"]), _p(vel["v"]), _p(vel["w"]), _p(occ),
-                                           C.byref(params), _p(self.arr(g3["u"])), _p(self.arr(g3["v"])),
-                                           _p(self.arr(g3["w"])), _p(g2["u"]), _p(g2["v"]), _p(g2["w"]))
+                                           C.byref(params), _p(a3["u"]), _p(a3["v"]),
+                                           _p(a3["w"]), _p(g2["u"]), _p(g2["v"]), _p(g2["w"]))
         return g2
 
     def add_force_adjoint(self, W, H, D, vel, occ, params, g, gT, grho, gF=None):
@@ -138,8 +144,9 @@ class Oracle:
 
     def step_adjoint(self, W, H, D, st, occ, params, F, g, gF):
         """Adjoint of one step(F) from state st; g (state adjoint) in place, gF += dL/dF."""
+        Fa = None if F is None else self.arr(F)
         return self._f("step_adjoint")(W, H, D, _p(st["u"]), _p(st["v"]), _p(st["w"]), _p(st["T"]), _p(st["rho"]),
-                                       _p(occ), C.byref(params), _p(None if F is None else self.arr(F)),
+                                       _p(occ), C.byref(params), _p(Fa),
                                        _p(g["u"]), _p(g["v"]), _p(g["w"]), _p(g["T"]), _p(g["rho"]), _p(gF))
 
     def control_loss(self, W, H, D, st, occ, params, nsteps, F, target, grad=False):
@@ -149,9 +156,11 @@ class Oracle:
         gF = np.zeros((3, D, H, W), self.dtype) if grad else None
         n0 = sum(st[k].size for k in ("u", "v", "w", "T", "rho"))
         g0 = np.zeros(n0, self.dtype) if grad else None
-        rc = self._f("control_loss")(W, H, D, _p(self.arr(st["u"])), _p(self.arr(st["v"])), _p(self.arr(st["w"])),
-                                     _p(self.arr(st["T"])), _p(self.arr(st["rho"])), _p(occ), C.byref(params),
-                                     nsteps, _p(self.arr(F)), _p(self.arr(target)), C.byref(loss), _p(gF), _p(g0))
+        s = {k: self.arr(st[k]) for k in ("u", "v", "w", "T", "rho")}
+        Fa, ta = self.arr(F), self.arr(target)
+        rc = self._f("control_loss")(W, H, D, _p(s["u"]), _p(s["v"]), _p(s["w"]),
+                                     _p(s["T"]), _p(s["rho"]), _p(occ), C.byref(params),
+                                     nsteps, _p(Fa), _p(ta), C.byref(loss), _p(gF), _p(g0))
         if rc != 0:
             raise RuntimeError(f"oracle control_loss failed: {rc}")
         return (loss.value, gF, g0) if grad else loss.value

@@ -69,6 +69,12 @@ class SorVariant(C.Structure):
                 ("smem_bytes", C.c_int64)]
 
 
+class AdjointInfo(C.Structure):
+    _fields_ = [("device_bytes", C.c_int64), ("launches_forward", C.c_int64), ("launches_backward", C.c_int64),
+                ("nsteps", C.c_int32), ("checkpoint_every", C.c_int32), ("checkpoints", C.c_int32),
+                ("pad", C.c_int32)]
+
+
 class Layout(C.Structure):
     _fields_ = [("W", C.c_int32), ("H", C.c_int32), ("D", C.c_int32), ("pitch_x", C.c_int32),
                 ("rows", C.c_int32), ("planes", C.c_int32), ("plane_elems", C.c_int64),
@@ -85,6 +91,8 @@ CAPI_SYMBOLS = [
     "zqs_sor_variant_info", "zqs_grid_set_sor_variant", "zqs_grid_synchronize", "zqs_grid_launch_count",
     "zqs_batch_create", "zqs_batch_destroy", "zqs_batch_step", "zqs_batch_use_graph", "zqs_batch_set_sor_variant",
     "zqs_batch_launch_count", "zqs_batch_synchronize",
+    "zqs_grid_set_force", "zqs_adjoint_create", "zqs_adjoint_destroy", "zqs_adjoint_forward",
+    "zqs_adjoint_backward", "zqs_adjoint_download", "zqs_adjoint_get_info",
 ]
 LEGACY_C_SYMBOLS = ["ZQ_Cuda_Prepare_Advection", "Advect_Velocity", "Advect_Scalar", "AddForce3D",
                     "Attenuation3D", "zqs_project_sor", "zqs_project_sor_noalloc"]
@@ -152,6 +160,13 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.zqs_batch_launch_count.argtypes = [vp]
     lib.zqs_batch_launch_count.restype = C.c_int64
     lib.zqs_batch_synchronize.argtypes = [vp, vp]
+    lib.zqs_grid_set_force.argtypes = [vp, vp, i, vp]
+    lib.zqs_adjoint_create.argtypes = [C.POINTER(vp), vp, i, i]
+    lib.zqs_adjoint_destroy.argtypes = [vp]
+    lib.zqs_adjoint_forward.argtypes = [vp, vp, i, vp]
+    lib.zqs_adjoint_backward.argtypes = [vp, vp, vp, i, vp]
+    lib.zqs_adjoint_download.argtypes = [vp, i, vp, i, vp]
+    lib.zqs_adjoint_get_info.argtypes = [vp, C.POINTER(AdjointInfo)]
     # legacy shims
     lib.ZQ_Cuda_Prepare_Advection.argtypes = [C.c_uint, C.c_uint, C.c_uint, f, C.c_uint, f]
     lib.ZQ_Cuda_Prepare_Advection.restype = None
@@ -348,6 +363,21 @@ class Grid:
     def launch_count(self) -> int:
         return int(self.lib.zqs_grid_launch_count(self.h))
 
+    def set_force(self, F: np.ndarray | None):
+        """External per-cell force (3, D, H, W) added every step; None removes it."""
+        if F is None:
+            check(self.lib.zqs_grid_set_force(self.h, None, 0, None), "zqs_grid_set_force")
+            return
+        a = np.ascontiguousarray(F, dtype=np.float32)
+        if a.size != 3 * self.W * self.H * self.D:
+            raise ValueError("force must hold 3*W*H*D values")
+        check(self.lib.zqs_grid_set_force(self.h, C.c_void_p(ptr(a)), 0, None), "zqs_grid_set_force")
+        self.sync()
+
+    def set_force_device(self, dev_ptr: int, stream: int | None = None):
+        check(self.lib.zqs_grid_set_force(self.h, C.c_void_p(dev_ptr), 1, C.c_void_p(stream or 0)),
+              "zqs_grid_set_force")
+
 
 class Batch:
     """Many grids advanced together (a zqs_batch handle): one persistent launch
@@ -394,3 +424,65 @@ class Batch:
 
     def launch_count(self) -> int:
         return int(self.lib.zqs_batch_launch_count(self.h))
+
+
+class Adjoint:
+    """Reverse-mode session (a zqs_adjoint handle) over nsteps steps of a grid
+    with a control force, for losses on the final density."""
+
+    def __init__(self, grid: Grid, nsteps: int, checkpoint_every: int = 8):
+        self.lib = load()
+        self.grid = grid
+        self.nsteps = nsteps
+        h = C.c_void_p()
+        check(self.lib.zqs_adjoint_create(C.byref(h), grid.h, nsteps, checkpoint_every), "zqs_adjoint_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            self.lib.zqs_adjoint_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def forward(self, F: np.ndarray | None):
+        g = self.grid
+        if F is None:
+            check(self.lib.zqs_adjoint_forward(self.h, None, 0, None), "zqs_adjoint_forward")
+        else:
+            a = np.ascontiguousarray(F, dtype=np.float32)
+            check(self.lib.zqs_adjoint_forward(self.h, C.c_void_p(ptr(a)), 0, None), "zqs_adjoint_forward")
+        g.sync()
+
+    def forward_device(self, dev_ptr: int, stream: int | None = None):
+        check(self.lib.zqs_adjoint_forward(self.h, C.c_void_p(dev_ptr), 1, C.c_void_p(stream or 0)),
+              "zqs_adjoint_forward")
+
+    def backward(self, g_density: np.ndarray) -> np.ndarray:
+        g = self.grid
+        gd = np.ascontiguousarray(g_density, dtype=np.float32)
+        out = np.empty((3, g.D, g.H, g.W), np.float32)
+        check(self.lib.zqs_adjoint_backward(self.h, C.c_void_p(ptr(gd)), C.c_void_p(ptr(out)), 0, None),
+              "zqs_adjoint_backward")
+        g.sync()
+        return out
+
+    def backward_device(self, g_density_ptr: int, grad_ptr: int, stream: int | None = None):
+        check(self.lib.zqs_adjoint_backward(self.h, C.c_void_p(g_density_ptr), C.c_void_p(grad_ptr), 1,
+                                            C.c_void_p(stream or 0)), "zqs_adjoint_backward")
+
+    def initial_adjoint(self, field: int) -> np.ndarray:
+        g = self.grid
+        out = np.empty(field_shape(field, g.W, g.H, g.D), np.float32)
+        check(self.lib.zqs_adjoint_download(self.h, field, C.c_void_p(ptr(out)), 0, None), "zqs_adjoint_download")
+        g.sync()
+        return out
+
+    def info(self) -> AdjointInfo:
+        inf = AdjointInfo()
+        check(self.lib.zqs_adjoint_get_info(self.h, C.byref(inf)), "zqs_adjoint_get_info")
+        return inf

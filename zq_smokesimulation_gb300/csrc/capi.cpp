@@ -54,6 +54,7 @@ int make_kparams(const zqs_params& p, KParams& kp) {
     kp.solver = p.solver;
     kp.mean_override = 0;
     kp.mean_value = 0.0f;
+    kp.fext = nullptr;
     return ZQS_OK;
 }
 
@@ -306,6 +307,7 @@ ZQS_API int zqs_grid_destroy(zqs_grid* g) {
     cudaStreamDestroy(g->own);
     cudaFree(g->occ_dense);
     cudaFree(g->base);
+    if (g->fext_base) cudaFree(g->fext_base);
     delete g;
     return ZQS_OK;
 }
@@ -337,6 +339,7 @@ ZQS_API int zqs_grid_set_params(zqs_grid* g, const zqs_params* p) {
     bool solver_changed = !g->has_params || g->params.solver != p->solver;
     g->params = *p;
     make_kparams(*p, g->kp);
+    if (g->fext_on) g->kp.fext = g->fext_base + g->g.L.plane;
     g->src.n = p->n_sources;
     for (int s = 0; s < p->n_sources; s++) g->src.s[s] = p->sources[s];
     g->has_params = true;

@@ -87,6 +87,11 @@ __device__ __forceinline__ void force_cell_tile(const Layout& L, const float4* _
     float fz = kp.cc * (gx * o.y - gy * o.x);
     fy = fy + kp.beta * (__ldg(T + c) - kp.tamb);
     fy = fy - kp.alpha * __ldg(rho + c);
+    if (kp.fext) {
+        fx = fx + __ldg(kp.fext + c);
+        fy = fy + __ldg(kp.fext + L.elems + c);
+        fz = fz + __ldg(kp.fext + 2 * L.elems + c);
+    }
     force[c] = make_float4(fx, fy, fz, 0.0f);
 }
 

@@ -27,6 +27,8 @@ struct zqs_grid {
     long long graph_launches[4] = {0, 0, 0, 0};
     float* graph_p_last[4] = {nullptr, nullptr, nullptr, nullptr};
     long long gen = 0;  // bumped whenever parameters, occupancy or the SOR setup change
+    float* fext_base = nullptr;  // external per-cell force, 3 padded cell fields (allocated on first use)
+    bool fext_on = false;
 
     cudaStream_t pick(void* s) const { return s ? (cudaStream_t)s : own; }
 

@@ -57,6 +57,10 @@ struct KParams {
     int solver;
     int mean_override;  // closed solver: subtract mean_value instead of the FP64 mean
     float mean_value;
+    // External per-cell force added to the cell force after the buoyancy terms
+    // (the control of the adjoint problem): component q of cell c at
+    // fext[q*elems + c] in the padded layout; null when absent.
+    const float* fext;
 };
 
 struct SourceList {

@@ -1,0 +1,179 @@
+// Device helpers of the semi-Lagrangian advection, shared by the forward
+// kernels (kernels_advect.cu) and their reverse mode (kernels_adjoint.cu).
+// Internal header.
+#pragma once
+
+#include "zqs_internal.h"
+
+namespace zqs {
+
+struct Ax {
+    int i0, i1;
+    float t;
+};
+
+// Clamp-to-edge linear filter along one axis; g in texel-index units.
+__device__ __forceinline__ Ax axis(float g, int n) {
+    g = fminf(fmaxf(g, -1.0f), (float)n);
+    float f = floorf(g);
+    Ax a;
+    a.t = g - f;
+    int i = (int)f;
+    a.i0 = min(max(i, 0), n - 1);
+    a.i1 = min(max(i + 1, 0), n - 1);
+    return a;
+}
+
+__device__ __forceinline__ float lerpf(float a, float b, float t) { return a + t * (b - a); }
+
+struct Corners {
+    int r00, r10, r01, r11;  // row offsets (j0,k0) (j1,k0) (j0,k1) (j1,k1)
+    int i0, i1;
+    float tx, ty, tz;
+};
+
+__device__ __forceinline__ Corners corners(const Layout& L, int nx, int ny, int nz, float gx, float gy, float gz) {
+    Ax ax = axis(gx, nx), ay = axis(gy, ny), az = axis(gz, nz);
+    Corners c;
+    c.r00 = (az.i0 * L.py + ay.i0) * L.px;
+    c.r10 = (az.i0 * L.py + ay.i1) * L.px;
+    c.r01 = (az.i1 * L.py + ay.i0) * L.px;
+    c.r11 = (az.i1 * L.py + ay.i1) * L.px;
+    c.i0 = ax.i0;
+    c.i1 = ax.i1;
+    c.tx = ax.t;
+    c.ty = ay.t;
+    c.tz = az.t;
+    return c;
+}
+
+// x, then y, then z (same tree as the oracle's trilinear()).
+__device__ __forceinline__ float tri(const float* __restrict__ f, const Corners& c, float scale) {
+    float c00 = lerpf(__ldg(f + c.r00 + c.i0) * scale, __ldg(f + c.r00 + c.i1) * scale, c.tx);
+    float c10 = lerpf(__ldg(f + c.r10 + c.i0) * scale, __ldg(f + c.r10 + c.i1) * scale, c.tx);
+    float c01 = lerpf(__ldg(f + c.r01 + c.i0) * scale, __ldg(f + c.r01 + c.i1) * scale, c.tx);
+    float c11 = lerpf(__ldg(f + c.r11 + c.i0) * scale, __ldg(f + c.r11 + c.i1) * scale, c.tx);
+    float c0 = lerpf(c00, c10, c.ty);
+    float c1 = lerpf(c01, c11, c.ty);
+    return lerpf(c0, c1, c.tz);
+}
+__device__ __forceinline__ float tri_unscaled(const float* __restrict__ f, const Corners& c) {
+    float c00 = lerpf(__ldg(f + c.r00 + c.i0), __ldg(f + c.r00 + c.i1), c.tx);
+    float c10 = lerpf(__ldg(f + c.r10 + c.i0), __ldg(f + c.r10 + c.i1), c.tx);
+    float c01 = lerpf(__ldg(f + c.r01 + c.i0), __ldg(f + c.r01 + c.i1), c.tx);
+    float c11 = lerpf(__ldg(f + c.r11 + c.i0), __ldg(f + c.r11 + c.i1), c.tx);
+    float c0 = lerpf(c00, c10, c.ty);
+    float c1 = lerpf(c01, c11, c.ty);
+    return lerpf(c0, c1, c.tz);
+}
+__device__ __forceinline__ float3 tri4(const float4* __restrict__ f, const Corners& c) {
+    float4 a00 = __ldg(f + c.r00 + c.i0), b00 = __ldg(f + c.r00 + c.i1);
+    float4 a10 = __ldg(f + c.r10 + c.i0), b10 = __ldg(f + c.r10 + c.i1);
+    float4 a01 = __ldg(f + c.r01 + c.i0), b01 = __ldg(f + c.r01 + c.i1);
+    float4 a11 = __ldg(f + c.r11 + c.i0), b11 = __ldg(f + c.r11 + c.i1);
+    float3 r;
+    {
+        float c00 = lerpf(a00.x, b00.x, c.tx), c10 = lerpf(a10.x, b10.x, c.tx);
+        float c01 = lerpf(a01.x, b01.x, c.tx), c11 = lerpf(a11.x, b11.x, c.tx);
+        r.x = lerpf(lerpf(c00, c10, c.ty), lerpf(c01, c11, c.ty), c.tz);
+    }
+    {
+        float c00 = lerpf(a00.y, b00.y, c.tx), c10 = lerpf(a10.y, b10.y, c.tx);
+        float c01 = lerpf(a01.y, b01.y, c.tx), c11 = lerpf(a11.y, b11.y, c.tx);
+        r.y = lerpf(lerpf(c00, c10, c.ty), lerpf(c01, c11, c.ty), c.tz);
+    }
+    {
+        float c00 = lerpf(a00.z, b00.z, c.tx), c10 = lerpf(a10.z, b10.z, c.tx);
+        float c01 = lerpf(a01.z, b01.z, c.tx), c11 = lerpf(a11.z, b11.z, c.tx);
+        r.z = lerpf(lerpf(c00, c10, c.ty), lerpf(c01, c11, c.ty), c.tz);
+    }
+    return r;
+}
+__device__ __forceinline__ float tri4c(const float4* __restrict__ f4, int q, const Corners& c) {
+    const float* f = reinterpret_cast<const float*>(f4);
+    auto at = [&](int o) -> float { return __ldg(f + (size_t)o * 4 + q); };
+    float c00 = lerpf(at(c.r00 + c.i0), at(c.r00 + c.i1), c.tx);
+    float c10 = lerpf(at(c.r10 + c.i0), at(c.r10 + c.i1), c.tx);
+    float c01 = lerpf(at(c.r01 + c.i0), at(c.r01 + c.i1), c.tx);
+    float c11 = lerpf(at(c.r11 + c.i0), at(c.r11 + c.i1), c.tx);
+    return lerpf(lerpf(c00, c10, c.ty), lerpf(c01, c11, c.ty), c.tz);
+}
+
+struct MacVel {
+    Layout L;
+    const float *u, *v, *w;
+    __device__ __forceinline__ void operator()(float px, float py, float pz, float& vx, float& vy, float& vz) const {
+        vx = tri_unscaled(u, corners(L, L.W + 1, L.H, L.D, px, py - 0.5f, pz - 0.5f));
+        vy = tri_unscaled(v, corners(L, L.W, L.H + 1, L.D, px - 0.5f, py, pz - 0.5f));
+        vz = tri_unscaled(w, corners(L, L.W, L.H, L.D + 1, px - 0.5f, py - 0.5f, pz));
+    }
+};
+struct RegVel {
+    Layout L;
+    const float4* vel4;
+    __device__ __forceinline__ void operator()(float px, float py, float pz, float& vx, float& vy, float& vz) const {
+        float3 r = tri4(vel4, corners(L, L.W, L.H, L.D, px - 0.5f, py - 0.5f, pz - 0.5f));
+        vx = r.x;
+        vy = r.y;
+        vz = r.z;
+    }
+};
+
+// The reference backtrace (e.g. ZQ_CUDA_Advection3D.cu:253-273): test the
+// point (inside [0,W]x[0,H]x[0,D] and its clamped floor cell free), remember
+// it, move by -(vel*dt_sub)/h, resample; `steps` moves at most.  The result
+// is the last point that passed the test before the final move.  The velocity
+// after the final move is never used, so it is not sampled.
+template <class VelF>
+__device__ __forceinline__ void backtrace(const Layout& L, const uint8_t* __restrict__ flags, const VelF& vel,
+                                          const KParams& kp, float& px, float& py, float& pz) {
+    float vx, vy, vz;
+    vel(px, py, pz, vx, vy, vz);
+    float lx = px, ly = py, lz = pz;
+    const float Wf = (float)L.W, Hf = (float)L.H, Df = (float)L.D;
+    auto ok = [&](float x, float y, float z) -> bool {
+        if (!(x >= 0.0f && x <= Wf && y >= 0.0f && y <= Hf && z >= 0.0f && z <= Df)) return false;
+        int i = min(max((int)floorf(x), 0), L.W - 1);
+        int j = min(max((int)floorf(y), 0), L.H - 1);
+        int k = min(max((int)floorf(z), 0), L.D - 1);
+        return (__ldg(flags + lidx(L, i, j, k)) & F_FREE) != 0;
+    };
+    const float dt = kp.dt_sub;
+    int istep = 0;
+    bool broke = false;
+    do {
+        if (!ok(px, py, pz)) {
+            broke = true;
+            break;
+        }
+        lx = px;
+        ly = py;
+        lz = pz;
+        if (kp.inv_h != 0.0f) {
+            px = px - (vx * dt) * kp.inv_h;
+            py = py - (vy * dt) * kp.inv_h;
+            pz = pz - (vz * dt) * kp.inv_h;
+        } else {
+            px = px - (vx * dt) / kp.h;
+            py = py - (vy * dt) / kp.h;
+            pz = pz - (vz * dt) / kp.h;
+        }
+        istep++;
+        if (istep < kp.substeps) vel(px, py, pz, vx, vy, vz);
+    } while (istep < kp.substeps);
+    if (kp.full && !broke && ok(px, py, pz)) {
+        lx = px;
+        ly = py;
+        lz = pz;
+    }
+    px = lx;
+    py = ly;
+    pz = lz;
+}
+
+__device__ __forceinline__ bool face_live(uint8_t fl, uint8_t bit, int idx, int n, bool open) {
+    if (!(fl & bit)) return false;
+    return open || (idx > 0 && idx < n);
+}
+
+}  // namespace zqs

@@ -20,6 +20,11 @@ Named configurations (cell units, y is up, gravity along -y):
                  source (r ~ U[.06,.12] x the shortest edge, in the bottom 15%),
                  alpha ~ U[.05,.2], beta ~ U[.2,.8], eps ~ U[0,.3],
                  dt ~ U[.25,.75]; K=200, 100 steps (batch_mixed())
+  control64 / control128  the adjoint problem: plain64's walls, forces and
+                 solver at N^3 (source r = 6N/64 at (N/2, N/8, N/2)), a zero
+                 per-cell control force, 64 steps, and a target density that
+                 is a Gaussian blob (sigma 8 cells, peak 1) centred uniformly
+                 in the upper half (control_problem())
 "Walls closed except an open top" = the open (Dirichlet p=0 outside) solver
 with an occupied layer at x=0, x=W-1, y=0, z=0, z=D-1: outside the top face the
 pressure is 0, every other side is a solid wall, like ZQ_InitFineGrid3D's
@@ -280,3 +285,27 @@ def batch_member(idx: int, *, seed: int = 0, K: int = 200, edges=(32, 48, 64, 96
 def batch_mixed(n: int = 64, *, seed: int = 0, K: int = 200, edges=(32, 48, 64, 96, 128)) -> list[Workload]:
     """The mixed-size batch: n seeded instances (batch_member(0..n-1))."""
     return [batch_member(i, seed=seed, K=K, edges=edges) for i in range(n)]
+
+
+def control_problem(N: int = 64, *, seed: int = 0, K: int = 200, nsteps: int = 64, substeps: int = 20,
+                    sigma: float = 8.0):
+    """The force-field control problem at N^3: (workload, target density).
+
+    Loss L(F) = sum_cells (rho_final - target)^2 after nsteps steps with the
+    per-cell force F (3, N, N, N) added every step; F = 0 initially."""
+    occ = walls_open_top(N, N, N)
+    p = smoke_params(N, K, substeps=substeps)
+    p.set_sources([sphere(N / 2, N / 8, N / 2, 6.0 * N / 64)])
+    u, v, w = initial_velocity(occ, seed)
+    T = np.zeros((N, N, N), np.float32)
+    rho = np.zeros((N, N, N), np.float32)
+    wl = Workload(f"control{N}", N, N, N, p, occ, u, v, w, T, rho, nsteps, {"seed": seed, "K": K})
+    c = uniform01(seed + 4242, 3)
+    cx = float(np.float32(sigma) + np.float32(N - 2 * sigma) * c[0])
+    cy = float(np.float32(N / 2) + np.float32(N / 2 - sigma) * c[1])
+    cz = float(np.float32(sigma) + np.float32(N - 2 * sigma) * c[2])
+    z, y, x = np.meshgrid(np.arange(N) + 0.5, np.arange(N) + 0.5, np.arange(N) + 0.5, indexing="ij")
+    r2 = (x - cx) ** 2 + (y - cy) ** 2 + (z - cz) ** 2
+    target = np.exp(-r2 / (2.0 * sigma * sigma)).astype(np.float32)
+    wl.meta.update({"target_centre": (cx, cy, cz), "sigma": sigma})
+    return wl, target
