@@ -51,6 +51,9 @@ def parse():
     ap.add_argument("--batch-steps", type=int, default=10)
     ap.add_argument("--batch-variant", type=int, default=-1)
     ap.add_argument("--batch-zchunk", type=int, default=0)
+    ap.add_argument("--adjoint", default="64,128", help="control-problem sizes timed for the reverse mode ('' = skip)")
+    ap.add_argument("--adjoint-steps", type=int, default=64)
+    ap.add_argument("--checkpoint-every", type=int, default=8)
     return ap.parse_args()
 
 
@@ -248,6 +251,83 @@ def measure_batch(args, stream, rel_check: bool = True):
             "step_alg_gbs": step_alg / (ms_b / steps * 1e-3) / 1e9}
 
 
+def measure_adjoint(args, stream, N: int):
+    """The force-field control problem at N^3: forward (nsteps steps with the
+    control force, checkpoints every k) and backward (recomputation + adjoint
+    kernels) timed with CUDA events; device memory the problem holds."""
+    import numpy as np
+    import torch
+
+    from zq_smokesimulation_gb300 import capi
+    from zq_smokesimulation_gb300 import workloads as wl
+
+    nsteps = args.adjoint_steps
+    w, target = wl.control_problem(N, nsteps=nsteps)
+    sp = stream.cuda_stream
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    g = capi.Grid(w.W, w.H, w.D)
+    g.set_params(w.params)
+    g.load_state(w.occ, w.u, w.v, w.w, w.T, w.rho)
+    adj = capi.Adjoint(g, nsteps, args.checkpoint_every)
+    F = torch.zeros((3, N, N, N), device="cuda", dtype=torch.float32)
+    tgt = torch.tensor(target, device="cuda")
+    rho = torch.empty((N, N, N), device="cuda", dtype=torch.float32)
+    grad = torch.empty_like(F)
+
+    def ev():
+        return torch.cuda.Event(enable_timing=True)
+
+    def reset():
+        for f, arr in ((capi.FIELD_U, w.u), (capi.FIELD_V, w.v), (capi.FIELD_W, w.w),
+                       (capi.FIELD_TEMPERATURE, w.T), (capi.FIELD_DENSITY, w.rho)):
+            g.upload(f, arr)
+
+    fwd_ms, bwd_ms = [], []
+    for rep in range(3):
+        reset()
+        torch.cuda.synchronize()
+        a, b, c = ev(), ev(), ev()
+        a.record(stream)
+        adj.forward_device(F.data_ptr(), sp)
+        b.record(stream)
+        capi.check(g.lib.zqs_grid_download(g.h, capi.FIELD_DENSITY, capi.C.c_void_p(rho.data_ptr()), 1,
+                                           capi.C.c_void_p(sp)), "download")
+        gd = 2.0 * (rho - tgt)
+        c0 = ev()
+        c0.record(stream)
+        adj.backward_device(gd.data_ptr(), grad.data_ptr(), sp)
+        c.record(stream)
+        c.synchronize()
+        fwd_ms.append(a.elapsed_time(b))
+        bwd_ms.append(c0.elapsed_time(c))
+    free1 = torch.cuda.mem_get_info()[0]
+    # plain forward of the same steps (graph replay, no checkpoint copies)
+    reset()
+    g.set_force_device(F.data_ptr(), sp)
+    g.step(1, sp)
+    torch.cuda.synchronize()
+    a, b = ev(), ev()
+    a.record(stream)
+    g.step(nsteps, sp)
+    b.record(stream)
+    b.synchronize()
+    plain_ms = a.elapsed_time(b)
+    loss = float(((rho - tgt) ** 2).sum())
+    inf = adj.info()
+    out = {"grid": [N, N, N], "steps": nsteps, "checkpoint_every": args.checkpoint_every,
+           "sor_iters": int(w.params.sor_iters), "substeps": int(w.params.substeps),
+           "forward_ms": min(fwd_ms), "backward_ms": min(bwd_ms), "plain_forward_ms": plain_ms,
+           "ratio_backward_to_forward": min(bwd_ms) / min(fwd_ms),
+           "ratio_forward_plus_backward_to_forward": (min(fwd_ms) + min(bwd_ms)) / min(fwd_ms),
+           "loss": loss, "grad_norm": float(grad.norm()),
+           "session_bytes": int(inf.device_bytes), "device_bytes_used": int(free0 - free1),
+           "launches_backward": int(inf.launches_backward)}
+    adj.close()
+    g.close()
+    return out
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -358,6 +438,9 @@ def run_ours(args):
     batch = None
     if args.batch and world == 1:
         batch = measure_batch(args, stream)
+    adjoint = None
+    if args.adjoint and world == 1:
+        adjoint = {f"control{n}": measure_adjoint(args, stream, int(n)) for n in args.adjoint.split(",") if n}
     clocks = sampler.stop()
 
     if dist is not None:
@@ -388,7 +471,7 @@ def run_ours(args):
                          "step_alg_gbs": step_alg / (ms / args.steps * 1e-3) / 1e9,
                          "step_frac": step_alg / (ms / args.steps * 1e-3) / 1e9 / peak},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches_per_step * args.steps, "clocks": clocks,
-            "batch": batch,
+            "batch": batch, "adjoint": adjoint,
         }
         print(json.dumps(line), flush=True)
     g.close()

@@ -173,3 +173,62 @@ def test_torch_autograd_function(zqs_lib, oracle64):
     # a second evaluation restarts from the initial state
     rho2 = ctl(Ft.detach())
     assert torch.equal(rho2, rho.detach())
+
+
+def _control64_check(ndirs, seed=0):
+    """The control problem at 64^3 (64 steps, checkpoints every 8): GPU
+    gradient against the FP64 CPU gradient, and against FP64 central
+    differences along ndirs seeded unit directions (h = 1e-3)."""
+    import json
+    import os
+
+    from oracle.binding import Oracle
+    o64 = Oracle(np.float64)
+    w, target = wl.control_problem(64, seed=seed)
+    F = np.zeros((3, 64, 64, 64), np.float32)
+    rho, gF, a, g = gpu_gradient(w, F, target, w.steps, 8)
+    L64, gF64, _ = o64.control_loss(64, 64, 64, o64.state(w), w.occ, w.params, w.steps, F, target, grad=True)
+    gnorm = float(np.linalg.norm(gF64))
+    rel64 = rel_l2(gF, gF64)
+    rng = np.random.default_rng(1234 + seed)
+    st = o64.state(w)
+    errs = []
+    for _ in range(ndirs):
+        d = rng.standard_normal(F.shape)
+        d /= np.linalg.norm(d)
+        h = 1e-3
+        lp = o64.control_loss(64, 64, 64, st, w.occ, w.params, w.steps, F + h * d, target)
+        lm = o64.control_loss(64, 64, 64, st, w.occ, w.params, w.steps, F - h * d, target)
+        fd = (lp - lm) / (2 * h)
+        an = float(np.sum(gF.astype(np.float64) * d))
+        errs.append({"fd": fd, "gpu": an, "err_rel_fd": abs(fd - an) / abs(fd),
+                     "err_rel_gnorm": abs(fd - an) / gnorm})
+    report = {"problem": "control64", "steps": w.steps, "loss_fp64": L64, "grad_norm_fp64": gnorm,
+              "rel_l2_gpu_vs_fp64": rel64, "directions": ndirs,
+              "max_err_rel_gnorm": max(e["err_rel_gnorm"] for e in errs),
+              "median_err_rel_fd": float(np.median([e["err_rel_fd"] for e in errs]))}
+    print(json.dumps(report))
+    out = os.environ.get("ZQS_ADJOINT_REPORT")
+    if out:
+        with open(out, "w") as fh:
+            json.dump({"summary": report, "directions": errs}, fh, indent=1)
+    return rel64, errs, gnorm
+
+
+@pytest.mark.slow
+def test_control64_gradient(zqs_lib):
+    rel64, errs, gnorm = _control64_check(4)
+    assert rel64 <= GRAD_TOL
+    for e in errs:
+        assert e["err_rel_gnorm"] <= GRAD_TOL, e
+
+
+@pytest.mark.slow
+def test_control64_gradient_32_directions(zqs_lib):
+    import os
+    if os.environ.get("ZQS_FULL_ADJOINT_CHECK") != "1":
+        pytest.skip("32-direction FP64 finite differences take minutes; set ZQS_FULL_ADJOINT_CHECK=1")
+    rel64, errs, gnorm = _control64_check(32)
+    assert rel64 <= GRAD_TOL
+    for e in errs:
+        assert e["err_rel_gnorm"] <= GRAD_TOL, e

@@ -108,10 +108,48 @@ struct zqs_adjoint {
     std::vector<Slot> cp;   // ncp checkpoints + the final state
     std::vector<Slot> seg;  // start states 1..every-1 of the segment being reversed
     AdjBufs b{};
+    // fixed inputs of one reversed step (the step's graph reads these):
+    // fix0 = start state (its velocity becomes the advection input in place),
+    // fix1 = velocity at the end of the step; t4a/t4b = vorticity and force
+    Slot fix0, fix1;
+    float4 *t4a = nullptr, *t4b = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    long long graph_gen = -1;
+    long long graph_launches = 0;
     bool forward_done = false;
     bool backward_done = false;
     long long launches_fwd = 0, launches_bwd = 0;
 };
+
+// The launches of one reversed step on the session's fixed buffers: the
+// forward force stage on the start state (advection input and vorticity),
+// then the adjoint kernels.
+int issue_adj_step(zqs_adjoint* a, int K, cudaStream_t s, LaunchCounter& lc) {
+    zqs_grid* w = a->wg;
+    const Layout& L = w->g.L;
+    DevGrid view = w->g;
+    view.u = a->fix0.f(L, 0);
+    view.v = a->fix0.f(L, 1);
+    view.w = a->fix0.f(L, 2);
+    view.T = a->fix0.f(L, 3);
+    view.rho = a->fix0.f(L, 4);
+    view.t4a = a->t4a;
+    view.t4b = a->t4b;
+    int rc = launch_force(view, w->kp, true, s, lc);
+    if (rc) return rc;
+    AdjFwd f;
+    f.u4 = a->fix1.f(L, 0);
+    f.v4 = a->fix1.f(L, 1);
+    f.w4 = a->fix1.f(L, 2);
+    f.u2 = view.u;
+    f.v2 = view.v;
+    f.w2 = view.w;
+    f.T0 = view.T;
+    f.rho0 = view.rho;
+    f.vort = view.t4a;
+    f.flags = view.flags;
+    return launch_adj_step(L, f, a->b, w->kp, w->src, K, s, lc);
+}
 
 extern "C" {
 
@@ -138,9 +176,13 @@ ZQS_API int zqs_grid_set_force(zqs_grid* g, const float* F, int src_on_device, v
                                    src_on_device != 0, s);
         if (rc) return rc;
     }
-    g->fext_on = true;
-    g->kp.fext = g->fext_base + L.plane;
-    g->drop_graphs();
+    // the captured graphs read the force buffer at run time: only switching
+    // the force on needs new graphs (work on stream s is ordered after the copy)
+    if (!g->fext_on) {
+        g->fext_on = true;
+        g->kp.fext = g->fext_base + L.plane;
+        g->drop_graphs();
+    }
     return ZQS_OK;
 }
 
@@ -179,9 +221,9 @@ ZQS_API int zqs_adjoint_create(zqs_adjoint** out, zqs_grid* g, int nsteps, int c
     };
     // slots: ncp checkpoints + final + (every-1) segment states; adjoint fields
     const size_t fe = (size_t)L.elems;
-    const size_t nslots = (size_t)a->ncp + 1 + (size_t)(a->every - 1);
-    const size_t nflt = 9 + 7 + 3;        // gu.., gu3.., gu2.., gT, grho, gTa, grhoa, q, acc, wt, gF(3)
-    const size_t nf4 = 3;                 // gom4, gg4, gw4
+    const size_t nslots = (size_t)a->ncp + 1 + (size_t)(a->every - 1) + 2;  // + fix0, fix1
+    const size_t nflt = 9 + 8 + 3;        // gu.., gu3.., gu2.., gT, grho, gTa, grhoa, q, q2, acc, wt, gF(3)
+    const size_t nf4 = 5;                 // gom4, gg4, gw4, t4a, t4b
     const long long nblocks = (long long)((L.W + 31) / 32) * ((L.H + 7) / 8) * L.D;
     const size_t red_len = (size_t)(2 * nblocks + 16);
     const size_t total = (nslots * 5 + nflt) * fe * 4 + nf4 * fe * 16 + red_len * 8 + 256;
@@ -200,6 +242,8 @@ ZQS_API int zqs_adjoint_create(zqs_adjoint** out, zqs_grid* g, int nsteps, int c
     for (auto& s : a->cp) s.base = (float*)take(5 * fe * 4);
     a->seg.resize(a->every);  // index 0 unused (the checkpoint itself)
     for (int t = 1; t < a->every; t++) a->seg[t].base = (float*)take(5 * fe * 4);
+    a->fix0.base = (float*)take(5 * fe * 4);
+    a->fix1.base = (float*)take(5 * fe * 4);
     auto fld = [&]() -> float* { return (float*)take(fe * 4) + L.plane; };
     AdjBufs& b = a->b;
     b.gu = fld();
@@ -216,12 +260,15 @@ ZQS_API int zqs_adjoint_create(zqs_adjoint** out, zqs_grid* g, int nsteps, int c
     b.gTa = fld();
     b.grhoa = fld();
     b.q = fld();
+    b.q2 = fld();
     b.acc = fld();
     b.wt = fld();
     b.gF = (float*)take(3 * fe * 4) + L.plane;
     b.gom4 = (float4*)take(fe * 16) + L.plane;
     b.gg4 = (float4*)take(fe * 16) + L.plane;
     b.gw4 = (float4*)take(fe * 16) + L.plane;
+    a->t4a = (float4*)take(fe * 16) + L.plane;
+    a->t4b = (float4*)take(fe * 16) + L.plane;
     b.red = (double*)take(red_len * 8);
     b.red_len = (long long)red_len;
     // the work grid: same parameters, occupancy and SOR setup
@@ -241,6 +288,7 @@ ZQS_API int zqs_adjoint_create(zqs_adjoint** out, zqs_grid* g, int nsteps, int c
 
 ZQS_API int zqs_adjoint_destroy(zqs_adjoint* a) {
     if (!a) return ZQS_OK;
+    if (a->graph) cudaGraphExecDestroy(a->graph);
     if (a->wg) {
         cudaStreamSynchronize(a->wg->own);
         zqs_grid_destroy(a->wg);
@@ -293,23 +341,33 @@ ZQS_API int zqs_adjoint_backward(zqs_adjoint* a, const float* g_density, float* 
     zqs_grid* w = a->wg;
     const Layout& L = g->g.L;
     cudaStream_t s = g->pick(stream);
-    // the work grid follows the grid's parameters and force
-    int rc = zqs_grid_set_params(w, &g->params);
-    if (rc) return rc;
-    w->sor = g->sor;
+    // the work grid follows the grid's parameters, SOR setup and force
+    // (its graphs are kept while none of them changes)
+    int rc = ZQS_OK;
+    if (memcmp(&w->params, &g->params, sizeof(zqs_params)) != 0) {
+        rc = zqs_grid_set_params(w, &g->params);
+        if (rc) return rc;
+    }
+    if (memcmp(&w->sor, &g->sor, sizeof(SorConfig)) != 0) {
+        w->sor = g->sor;
+        w->drop_graphs();
+    }
     if (g->fext_on) {
         if (!w->fext_base) {
             ZQS_CUDA_TRY(cudaMalloc(&w->fext_base, (size_t)L.elems * 3 * 4));
         }
         ZQS_CUDA_TRY(cudaMemcpyAsync(w->fext_base, g->fext_base, (size_t)L.elems * 3 * 4, cudaMemcpyDeviceToDevice,
                                      s));
-        w->fext_on = true;
-        w->kp.fext = w->fext_base + L.plane;
-    } else {
+        if (!w->fext_on) {
+            w->fext_on = true;
+            w->kp.fext = w->fext_base + L.plane;
+            w->drop_graphs();
+        }
+    } else if (w->fext_on) {
         w->fext_on = false;
         w->kp.fext = nullptr;
+        w->drop_graphs();
     }
-    w->drop_graphs();
     const AdjBufs& b = a->b;
     const size_t fe = (size_t)L.elems;
     LaunchCounter lc;
@@ -346,27 +404,37 @@ ZQS_API int zqs_adjoint_backward(zqs_adjoint* a, const float* g_density, float* 
         for (int t = len - 1; t >= 0; t--) {
             const Slot& S0 = state(t);
             const Slot& S1 = state(t + 1);
-            // advection input and vorticity of this step, from its start state
-            rc = load_state(S0, w->g, 3, s);
-            if (rc) return rc;
-            DevGrid view = w->g;
-            view.T = S0.f(L, 3);
-            view.rho = S0.f(L, 4);
-            rc = launch_force(view, w->kp, true, s, lc);
-            if (rc) return rc;
-            AdjFwd f;
-            f.u4 = S1.f(L, 0);
-            f.v4 = S1.f(L, 1);
-            f.w4 = S1.f(L, 2);
-            f.u2 = view.u;
-            f.v2 = view.v;
-            f.w2 = view.w;
-            f.T0 = S0.f(L, 3);
-            f.rho0 = S0.f(L, 4);
-            f.vort = view.t4a;
-            f.flags = view.flags;
-            rc = launch_adj_step(L, f, b, w->kp, w->src, K, s, lc);
-            if (rc) return rc;
+            // this step's inputs into the fixed buffers the step graph reads
+            for (int q = 0; q < 5; q++)
+                ZQS_CUDA_TRY(cudaMemcpyAsync(a->fix0.base + q * fe, S0.base + q * fe, fe * 4,
+                                             cudaMemcpyDeviceToDevice, s));
+            for (int q = 0; q < 3; q++)
+                ZQS_CUDA_TRY(cudaMemcpyAsync(a->fix1.base + q * fe, S1.base + q * fe, fe * 4,
+                                             cudaMemcpyDeviceToDevice, s));
+            if (!a->graph || a->graph_gen != w->gen) {
+                if (a->graph) cudaGraphExecDestroy(a->graph);
+                a->graph = nullptr;
+                LaunchCounter glc;
+                ZQS_CUDA_TRY(cudaStreamBeginCapture(w->own, cudaStreamCaptureModeThreadLocal));
+                rc = issue_adj_step(a, K, w->own, glc);
+                cudaGraph_t gr = nullptr;
+                cudaError_t e = cudaStreamEndCapture(w->own, &gr);
+                if (rc) {
+                    if (gr) cudaGraphDestroy(gr);
+                    return rc;
+                }
+                if (e != cudaSuccess) return cuda_fail(e, "zqs_adjoint_backward: cudaStreamEndCapture");
+                e = cudaGraphInstantiate(&a->graph, gr, 0);
+                cudaGraphDestroy(gr);
+                if (e != cudaSuccess) {
+                    a->graph = nullptr;
+                    return cuda_fail(e, "zqs_adjoint_backward: cudaGraphInstantiate");
+                }
+                a->graph_gen = w->gen;
+                a->graph_launches = glc.n;
+            }
+            ZQS_CUDA_TRY(cudaGraphLaunch(a->graph, s));
+            lc.n += a->graph_launches;
         }
     }
     if (grad_F) {

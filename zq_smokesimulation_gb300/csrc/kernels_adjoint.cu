@@ -572,21 +572,19 @@ int launch_adj_step(const Layout& L, const AdjFwd& f, const AdjBufs& b, const KP
     k_adj_gradT<<<gc, blk, 0, s>>>(L, f.flags, b, open);
     lc.n++;
     if (K > 0) {
-        // forward order per iteration: red (0) then black (1); reversed:
-        // head red gather, then black/red full sweeps, ending with black,
-        // then the red tail
+        // forward order per iteration: red (0) then black (1); reversed: the
+        // head red gather, K-1 black/red pairs (fused, temporally blocked),
+        // the last black sweep, then the red tail
         k_adj_sor_sweep<<<gc, blk, 0, s>>>(L, b.q, b.wt, b.acc, 0, 0, kp.om1);
         lc.n++;
-        for (int it = 0; it < K; it++) {
-            k_adj_sor_sweep<<<gc, blk, 0, s>>>(L, b.q, b.wt, b.acc, 1, 1, kp.om1);
-            lc.n++;
-            if (it + 1 < K) {
-                k_adj_sor_sweep<<<gc, blk, 0, s>>>(L, b.q, b.wt, b.acc, 0, 1, kp.om1);
-                lc.n++;
-            }
+        float* qc = b.q;
+        if (K > 1) {
+            int rc = launch_sor_adjoint_pairs(L, b.q, b.q2, b.wt, b.acc, kp.om1, K - 1, s, lc, &qc);
+            if (rc) return rc;
         }
-        k_adj_sor_sweep<<<gc, blk, 0, s>>>(L, b.q, b.wt, b.acc, 0, 2, kp.om1);
-        lc.n++;
+        k_adj_sor_sweep<<<gc, blk, 0, s>>>(L, qc, b.wt, b.acc, 1, 1, kp.om1);
+        k_adj_sor_sweep<<<gc, blk, 0, s>>>(L, qc, b.wt, b.acc, 0, 2, kp.om1);
+        lc.n += 2;
     }
     ZQS_LAUNCH_CHECK("k_adj_sor_sweep");
     if (!open && !kp.mean_override) {

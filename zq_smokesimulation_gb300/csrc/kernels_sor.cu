@@ -26,6 +26,7 @@
 //                 the two-plane lag lets all S half-sweeps of a step run at once
 //                 with one barrier per step, and every value each reads is at the
 //                 right sweep.  Results equal S/2 iterations of k_sor_colour.
+#include "zqs_adjoint.h"
 #include "zqs_batch.h"
 
 #include <algorithm>
@@ -341,11 +342,17 @@ struct RegShape {
 // One CTA tile (bx, by) of TX x TY columns and z chunk bz; every thread of the
 // block takes part (barriers inside), and the last step ends with a barrier,
 // so a persistent block may run the next tile on the same shared memory.
-template <int S, int TX, int TY, int PPT>
+//
+// ADJ: the reversed SOR of the adjoint in its scaled variable q (see
+// kernels_adjoint.cu): `div` carries wt = omega/cnt (0 where the forward never
+// updates), flags are not read, the half-sweeps run black first, each update
+// is q = (1-omega) q + wt * sum(q_n), and every cell's value before each
+// update is added to acc (read and written in place by the owning thread).
+template <int S, int TX, int TY, int PPT, bool ADJ = false>
 __device__ __forceinline__ void sor_reg_tile(const Layout& L, const float* __restrict__ pin,
                                              float* __restrict__ pout, const float* __restrict__ div,
                                              const uint8_t* __restrict__ flags, float omega, float om1, int zc,
-                                             int bx, int by, int bz) {
+                                             int bx, int by, int bz, float* __restrict__ acc = nullptr) {
     using Sh = RegShape<S, TX, TY, PPT>;
     constexpr int PW = Sh::PW, NP = Sh::NP, CA = Sh::CA, NT = Sh::NT;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -389,7 +396,8 @@ __device__ __forceinline__ void sor_reg_tile(const Layout& L, const float* __res
 
     float P[PPT][NP][2];     // pressure by colour, ring of planes
     unsigned F[PPT][NP];     // flags by colour: byte c = flags of the colour-c cell
-    float2 np_[PPT], nd[PPT];
+    float A[PPT][ADJ ? NP : 1][2];  // ADJ: acc by colour, ring of planes
+    float2 np_[PPT], nd[PPT], na[PPT];
     unsigned nf[PPT];
 #pragma unroll
     for (int q = 0; q < PPT; q++) {
@@ -398,14 +406,18 @@ __device__ __forceinline__ void sor_reg_tile(const Layout& L, const float* __res
             P[q][a][0] = P[q][a][1] = 0.0f;
             F[q][a] = 0u;
         }
+#pragma unroll
+        for (int a = 0; a < (ADJ ? NP : 1); a++) A[q][a][0] = A[q][a][1] = 0.0f;
         np_[q] = make_float2(0.0f, 0.0f);
         nd[q] = np_[q];
+        na[q] = np_[q];
         nf[q] = 0;
         if (pin_ok[q] && tbeg >= flo && tbeg < fhi) {
             np_[q] = __ldg(reinterpret_cast<const float2*>(pin + gaddr[q]));
             nd[q] = __ldg(reinterpret_cast<const float2*>(div + gaddr[q]));
-            nf[q] = __ldg(reinterpret_cast<const unsigned short*>(flags + gaddr[q]));
+            if (!ADJ) nf[q] = __ldg(reinterpret_cast<const unsigned short*>(flags + gaddr[q]));
         }
+        if (ADJ && out_ok[q] && tbeg >= z0 && tbeg < z1) na[q] = *reinterpret_cast<const float2*>(acc + gaddr[q]);
     }
 
     for (int g = 0; g < nsteps; g += NP) {
@@ -420,6 +432,10 @@ __device__ __forceinline__ void sor_reg_tile(const Layout& L, const float* __res
                     P[q][qs][0] = lc ? np_[q].y : np_[q].x;
                     P[q][qs][1] = lc ? np_[q].x : np_[q].y;
                     F[q][qs] = lc ? (((nf[q] & 0xffu) << 8) | (nf[q] >> 8)) : nf[q];
+                    if (ADJ) {
+                        A[q][ADJ ? qs : 0][0] = lc ? na[q].y : na[q].x;
+                        A[q][ADJ ? qs : 0][1] = lc ? na[q].x : na[q].y;
+                    }
                     float* Pp = sp + qs * 2 * CA + me[q];
                     float* Dp = sd + qs * 2 * CA + me[q];
                     Pp[0] = P[q][qs][0];
@@ -437,7 +453,12 @@ __device__ __forceinline__ void sor_reg_tile(const Layout& L, const float* __res
                     if (pin_ok[q] && t + 1 >= flo && t + 1 < fhi) {
                         np_[q] = __ldg(reinterpret_cast<const float2*>(pin + gaddr[q]));
                         nd[q] = __ldg(reinterpret_cast<const float2*>(div + gaddr[q]));
-                        nf[q] = __ldg(reinterpret_cast<const unsigned short*>(flags + gaddr[q]));
+                        if (!ADJ) nf[q] = __ldg(reinterpret_cast<const unsigned short*>(flags + gaddr[q]));
+                    }
+                    if (ADJ) {
+                        na[q] = make_float2(0.0f, 0.0f);
+                        if (out_ok[q] && t + 1 >= z0 && t + 1 < z1)
+                            na[q] = *reinterpret_cast<const float2*>(acc + gaddr[q]);
                     }
                 }
                 // 3. half-sweeps
@@ -446,15 +467,16 @@ __device__ __forceinline__ void sor_reg_tile(const Layout& L, const float* __res
                     const int z = t - 2 * s;
                     const int r = S - s;
                     if (z >= max(z0 - r, 0) && z < min(z1 + r, L.D)) {
-                        const int c = (s - 1) & 1;
+                        const int c = ((s - 1) & 1) ^ (ADJ ? 1 : 0);
                         const int sz = (qs - 2 * s + 2 * NP) % NP;
                         const int szm = (sz + NP - 1) % NP;
                         const int szp = (sz + 1) % NP;
 #pragma unroll
                         for (int q = 0; q < PPT; q++) {
                             const int o = ((jrow[q] + t) & 1) ^ c;
-                            const int cnt = (F[q][sz] >> (8 * c + F_CNT_SHIFT)) & 7;
-                            if (((amask[q] >> (2 * r + o)) & 1u) && cnt) {
+                            const int cnt = ADJ ? 1 : (F[q][sz] >> (8 * c + F_CNT_SHIFT)) & 7;
+                            const float wgt = ADJ ? sd[(sz * 2 + c) * CA + me[q]] : 0.0f;
+                            if (((amask[q] >> (2 * r + o)) & 1u) && cnt && (!ADJ || wgt != 0.0f)) {
                                 const float* Po = sp + (sz * 2 + (c ^ 1)) * CA + me[q];
                                 const float own = P[q][sz][c ^ 1];
                                 const float adj = o ? Po[1] : Po[-1];
@@ -465,8 +487,15 @@ __device__ __forceinline__ void sor_reg_tile(const Layout& L, const float* __res
                                 sum = sum + Po[PW];
                                 sum = sum + P[q][szm][c ^ 1];
                                 sum = sum + P[q][szp][c ^ 1];
-                                const float nv = sor_update(P[q][sz][c], sum, sd[(sz * 2 + c) * CA + me[q]], cnt,
-                                                            omega, om1);
+                                float nv;
+                                if (ADJ) {
+                                    const float old = P[q][sz][c];
+                                    nv = om1 * old + wgt * sum;
+                                    A[q][ADJ ? sz : 0][c] += old;
+                                } else {
+                                    nv = sor_update(P[q][sz][c], sum, sd[(sz * 2 + c) * CA + me[q]], cnt, omega,
+                                                    om1);
+                                }
                                 P[q][sz][c] = nv;
                                 sp[(sz * 2 + c) * CA + me[q]] = nv;
                             }
@@ -484,6 +513,12 @@ __device__ __forceinline__ void sor_reg_tile(const Layout& L, const float* __res
                             const float a = lc ? P[q][so][1] : P[q][so][0];
                             const float b = lc ? P[q][so][0] : P[q][so][1];
                             *reinterpret_cast<float2*>(pout + gaddr[q] - (2 * S + 2) * plane) = make_float2(a, b);
+                            if (ADJ) {
+                                const float aa = lc ? A[q][ADJ ? so : 0][1] : A[q][ADJ ? so : 0][0];
+                                const float ab = lc ? A[q][ADJ ? so : 0][0] : A[q][ADJ ? so : 0][1];
+                                *reinterpret_cast<float2*>(acc + gaddr[q] - (2 * S + 2) * plane) =
+                                    make_float2(aa, ab);
+                            }
                         }
                     }
                 }
@@ -516,6 +551,15 @@ __global__ void __launch_bounds__(RegShape<S, TX, TY, PPT>::NT)
         sor_reg_tile<S, TX, TY, PPT>(d.L, d.p[pcur], d.p[pcur ^ 1], d.div, d.flags, d.kp.omega, d.kp.om1,
                                      d.zc[which], bx, by, bz);
     }
+}
+
+// The reversed SOR of the adjoint (ADJ form of the tile): q ping-pongs, acc in place.
+template <int S, int TX, int TY, int PPT>
+__global__ void __launch_bounds__(RegShape<S, TX, TY, PPT>::NT)
+    k_sor_reg_adj(Layout L, const float* __restrict__ qin, float* __restrict__ qout, const float* __restrict__ wt,
+                  float* __restrict__ acc, float om1, int zc) {
+    sor_reg_tile<S, TX, TY, PPT, true>(L, qin, qout, wt, nullptr, 0.0f, om1, zc, blockIdx.x, blockIdx.y,
+                                       blockIdx.z, acc);
 }
 
 // Quad form: one thread owns four consecutive cells along x (two of each
@@ -920,6 +964,11 @@ struct RbVariant {
     cudaError_t (*launch_batch)(int, const BatchLaunch&, int, int, cudaStream_t);
     const void* fn_batch;
     int ctas_per_sm_batch;
+    // reversed SOR of the adjoint (register-column variants only)
+    cudaError_t (*launch_adj)(dim3, const Layout&, const float*, float*, const float*, float*, float, int,
+                              cudaStream_t);
+    const void* fn_adj;
+    int ctas_per_sm_adj;
 };
 
 template <int S, int TX, int TY, int PPT>
@@ -942,6 +991,9 @@ RbVariant rb_variant() {
     v.smem = Sh::smem;
     v.ctas_per_sm = 0;
     v.launch = &rb_launch<S, TX, TY, PPT>;
+    v.launch_adj = nullptr;
+    v.fn_adj = nullptr;
+    v.ctas_per_sm_adj = 0;
     v.launch_batch = nullptr;
     v.fn_batch = nullptr;
     v.ctas_per_sm_batch = 0;
@@ -965,6 +1017,14 @@ cudaError_t reg_launch_batch(int blocks, const BatchLaunch& B, int pcur, int whi
 }
 
 template <int S, int TX, int TY, int PPT>
+cudaError_t reg_launch_adj(dim3 gr, const Layout& L, const float* qin, float* qout, const float* wt, float* acc,
+                           float om1, int zc, cudaStream_t st) {
+    using Sh = RegShape<S, TX, TY, PPT>;
+    k_sor_reg_adj<S, TX, TY, PPT><<<gr, Sh::NT, Sh::smem, st>>>(L, qin, qout, wt, acc, om1, zc);
+    return cudaGetLastError();
+}
+
+template <int S, int TX, int TY, int PPT>
 RbVariant reg_variant() {
     using Sh = RegShape<S, TX, TY, PPT>;
     RbVariant v;
@@ -980,6 +1040,9 @@ RbVariant reg_variant() {
     v.launch_batch = &reg_launch_batch<S, TX, TY, PPT>;
     v.fn_batch = (const void*)k_sor_reg_batch<S, TX, TY, PPT>;
     v.ctas_per_sm_batch = 0;
+    v.launch_adj = &reg_launch_adj<S, TX, TY, PPT>;
+    v.fn_adj = (const void*)k_sor_reg_adj<S, TX, TY, PPT>;
+    v.ctas_per_sm_adj = 0;
     return v;
 }
 
@@ -1003,6 +1066,9 @@ RbVariant quad_variant() {
     v.smem = Sh::smem;
     v.ctas_per_sm = 0;
     v.launch = &quad_launch<S, TX, TY>;
+    v.launch_adj = nullptr;
+    v.fn_adj = nullptr;
+    v.ctas_per_sm_adj = 0;
     v.launch_batch = nullptr;
     v.fn_batch = nullptr;
     v.ctas_per_sm_batch = 0;
@@ -1020,6 +1086,8 @@ RbVariant g_var[kNumVariants];
 const int kDefaultVariant[5] = {-1, 16, 13, 15, 7};
 // batched default: register-column 32x16 at depth 2 (small tiles suit 32..128 edges)
 const int kBatchDefaultVariant = 12;
+// reversed SOR of the adjoint: register-column variants in order of preference
+const int kAdjVariants[] = {13, 12, 11, 10};
 int g_num_sms = 0;
 int g_prepared = 0;
 
@@ -1085,6 +1153,12 @@ int sor_prepare() {
             n = 0;
             ZQS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, v.fn_batch, v.nt, v.smem));
             v.ctas_per_sm_batch = n;
+        }
+        if (v.fn_adj) {
+            ZQS_CUDA_TRY(cudaFuncSetAttribute(v.fn_adj, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)v.smem));
+            n = 0;
+            ZQS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, v.fn_adj, v.nt, v.smem));
+            v.ctas_per_sm_adj = n;
         }
     }
     g_prepared = 1;
@@ -1239,6 +1313,42 @@ int launch_project_batch(const BatchLaunch& cell, const BatchLaunch& face, const
     lc.n++;
     ZQS_LAUNCH_CHECK("k_gradient_batch");
     if (pfin) *pfin = pcur;
+    return ZQS_OK;
+}
+
+int launch_sor_adjoint_pairs(const Layout& L, float* q, float* q2, const float* wt, float* acc, float om1,
+                             int npairs, cudaStream_t s, LaunchCounter& lc, float** qcur) {
+    int rc = sor_prepare();
+    if (rc) return rc;
+    auto fits = [](int i) { return g_var[i].launch_adj && g_var[i].ctas_per_sm_adj > 0; };
+    int vmain = -1, vrem = -1;
+    for (int i : kAdjVariants)
+        if (vmain < 0 && fits(i) && g_var[i].S == 4) vmain = i;
+    for (int i : kAdjVariants)
+        if (vrem < 0 && fits(i) && g_var[i].S == 2) vrem = i;
+    if (vrem < 0) {
+        set_error("reversed SOR: no fused variant fits this device");
+        return ZQS_EUNSUPPORTED;
+    }
+    if (vmain < 0) vmain = vrem;
+    float* cur = q;
+    float* nxt = q2;
+    int remaining = npairs;
+    while (remaining > 0) {
+        const int dmain = g_var[vmain].S / 2;
+        const RbVariant& v = remaining >= dmain ? g_var[vmain] : g_var[vrem];
+        const int d = v.S / 2;
+        RbVariant occ = v;
+        occ.ctas_per_sm = v.ctas_per_sm_adj;
+        const int zc = choose_zc(L, occ);
+        dim3 gr((L.W + v.TX - 1) / v.TX, (L.H + v.TY - 1) / v.TY, (L.D + zc - 1) / zc);
+        cudaError_t e = v.launch_adj(gr, L, cur, nxt, wt, acc, om1, zc, s);
+        if (e != cudaSuccess) return cuda_fail(e, "k_sor_reg_adj");
+        lc.n++;
+        std::swap(cur, nxt);
+        remaining -= d;
+    }
+    *qcur = cur;
     return ZQS_OK;
 }
 

@@ -36,6 +36,7 @@ struct AdjBufs {
     float *gT, *grho;           // adjoint of the scalars (end in, start out)
     float *gTa, *grhoa;         // scatter accumulators of the scalar advection
     float *q, *acc, *wt;        // reversed SOR: scaled adjoint pressure, -gdiv, omega/cnt
+    float* q2;                  // second q buffer of the fused passes
     float *gF;                  // adjoint of the control, 3 components at stride elems
     float4 *gom4, *gg4, *gw4;   // confinement temporaries
     double* red;                // FP64 partials (closed-solver mean)
@@ -53,6 +54,10 @@ struct AdjFwd {
 
 int launch_adj_weights(const Layout& L, const uint8_t* flags, float omega, float* wt, cudaStream_t s,
                        LaunchCounter& lc);
+// npairs black/red pairs of the reversed SOR in temporally blocked passes
+// (register-column kernel, ADJ form); q and q2 ping-pong, *qcur = result.
+int launch_sor_adjoint_pairs(const Layout& L, float* q, float* q2, const float* wt, float* acc, float om1,
+                             int npairs, cudaStream_t s, LaunchCounter& lc, float** qcur);
 int launch_adj_step(const Layout& L, const AdjFwd& f, const AdjBufs& b, const KParams& kp, const SourceList& src,
                     int K, cudaStream_t s, LaunchCounter& lc);
 

@@ -20,8 +20,9 @@ Named configurations (cell units, y is up, gravity along -y):
                  source (r ~ U[.06,.12] x the shortest edge, in the bottom 15%),
                  alpha ~ U[.05,.2], beta ~ U[.2,.8], eps ~ U[0,.3],
                  dt ~ U[.25,.75]; K=200, 100 steps (batch_mixed())
-  control64 / control128  the adjoint problem: plain64's walls, forces and
-                 solver at N^3 (source r = 6N/64 at (N/2, N/8, N/2)), a zero
+  control64 / control128  the adjoint problem: plain64's walls, forces
+                 (confinement off, dt = 32/N, see control_problem()) and solver at N^3
+                 (source r = 6N/64 at (N/2, N/8, N/2)), a zero
                  per-cell control force, 64 steps, and a target density that
                  is a Gaussian blob (sigma 8 cells, peak 1) centred uniformly
                  in the upper half (control_problem())
@@ -288,13 +289,29 @@ def batch_mixed(n: int = 64, *, seed: int = 0, K: int = 200, edges=(32, 48, 64, 
 
 
 def control_problem(N: int = 64, *, seed: int = 0, K: int = 200, nsteps: int = 64, substeps: int = 20,
-                    sigma: float = 8.0):
+                    sigma: float = 8.0, confine: float = 0.0, dt: float | None = None):
     """The force-field control problem at N^3: (workload, target density).
 
     Loss L(F) = sum_cells (rho_final - target)^2 after nsteps steps with the
-    per-cell force F (3, N, N, N) added every step; F = 0 initially."""
+    per-cell force F (3, N, N, N) added every step; F = 0 initially.
+
+    Vorticity confinement is off by default: its normal N = grad|w| / |grad|w||
+    (ZQ_CUDA_AddForce3D.cu:64-111) has a derivative that grows as
+    1/|grad|w|| where the vorticity is nearly uniform, and over tens of steps
+    the exact gradient of the rollout grows without bound (measured at 64^3:
+    |dL/dF| ~ 1e3 for 16 steps, ~ 1e6 at 32, ~ 1e16 at 64 with eps = 0.2, where
+    FP32 and FP64 gradients and finite differences no longer agree).
+
+    dt defaults to 32/N (0.5 at 64^3, 0.25 at 128^3): the same distance in
+    cells per step at every resolution.  The backtrace chains 19 substeps;
+    at 128^3 with dt = 0.5 the plume moves ~2.3 cells per substep and the
+    exact gradient is ill-conditioned (|dL/dF| ~ 1e5 after 8 steps, 1e15
+    after 64, FP32 and FP64 gradients 1.5e-2 apart after 8 steps); with
+    dt = 0.25 it stays ~1e3 over 64 steps."""
     occ = walls_open_top(N, N, N)
     p = smoke_params(N, K, substeps=substeps)
+    p.confine = confine
+    p.step_time = float(np.float32(32.0 / N)) if dt is None else dt
     p.set_sources([sphere(N / 2, N / 8, N / 2, 6.0 * N / 64)])
     u, v, w = initial_velocity(occ, seed)
     T = np.zeros((N, N, N), np.float32)
