@@ -54,8 +54,9 @@ template <class R> static inline R lerp(R a, R b, R t) { return a + t * (b - a);
 
 /* One axis of clamp-to-edge linear filtering: the coordinate g is in texel
  * index units (texel n has its centre at g = n).  g is first clamped to
- * [-1, n] (which does not change the filtered value and makes NaN/inf safe:
- * fmax/fmin return the non-NaN operand), then split into floor and fraction.
+ * [0, n-1] (fmax/fmin return the non-NaN operand, so NaN becomes 0): outside
+ * that range clamp-to-edge filtering returns the edge texel, which the
+ * clamped coordinate gives with t = 0 or i0 == i1.  Then floor and fraction.
  * Mirrors cudaAddressModeClamp + cudaFilterModeLinear of the reference's
  * textures (ZQ_CUDA_Advection3D.cu:654-993). */
 template <class R> struct Axis {
@@ -63,13 +64,12 @@ template <class R> struct Axis {
     R t;
 };
 template <class R> static inline Axis<R> axis(R g, int n) {
-    g = std::fmin(std::fmax(g, R(-1)), R(n));
+    g = std::fmin(std::fmax(g, R(0)), R(n - 1));
     R f = std::floor(g);
     Axis<R> a;
     a.t = g - f;
-    int i = (int)f;
-    a.i0 = clampi(i, 0, n - 1);
-    a.i1 = clampi(i + 1, 0, n - 1);
+    a.i0 = (int)f;
+    a.i1 = a.i0 + 1 < n ? a.i0 + 1 : n - 1;
     return a;
 }
 

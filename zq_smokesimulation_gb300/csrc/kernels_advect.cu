@@ -60,9 +60,9 @@ __device__ __forceinline__ void advect_vel_macout_tile(const Layout& L, const fl
         } else {
             MacVel mv{L, u, v, w};
             backtrace(L, flags, mv, kp, px, py, pz);
-            if (comp == 0) out = tri_unscaled(u, corners(L, L.W + 1, L.H, L.D, px, py - 0.5f, pz - 0.5f));
-            else if (comp == 1) out = tri_unscaled(v, corners(L, L.W, L.H + 1, L.D, px - 0.5f, py, pz - 0.5f));
-            else out = tri_unscaled(w, corners(L, L.W, L.H, L.D + 1, px - 0.5f, py - 0.5f, pz));
+            if (comp == 0) out = tri0_sample(u, L, tri0(L, L.W + 1, L.H, L.D, px, py - 0.5f, pz - 0.5f));
+            else if (comp == 1) out = tri0_sample(v, L, tri0(L, L.W, L.H + 1, L.D, px - 0.5f, py, pz - 0.5f));
+            else out = tri0_sample(w, L, tri0(L, L.W, L.H, L.D + 1, px - 0.5f, py - 0.5f, pz));
         }
     }
     dst[c] = out;
@@ -173,9 +173,9 @@ __device__ __forceinline__ void advect_scalar_tile(const Layout& L, const float*
         MacVel mv{L, u, v, w};
         backtrace(L, flags, mv, kp, px, py, pz);
     }
-    Corners cs = corners(L, L.W, L.H, L.D, px - 0.5f, py - 0.5f, pz - 0.5f);
-    float t = tri(T, cs, aT);
-    float d = tri(rho, cs, aD);
+    const Tri0 cs = tri0(L, L.W, L.H, L.D, px - 0.5f, py - 0.5f, pz - 0.5f);
+    float t = tri0_sample(T, L, cs, aT);
+    float d = tri0_sample(rho, L, cs, aD);
     if (src.n > 0) reinject_cell(src, i, j, k, t, d);
     const int c = lidx(L, i, j, k);
     T2[c] = t;

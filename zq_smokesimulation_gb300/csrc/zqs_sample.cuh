@@ -12,15 +12,17 @@ struct Ax {
     float t;
 };
 
-// Clamp-to-edge linear filter along one axis; g in texel-index units.
+// Clamp-to-edge linear filter along one axis; g in texel-index units.  g is
+// clamped to [0, n-1] first (NaN -> 0): outside that range clamp-to-edge
+// filtering returns the edge texel, which the clamped coordinate gives with
+// t = 0 (or with i0 == i1), so only i1 needs a bound.
 __device__ __forceinline__ Ax axis(float g, int n) {
-    g = fminf(fmaxf(g, -1.0f), (float)n);
-    float f = floorf(g);
+    g = fminf(fmaxf(g, 0.0f), (float)(n - 1));
+    const float f = floorf(g);
     Ax a;
     a.t = g - f;
-    int i = (int)f;
-    a.i0 = min(max(i, 0), n - 1);
-    a.i1 = min(max(i + 1, 0), n - 1);
+    a.i0 = (int)f;
+    a.i1 = min(a.i0 + 1, n - 1);
     return a;
 }
 
@@ -99,13 +101,82 @@ __device__ __forceinline__ float tri4c(const float4* __restrict__ f4, int q, con
     return lerpf(lerpf(c00, c10, c.ty), lerpf(c01, c11, c.ty), c.tz);
 }
 
+// Forward-only trilinear sample with the upper corners at lower + 1 along
+// every axis, unclamped: one base offset plus {0, 1, px, plane} combinations.
+// axis() leaves i1 != i0 + 1 only at the upper edge, where t is exactly 0, and
+// the padded layout keeps that neighbour in bounds (padding column or row,
+// the next row or plane, or the trailing guard plane) and finite, so the value
+// equals the clamp-to-edge sample (up to the sign of an exact zero).
+struct Tri0 {
+    int r;
+    float tx, ty, tz;
+};
+__device__ __forceinline__ Tri0 tri0(const Layout& L, int nx, int ny, int nz, float gx, float gy, float gz) {
+    const Ax ax = axis(gx, nx), ay = axis(gy, ny), az = axis(gz, nz);
+    Tri0 c;
+    c.r = (az.i0 * L.py + ay.i0) * L.px + ax.i0;
+    c.tx = ax.t;
+    c.ty = ay.t;
+    c.tz = az.t;
+    return c;
+}
+// x, then y, then z; each corner times scale first (attenuation folding).
+__device__ __forceinline__ float tri0_sample(const float* __restrict__ f, const Layout& L, const Tri0& c,
+                                             float scale) {
+    const float* p = f + c.r;
+    const int px = L.px, pl = (int)L.plane;
+    const float c00 = lerpf(__ldg(p) * scale, __ldg(p + 1) * scale, c.tx);
+    const float c10 = lerpf(__ldg(p + px) * scale, __ldg(p + px + 1) * scale, c.tx);
+    const float c01 = lerpf(__ldg(p + pl) * scale, __ldg(p + pl + 1) * scale, c.tx);
+    const float c11 = lerpf(__ldg(p + pl + px) * scale, __ldg(p + pl + px + 1) * scale, c.tx);
+    return lerpf(lerpf(c00, c10, c.ty), lerpf(c01, c11, c.ty), c.tz);
+}
+__device__ __forceinline__ float tri0_sample(const float* __restrict__ f, const Layout& L, const Tri0& c) {
+    const float* p = f + c.r;
+    const int px = L.px, pl = (int)L.plane;
+    const float c00 = lerpf(__ldg(p), __ldg(p + 1), c.tx);
+    const float c10 = lerpf(__ldg(p + px), __ldg(p + px + 1), c.tx);
+    const float c01 = lerpf(__ldg(p + pl), __ldg(p + pl + 1), c.tx);
+    const float c11 = lerpf(__ldg(p + pl + px), __ldg(p + pl + px + 1), c.tx);
+    return lerpf(lerpf(c00, c10, c.ty), lerpf(c01, c11, c.ty), c.tz);
+}
+
 struct MacVel {
     Layout L;
     const float *u, *v, *w;
     __device__ __forceinline__ void operator()(float px, float py, float pz, float& vx, float& vy, float& vz) const {
-        vx = tri_unscaled(u, corners(L, L.W + 1, L.H, L.D, px, py - 0.5f, pz - 0.5f));
-        vy = tri_unscaled(v, corners(L, L.W, L.H + 1, L.D, px - 0.5f, py, pz - 0.5f));
-        vz = tri_unscaled(w, corners(L, L.W, L.H, L.D + 1, px - 0.5f, py - 0.5f, pz));
+        vx = tri0_sample(u, L, tri0(L, L.W + 1, L.H, L.D, px, py - 0.5f, pz - 0.5f));
+        vy = tri0_sample(v, L, tri0(L, L.W, L.H + 1, L.D, px - 0.5f, py, pz - 0.5f));
+        vz = tri0_sample(w, L, tri0(L, L.W, L.H, L.D + 1, px - 0.5f, py - 0.5f, pz));
+    }
+    // Also returns the cell containing the point when it lies in the domain:
+    // the u grid's x corner floor(clamp(x, 0, W)), the v grid's y and the w
+    // grid's z corners, bounded by the last cell (x = W lies in cell W-1).
+    __device__ __forceinline__ void operator()(float px, float py, float pz, float& vx, float& vy, float& vz,
+                                               int& ci, int& cj, int& ck) const {
+        const Ax xu = axis(px, L.W + 1), xc = axis(px - 0.5f, L.W);
+        const Ax yv = axis(py, L.H + 1), yc = axis(py - 0.5f, L.H);
+        const Ax zw = axis(pz, L.D + 1), zc = axis(pz - 0.5f, L.D);
+        const int rcc = zc.i0 * L.py;  // plane row of the cell-centred z corner
+        Tri0 cu, cv, cw;
+        cu.r = (rcc + yc.i0) * L.px + xu.i0;
+        cu.tx = xu.t;
+        cu.ty = yc.t;
+        cu.tz = zc.t;
+        cv.r = (rcc + yv.i0) * L.px + xc.i0;
+        cv.tx = xc.t;
+        cv.ty = yv.t;
+        cv.tz = zc.t;
+        cw.r = (zw.i0 * L.py + yc.i0) * L.px + xc.i0;
+        cw.tx = xc.t;
+        cw.ty = yc.t;
+        cw.tz = zw.t;
+        vx = tri0_sample(u, L, cu);
+        vy = tri0_sample(v, L, cv);
+        vz = tri0_sample(w, L, cw);
+        ci = min(xu.i0, L.W - 1);
+        cj = min(yv.i0, L.H - 1);
+        ck = min(zw.i0, L.D - 1);
     }
 };
 struct RegVel {
@@ -165,6 +236,55 @@ __device__ __forceinline__ void backtrace(const Layout& L, const uint8_t* __rest
         lx = px;
         ly = py;
         lz = pz;
+    }
+    px = lx;
+    py = ly;
+    pz = lz;
+}
+
+// backtrace() for the MAC sampler: the occupancy test reuses the cell index
+// that the velocity sample at the same point already floored.
+__device__ __forceinline__ void backtrace(const Layout& L, const uint8_t* __restrict__ flags, const MacVel& vel,
+                                          const KParams& kp, float& px, float& py, float& pz) {
+    float vx, vy, vz;
+    int ci, cj, ck;
+    vel(px, py, pz, vx, vy, vz, ci, cj, ck);
+    float lx = px, ly = py, lz = pz;
+    const float Wf = (float)L.W, Hf = (float)L.H, Df = (float)L.D;
+    auto inside = [&](float x, float y, float z) -> bool {
+        return x >= 0.0f && x <= Wf && y >= 0.0f && y <= Hf && z >= 0.0f && z <= Df;
+    };
+    const float dt = kp.dt_sub;
+    int istep = 0;
+    bool broke = false;
+    do {
+        if (!inside(px, py, pz) || !(__ldg(flags + lidx(L, ci, cj, ck)) & F_FREE)) {
+            broke = true;
+            break;
+        }
+        lx = px;
+        ly = py;
+        lz = pz;
+        if (kp.inv_h != 0.0f) {
+            px = px - (vx * dt) * kp.inv_h;
+            py = py - (vy * dt) * kp.inv_h;
+            pz = pz - (vz * dt) * kp.inv_h;
+        } else {
+            px = px - (vx * dt) / kp.h;
+            py = py - (vy * dt) / kp.h;
+            pz = pz - (vz * dt) / kp.h;
+        }
+        istep++;
+        if (istep < kp.substeps) vel(px, py, pz, vx, vy, vz, ci, cj, ck);
+    } while (istep < kp.substeps);
+    if (kp.full && !broke && inside(px, py, pz)) {
+        const int i = min((int)floorf(px), L.W - 1), j = min((int)floorf(py), L.H - 1);
+        const int k = min((int)floorf(pz), L.D - 1);
+        if (__ldg(flags + lidx(L, i, j, k)) & F_FREE) {
+            lx = px;
+            ly = py;
+            lz = pz;
+        }
     }
     px = lx;
     py = ly;
