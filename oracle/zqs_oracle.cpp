@@ -588,8 +588,11 @@ void reinject(const Dims& d, R* T, R* rho, const zqs_params& P) {
  *   update p = (sum w*p_n - div) / sum w                      CPU_PoissonSolver3D_OpenOctreePoisson.cpp:401-440
  *   gradient: u -= p_R - p_L on faces between free cells, open
  *     domain faces use p=0 outside                            Utils3D:2794-2926
- * Added: over-relaxation p <- (1-omega)*p + omega*GS (omega=1 gives GS
- * exactly), cold start p=0, neighbours summed in the order x-,x+,y-,y+,z-,z+.
+ * Added: over-relaxation p <- (1-omega)*p + omega*GS, evaluated as
+ * fma(omega/cnt, s - div, (1-omega)*p) with omega/cnt rounded once (a
+ * per-cell constant); cold start p=0; neighbours summed in the order
+ * x-,x+,y-,y+,z-,z+.  (The reference's SOR source is not in its tree, so the
+ * rounding of the update is this restatement's choice.)
  * Stats: max|div| after projection and ||div - Lp||_2, both in FP64. */
 template <class R>
 void project(const Dims& d, R* u, R* v, R* w, const uint8_t* occ, const zqs_params& P, R* p_out,
@@ -673,8 +676,8 @@ void project(const Dims& d, R* u, R* v, R* w, const uint8_t* occ, const zqs_para
                         if (j < H - 1 && !occ[c + sy]) s = s + p[c + sy];
                         if (k > 0 && !occ[c - sz]) s = s + p[c - sz];
                         if (k < D - 1 && !occ[c + sz]) s = s + p[c + sz];
-                        R gs = (s - div[c]) / cnt[c];
-                        p[c] = om1 * p[c] + omega * gs;
+                        const R wc = omega / cnt[c];
+                        p[c] = std::fma(wc, s - div[c], om1 * p[c]);
                     }
         }
     }

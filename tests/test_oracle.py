@@ -164,6 +164,12 @@ def test_closed_solver_removes_mean_divergence(oracle64):
     assert stats.residual_l2 < 1e-9
 
 
+def _fma(a, b, c):
+    """Correctly rounded a*b + c in double (exact rational arithmetic)."""
+    from fractions import Fraction
+    return float(Fraction(a) * Fraction(b) + Fraction(c))
+
+
 def _py_sor(div, occ, K, omega, open_):
     """Pure-Python red-black SOR on a tiny grid (same operation order)."""
     D, H, W = occ.shape
@@ -187,7 +193,7 @@ def _py_sor(div, occ, K, omega, open_):
                                 cnt += 1
                         if cnt == 0:
                             continue
-                        p[k, j, i] = (1.0 - omega) * p[k, j, i] + omega * ((s - div[k, j, i]) / cnt)
+                        p[k, j, i] = _fma(omega / cnt, s - div[k, j, i], (1.0 - omega) * p[k, j, i])
     return p
 
 

@@ -134,9 +134,10 @@ __global__ void k_div_subtract_const(Layout L, const uint8_t* __restrict__ flags
     if (__ldg(flags + c) & F_FREE) div[c] = div[c] - m;
 }
 
-__device__ __forceinline__ float sor_update(float pc, float s, float d, int cnt, float omega, float om1) {
-    float gs = (s - d) / (float)cnt;
-    return om1 * pc + omega * gs;
+// p = (1-omega) p + (omega/cnt)(s - d), evaluated as one fused multiply-add
+// with the per-cell weight wc = omega/cnt (one rounding), as the oracle does.
+__device__ __forceinline__ float sor_update(float pc, float s, float d, float wc, float om1) {
+    return __fmaf_rn(wc, s - d, om1 * pc);
 }
 
 // One colour, in place; one thread per cell.
@@ -159,7 +160,7 @@ __global__ void k_sor_colour(Layout L, float* __restrict__ p, const float* __res
     s = s + p[c + px];
     s = s + p[c - pl];
     s = s + p[c + pl];
-    p[c] = sor_update(p[c], s, __ldg(div + c), cnt, omega, om1);
+    p[c] = sor_update(p[c], s, __ldg(div + c), omega / (float)cnt, om1);
 }
 
 template <int S, int TX, int TY, int PPT>
@@ -295,7 +296,7 @@ __global__ void __launch_bounds__(RbShape<S, TX, TY, PPT>::NT)
                                     sum = sum + sp[(szm * 2 + (c ^ 1)) * CA + me[q]];
                                     sum = sum + sp[(szp * 2 + (c ^ 1)) * CA + me[q]];
                                     float* Pc = sp + (sz * 2 + c) * CA + me[q];
-                                    *Pc = sor_update(*Pc, sum, sd[(sz * 2 + c) * CA + me[q]], cnt, omega, om1);
+                                    *Pc = sor_update(*Pc, sum, sd[(sz * 2 + c) * CA + me[q]], omega / (float)cnt, om1);
                                 }
                             }
                         }
@@ -363,6 +364,12 @@ __device__ __forceinline__ void sor_reg_tile(const Layout& L, const float* __res
     const int z0 = bz * zc;
     const int z1 = min(z0 + zc, L.D);
     const int plane = (int)L.plane;
+    // forward: the update weight omega/cnt by stencil weight (entry 0 unused)
+    __shared__ float wtab[8];
+    if (!ADJ) {
+        if (threadIdx.x < 8) wtab[threadIdx.x] = threadIdx.x ? omega / (float)threadIdx.x : 0.0f;
+        __syncthreads();
+    }
 
     int me[PPT], jrow[PPT], gaddr[PPT];
     unsigned amask[PPT];
@@ -493,7 +500,7 @@ __device__ __forceinline__ void sor_reg_tile(const Layout& L, const float* __res
                                     nv = om1 * old + wgt * sum;
                                     A[q][ADJ ? sz : 0][c] += old;
                                 } else {
-                                    nv = sor_update(P[q][sz][c], sum, sd[(sz * 2 + c) * CA + me[q]], cnt, omega,
+                                    nv = sor_update(P[q][sz][c], sum, sd[(sz * 2 + c) * CA + me[q]], wtab[cnt],
                                                     om1);
                                 }
                                 P[q][sz][c] = nv;
@@ -560,223 +567,6 @@ __global__ void __launch_bounds__(RegShape<S, TX, TY, PPT>::NT)
                   float* __restrict__ acc, float om1, int zc) {
     sor_reg_tile<S, TX, TY, PPT, true>(L, qin, qout, wt, nullptr, 0.0f, om1, zc, blockIdx.x, blockIdx.y,
                                        blockIdx.z, acc);
-}
-
-// Quad form: one thread owns four consecutive cells along x (two of each
-// colour), so each half-sweep updates two same-colour cells at once with the
-// Blackwell FP32x2 instructions (add/mul/fma .rn.f32x2 for the neighbour sum
-// and the division; the final (1-omega)*p + omega*q stays scalar).  The
-// quad's own planes live in registers, colour-compressed as float2 (lane A =
-// the lower-x cell of that colour, lane B = the higher); neighbours in rows
-// y+-1 read one float2 from shared memory for both lanes, the x neighbour of
-// the outer cell reads one float from the adjacent quad.
-//
-// Division by the stencil weight: for weight 6 the quotient is formed as
-// 0.5 * (q0 + r*(x - 3*q0)) with q0 = x*RN(1/3) (one FMA correction of the
-// reciprocal product, Markstein's method).  An exhaustive check of all 2^32
-// float inputs showed it equals RN(x/6) for every |x| >= 1e-36; other
-// weights, tiny and non-finite values take the IEEE division per lane.
-template <int S, int TX, int TY>
-struct QuadShape {
-    static_assert(S % 2 == 0 && TX % 4 == 0 && (TX + 2 * S) % 4 == 0, "quads must tile the region");
-    static constexpr int RW = TX + 2 * S;
-    static constexpr int RH = TY + 2 * S;
-    static constexpr int QW = RW / 4;     // quads per row
-    static constexpr int NT = QW * RH;    // threads
-    static constexpr int NP = 2 * S + 2;  // ring planes
-    static constexpr size_t smem = (size_t)NP * 2 * NT * (8 + 8);  // float2 pressure + float2 divergence
-};
-
-__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
-
-// FP32x2 add / mul / fma as PTX with an explicit .rn rounding modifier: such
-// instructions are never contracted, so a packed multiply followed by a packed
-// add rounds twice, exactly like the scalar code (and the oracle).
-__device__ __forceinline__ unsigned long long pk(float2 a) {
-    unsigned long long r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
-    return r;
-}
-__device__ __forceinline__ float2 upk(unsigned long long r) {
-    float2 a;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(a.x), "=f"(a.y) : "l"(r));
-    return a;
-}
-__device__ __forceinline__ float2 add2(float2 a, float2 b) {
-    unsigned long long d;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk(a)), "l"(pk(b)));
-    return upk(d);
-}
-__device__ __forceinline__ float2 mul2(float2 a, float2 b) {
-    unsigned long long d;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk(a)), "l"(pk(b)));
-    return upk(d);
-}
-__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
-    unsigned long long d;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(pk(a)), "l"(pk(b)), "l"(pk(c)));
-    return upk(d);
-}
-
-template <int S, int TX, int TY>
-__global__ void __launch_bounds__(QuadShape<S, TX, TY>::NT)
-    k_sor_quad(Layout L, const float* __restrict__ pin, float* __restrict__ pout, const float* __restrict__ div,
-               const uint8_t* __restrict__ flags, float omega, float om1, int zc) {
-    using Sh = QuadShape<S, TX, TY>;
-    constexpr int QW = Sh::QW, NP = Sh::NP, NT = Sh::NT;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    float2* sp = reinterpret_cast<float2*>(smem_raw);  // [NP][2][NT] pressure by colour
-    float2* sd = sp + NP * 2 * NT;                       // [NP][2][NT] divergence by colour
-
-    const int me = threadIdx.x;
-    const int row = me / QW, mq = me - row * QW;
-    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
-    const int z0 = blockIdx.z * zc;
-    const int z1 = min(z0 + zc, L.D);
-    const int plane = (int)L.plane;
-    const int xq = x0 - S + 4 * mq;  // global x of the quad's first cell (even)
-    const int j = y0 - S + row;
-    const int ly = row - S, lxq = 4 * mq - S;
-    unsigned amask = 0;  // bit 4r+k: cell k of the quad is inside the ring-r region
-#pragma unroll
-    for (int r = 0; r < S; r++)
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
-            const int lx = lxq + k;
-            if (lx >= -r && lx < TX + r && ly >= -r && ly < TY + r) amask |= 1u << (4 * r + k);
-        }
-    const bool rowin = j >= 0 && j < L.H;
-    const bool h0 = rowin && xq >= 0 && xq < L.W;          // pair (xq, xq+1) loadable
-    const bool h1 = rowin && xq + 2 >= 0 && xq + 2 < L.W;  // pair (xq+2, xq+3)
-    const bool o0 = h0 && ly >= 0 && ly < TY && lxq >= 0 && lxq < TX;
-    const bool o1 = h1 && ly >= 0 && ly < TY && lxq + 2 >= 0 && lxq + 2 < TX;
-    int gaddr = rowin ? lidx(L, xq, j, z0 - S) : 0;
-
-    const int tbeg = z0 - S;
-    const int nsteps = (z1 - z0) + 3 * S + 1;
-    const int flo = max(0, z0 - S), fhi = min(L.D, z1 + S);
-
-    float2 P[NP][2];   // pressure by colour (lanes A, B)
-    unsigned F[NP];    // flags: byte (2c + lane) belongs to that cell
-    float2 na = f2(0.f, 0.f), nb = na, da = na, db = na;  // prefetched pairs (p and div)
-    unsigned nfa = 0, nfb = 0;
-#pragma unroll
-    for (int a = 0; a < NP; a++) {
-        P[a][0] = P[a][1] = f2(0.f, 0.f);
-        F[a] = 0u;
-    }
-    auto fetch = [&](int t, int addr) {
-        na = nb = da = db = f2(0.f, 0.f);
-        nfa = nfb = 0;
-        if (t >= flo && t < fhi) {
-            if (h0) {
-                na = __ldg(reinterpret_cast<const float2*>(pin + addr));
-                da = __ldg(reinterpret_cast<const float2*>(div + addr));
-                nfa = __ldg(reinterpret_cast<const unsigned short*>(flags + addr));
-            }
-            if (h1) {
-                nb = __ldg(reinterpret_cast<const float2*>(pin + addr + 2));
-                db = __ldg(reinterpret_cast<const float2*>(div + addr + 2));
-                nfb = __ldg(reinterpret_cast<const unsigned short*>(flags + addr + 2));
-            }
-        }
-    };
-    fetch(tbeg, gaddr);
-    const float2 ZERO = f2(0.f, 0.f);
-    const float2 R3 = f2(1.0f / 3.0f, 1.0f / 3.0f), NC3 = f2(-3.0f, -3.0f), HALF = f2(0.5f, 0.5f);
-
-    for (int g = 0; g < nsteps; g += NP) {
-#pragma unroll
-        for (int qs = 0; qs < NP; qs++) {
-            if (g + qs < nsteps) {
-                const int t = tbeg + g + qs;
-                const int lc = (j + t) & 1;  // colour of cells 0 and 2 at plane t
-                {   // 1. plane t: cells (0,1,2,3) -> colour lc (0,2), colour lc^1 (1,3)
-                    const float2 cl = f2(na.x, nb.x), co = f2(na.y, nb.y);
-                    const float2 dl = f2(da.x, db.x), dq = f2(da.y, db.y);
-                    // flags bytes: cell0 = nfa&255, cell1 = nfa>>8, cell2 = nfb&255, cell3 = nfb>>8
-                    const unsigned fl = (nfa & 0xffu) | ((nfb & 0xffu) << 8);  // colour lc: lanes A,B
-                    const unsigned fo = (nfa >> 8) | ((nfb >> 8) << 8);        // colour lc^1
-                    P[qs][0] = lc ? co : cl;
-                    P[qs][1] = lc ? cl : co;
-                    F[qs] = lc ? (fo | (fl << 16)) : (fl | (fo << 16));
-                    sp[(qs * 2 + 0) * NT + me] = P[qs][0];
-                    sp[(qs * 2 + 1) * NT + me] = P[qs][1];
-                    sd[(qs * 2 + 0) * NT + me] = lc ? dq : dl;
-                    sd[(qs * 2 + 1) * NT + me] = lc ? dl : dq;
-                }
-                gaddr += plane;
-                fetch(t + 1, gaddr);
-#pragma unroll
-                for (int s = 1; s <= S; s++) {
-                    const int z = t - 2 * s;
-                    const int r = S - s;
-                    if (z >= max(z0 - r, 0) && z < min(z1 + r, L.D)) {
-                        const int c = (s - 1) & 1;
-                        const int sz = (qs - 2 * s + 2 * NP) % NP;
-                        const int szm = (sz + NP - 1) % NP;
-                        const int szp = (sz + 1) % NP;
-                        const int o = lc ^ c;  // colour-c cells are quad cells o and o+2
-                        const unsigned fb = F[sz] >> (16 * c);
-                        const int cA = (fb >> F_CNT_SHIFT) & 7, cB = (fb >> (8 + F_CNT_SHIFT)) & 7;
-                        const bool liveA = ((amask >> (4 * r + o)) & 1u) && cA;
-                        const bool liveB = ((amask >> (4 * r + o + 2)) & 1u) && cB;
-                        if (liveA || liveB) {
-                            const float2 own = P[sz][c ^ 1];  // colour c' cells of this quad
-                            const float2* Po = sp + (sz * 2 + (c ^ 1)) * NT + me;
-                            float2 xm, xp;
-                            if (o == 0) {
-                                const float ext = liveA ? Po[-1].y : 0.0f;  // previous quad, cell 3
-                                xm = f2(ext, own.x);
-                                xp = own;
-                            } else {
-                                const float ext = liveB ? Po[1].x : 0.0f;   // next quad, cell 0
-                                xm = own;
-                                xp = f2(own.y, ext);
-                            }
-                            float2 sum = add2(ZERO, xm);
-                            sum = add2(sum, xp);
-                            sum = add2(sum, Po[-QW]);
-                            sum = add2(sum, Po[QW]);
-                            sum = add2(sum, P[szm][c ^ 1]);
-                            sum = add2(sum, P[szp][c ^ 1]);
-                            const float2 dd = sd[(sz * 2 + c) * NT + me];
-                            const float2 x = add2(sum, f2(-dd.x, -dd.y));
-                            float2 q;
-                            const float ax = fabsf(x.x), ay = fabsf(x.y);
-                            if (cA == 6 && cB == 6 && ax >= 1e-36f && ax <= 3.0e38f && ay >= 1e-36f &&
-                                ay <= 3.0e38f) {
-                                const float2 q0 = mul2(x, R3);
-                                const float2 e = fma2(q0, NC3, x);
-                                q = mul2(fma2(e, R3, q0), HALF);
-                            } else {
-                                q = f2(x.x / (float)(cA ? cA : 1), x.y / (float)(cB ? cB : 1));
-                            }
-                            const float2 old = P[sz][c];
-                            // Scalar on purpose: a packed multiply feeding a packed add
-                            // is contracted into an FMA by the assembler even with
-                            // explicit .rn (measured), which changes the rounding.
-                            const float2 nv = f2(om1 * old.x + omega * q.x, om1 * old.y + omega * q.y);
-                            const float2 res = f2(liveA ? nv.x : old.x, liveB ? nv.y : old.y);
-                            P[sz][c] = res;
-                            sp[(sz * 2 + c) * NT + me] = res;
-                        }
-                    }
-                }
-                const int zo = t - 2 * S - 1;
-                if (zo >= z0 && zo < z1) {
-                    const int so = (qs - 2 * S - 1 + 2 * NP) % NP;
-                    const bool lco = ((j + zo) & 1) != 0;
-                    const float2 a = lco ? P[so][1] : P[so][0];  // cells 0,2
-                    const float2 b = lco ? P[so][0] : P[so][1];  // cells 1,3
-                    float* dst = pout + gaddr - (2 * S + 2) * plane;
-                    if (o0) *reinterpret_cast<float2*>(dst) = f2(a.x, b.x);
-                    if (o1) *reinterpret_cast<float2*>(dst + 2) = f2(a.y, b.y);
-                }
-                __syncthreads();
-            }
-        }
-    }
 }
 
 // u -= p_R - p_L on live faces; OPEN also updates domain faces with p = 0 outside.
@@ -1046,40 +836,10 @@ RbVariant reg_variant() {
     return v;
 }
 
-template <int S, int TX, int TY>
-cudaError_t quad_launch(dim3 gr, const Layout& L, const float* pin, float* pout, const float* div,
-                        const uint8_t* flags, float omega, float om1, int zc, cudaStream_t st) {
-    using Sh = QuadShape<S, TX, TY>;
-    k_sor_quad<S, TX, TY><<<gr, Sh::NT, Sh::smem, st>>>(L, pin, pout, div, flags, omega, om1, zc);
-    return cudaGetLastError();
-}
-
-template <int S, int TX, int TY>
-RbVariant quad_variant() {
-    using Sh = QuadShape<S, TX, TY>;
-    RbVariant v;
-    v.S = S;
-    v.TX = TX;
-    v.TY = TY;
-    v.ppt = 2;  // two pairs (one quad) per thread
-    v.nt = Sh::NT;
-    v.smem = Sh::smem;
-    v.ctas_per_sm = 0;
-    v.launch = &quad_launch<S, TX, TY>;
-    v.launch_adj = nullptr;
-    v.fn_adj = nullptr;
-    v.ctas_per_sm_adj = 0;
-    v.launch_batch = nullptr;
-    v.fn_batch = nullptr;
-    v.ctas_per_sm_batch = 0;
-    v.fn = (const void*)k_sor_quad<S, TX, TY>;
-    return v;
-}
-
 // The registry of fused SOR variants (temporal depth S/2, tile, pairs per thread);
 // 0-9 keep every plane in shared memory (k_sor_rb), 10-17 keep the thread's own
-// column in registers (k_sor_reg), 18-23 are the FP32x2 quad form (k_sor_quad).
-constexpr int kNumVariants = 24;
+// column in registers (k_sor_reg).
+constexpr int kNumVariants = 18;
 RbVariant g_var[kNumVariants];
 // default variant per depth 1..4
 // (measured at 256^3 on GB300: register-column 64x16 at depth 2 is fastest)
@@ -1132,12 +892,6 @@ int sor_prepare() {
     g_var[15] = reg_variant<6, 32, 16, 1>();
     g_var[16] = reg_variant<2, 32, 16, 2>();
     g_var[17] = reg_variant<4, 32, 16, 2>();
-    g_var[18] = quad_variant<4, 64, 16>();
-    g_var[19] = quad_variant<4, 32, 16>();
-    g_var[20] = quad_variant<2, 64, 16>();
-    g_var[21] = quad_variant<2, 32, 16>();
-    g_var[22] = quad_variant<4, 32, 32>();
-    g_var[23] = quad_variant<6, 32, 16>();
     int dev = 0;
     ZQS_CUDA_TRY(cudaGetDevice(&dev));
     ZQS_CUDA_TRY(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
