@@ -1,0 +1,157 @@
+"""The C++ host API with the reference's class names (include/zqs_smoke3d.h).
+
+A small driver (tests/cpp/smoke3d_driver.cpp) is compiled against the built
+library.  CPU: config parsing (the reference's key/value format plus the added
+keys) and ZQ_InitFineGrid3D against the Python workload builders.  GPU: the
+resident path (ZQ_SmokeSimulation3D::Init + Run, .di3 frames) equals the
+free-function path (ZQ_UpdateOneFrame3D) and the FP32 oracle bit for bit.
+"""
+import ctypes as C
+import math
+import shutil
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from zq_smokesimulation_gb300 import capi
+from zq_smokesimulation_gb300 import workloads as wl
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+@pytest.fixture(scope="module")
+def driver(zqs_lib, tmp_path_factory):
+    gxx = shutil.which("g++")
+    if not gxx:
+        pytest.skip("g++ missing")
+    out = tmp_path_factory.mktemp("drv") / "smoke3d_driver"
+    libdir = ROOT / "zq_smokesimulation_gb300" / "lib"
+    cmd = [gxx, "-std=c++17", "-O1", f"-I{ROOT / 'include'}", str(ROOT / "tests" / "cpp" / "smoke3d_driver.cpp"),
+           f"-L{libdir}", "-lzqs_gb300", f"-Wl,-rpath,{libdir}", "-o", str(out)]
+    subprocess.run(cmd, check=True, capture_output=True, text=True)
+    return out
+
+
+CONFIG = """resolution 24 20 16
+subSize 4
+source 0.5 0.15 0.5 0.1 0.08 0.12 1.0 1.0
+sphereSource 0.3 0.2 0.6 0.12 0.7 0.5
+Tamb 0
+confineCoeff 0.2
+steps 4
+stepTime 0.05
+frameCount 3
+maxIter 12
+omega 1.9
+alpha 0.1
+beta 0.5
+velAttenFactor 0.99
+tempAttenCoeff 0.2
+densityAttenFactor 0.99
+wallsExceptTop true
+obstacleBox 8 10 9 11 5 8
+noiseAmp 0.05
+seed 3
+advVelType inMAC_outMAC
+advScaType MAC
+globalGridSolver COARSE_CLOSED_POISSON_SOR
+"""
+
+
+def run_driver(driver, mode, cfg_text, outdir):
+    outdir.mkdir(parents=True, exist_ok=True)
+    cfg = outdir / "config.txt"
+    cfg.write_text(cfg_text)
+    r = subprocess.run([str(driver), mode, str(cfg), str(outdir)], capture_output=True, text=True)
+    assert r.returncode == 0, (mode, r.returncode, r.stdout, r.stderr)
+    return outdir
+
+
+def load_setup(outdir, W, H, D):
+    p = capi.Params.from_buffer_copy((outdir / "params.bin").read_bytes())
+    occ = np.fromfile(outdir / "occupancy.bin", np.uint8).reshape(D, H, W)
+    st = load_guide(outdir / "init.guidedat", W, H, D)
+    return p, occ, st
+
+
+def load_guide(path, W, H, D):
+    a = np.fromfile(path, np.float32)
+    nu, nv, nw, n = (W + 1) * H * D, W * (H + 1) * D, W * H * (D + 1), W * H * D
+    assert a.size == nu + nv + nw + 2 * n
+    o = np.cumsum([0, nu, nv, nw, n, n])
+    return {"u": a[o[0]:o[1]].reshape(D, H, W + 1), "v": a[o[1]:o[2]].reshape(D, H + 1, W),
+            "w": a[o[2]:o[3]].reshape(D + 1, H, W), "rho": a[o[3]:o[4]].reshape(D, H, W),
+            "T": a[o[4]:o[5]].reshape(D, H, W)}
+
+
+def load_di3(path):
+    b = Path(path).read_bytes()
+    assert b[:5] == b"float" and len(b) >= 33
+    W, H, D, ch = np.frombuffer(b[16:32], np.int32)
+    assert ch == 1
+    return np.frombuffer(b[33:], np.float32).reshape(D, H, W)
+
+
+def test_config_and_initial_state(driver, tmp_path):
+    out = run_driver(driver, "parse", CONFIG, tmp_path / "p")
+    W, H, D = 24, 20, 16
+    p, occ, st = load_setup(out, W, H, D)
+    assert (p.substeps, p.sor_iters, p.solver) == (4, 12, capi.SOLVER_OPEN)  # wallsExceptTop -> open solver
+    assert p.voxel_size == np.float32(1.0 / 24) and p.omega == np.float32(1.9)
+    assert p.gravity == np.float32(0.1) and p.buoyancy == np.float32(0.5) and p.confine == np.float32(0.2)
+    assert p.vel_atten == np.float32(0.99) and p.dens_atten == np.float32(0.99)
+    assert p.temp_atten == np.float32(math.exp(np.float32(-0.05) * np.float32(0.2)))
+    assert (p.adv_vel_mode, p.adv_sca_mode) == (capi.ADV_VEL_INMAC_OUTMAC, capi.ADV_SCA_MAC)
+    assert p.n_sources == 2
+    s0, s1 = p.sources[0], p.sources[1]
+    assert s0.shape == capi.SOURCE_BOX and s0.cx == np.float32(0.5) * 24 and s0.hy == np.float32(0.08) * 20
+    assert s1.shape == capi.SOURCE_SPHERE and s1.hx == np.float32(0.12) * 24 and s1.temperature == np.float32(0.5)
+    ref_occ = wl.add_box(wl.walls_open_top(W, H, D), 8, 10, 9, 11, 5, 8)
+    np.testing.assert_array_equal(occ, ref_occ)
+    u, v, w = wl.initial_velocity(ref_occ, 3, amp=0.05)
+    np.testing.assert_array_equal(st["u"], u)
+    np.testing.assert_array_equal(st["v"], v)
+    np.testing.assert_array_equal(st["w"], w)
+    assert not st["rho"].any() and not st["T"].any()
+
+
+def test_reference_config_quirks(driver, tmp_path):
+    # the reference's own preview config: "step" is not a key (steps stays 20),
+    # "inReg_outMAC2" is an unknown advection type, so LoadFromFile fails
+    bad = "resolution 16 16 16\nsubSize 2\nsource 0.5 0.1 0.5 0.1 0.05 0.1 0.8 20\nadvVelType inReg_outMAC2\n"
+    cfg = tmp_path / "bad.txt"
+    cfg.write_text(bad)
+    r = subprocess.run([str(driver), "parse", str(cfg), str(tmp_path)], capture_output=True, text=True)
+    assert r.returncode == 3
+    ok = "resolution 16 16 16\nsubSize 2\nsource 0.5 0.1 0.5 0.1 0.05 0.1 0.8 20\nstep 30\nvelAttenCoeff 10\n"
+    out = run_driver(driver, "parse", ok, tmp_path / "q")
+    p, occ, _ = load_setup(out, 16, 16, 16)
+    assert p.substeps == 20 and p.sor_iters == 100 and p.solver == capi.SOLVER_OPEN
+    assert p.vel_atten == np.float32(math.exp(np.float32(-0.01) * np.float32(10.0)))
+    assert (p.adv_vel_mode, p.adv_sca_mode) == (capi.ADV_VEL_INREG_OUTREG, capi.ADV_SCA_REG)
+    assert not occ.any()  # open solver, no internal object
+    nosrc = "resolution 16 16 16\nsubSize 2\n"
+    cfg.write_text(nosrc)
+    assert subprocess.run([str(driver), "parse", str(cfg), str(tmp_path)], capture_output=True).returncode == 3
+
+
+@pytest.mark.gpu
+def test_resident_and_stage_paths_match_oracle(driver, tmp_path, oracle32):
+    W, H, D = 24, 20, 16
+    run_out = run_driver(driver, "run", CONFIG, tmp_path / "run")
+    stage_out = run_driver(driver, "stages", CONFIG, tmp_path / "stages")
+    p, occ, st = load_setup(run_out, W, H, D)
+    ref = {k: np.ascontiguousarray(v) for k, v in st.items()}
+    for i in range(3):
+        rc, _ = oracle32.step(W, H, D, ref, occ, p, 1)
+        assert rc == 0
+        resident = load_di3(run_out / f"frame{i}.di3")
+        staged = load_di3(stage_out / f"stage_frame{i}.di3")
+        np.testing.assert_array_equal(resident, ref["rho"])
+        np.testing.assert_array_equal(staged, ref["rho"])
+    fin = load_guide(run_out / "final.guidedat", W, H, D)
+    for k in ("u", "v", "w", "T", "rho"):
+        np.testing.assert_array_equal(fin[k], ref[k])
+    assert float(ref["rho"].sum()) > 0.0
