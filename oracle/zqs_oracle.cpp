@@ -590,8 +590,8 @@ void reinject(const Dims& d, R* T, R* rho, const zqs_params& P) {
  *     domain faces use p=0 outside                            Utils3D:2794-2926
  * Added: over-relaxation p <- (1-omega)*p + omega*GS, evaluated as
  * fma(omega/cnt, s - div, (1-omega)*p) with omega/cnt rounded once (a
- * per-cell constant); cold start p=0; neighbours summed in the order
- * x-,x+,y-,y+,z-,z+.  (The reference's SOR source is not in its tree, so the
+ * per-cell constant); cold start p=0; neighbours summed as the tree
+ * ((x- + x+) + (y- + y+)) + (z- + z+), +0 for excluded neighbours.  (The reference's SOR source is not in its tree, so the
  * rounding of the update is this restatement's choice.)
  * Stats: max|div| after projection and ||div - Lp||_2, both in FP64. */
 template <class R>
@@ -669,13 +669,13 @@ void project(const Dims& d, R* u, R* v, R* w, const uint8_t* occ, const zqs_para
                     for (int i = (j + k + colour) & 1; i < W; i += 2) {
                         size_t c = d.cell(i, j, k);
                         if (occ[c] || cnt[c] == R(0)) continue;
-                        R s = R(0);
-                        if (i > 0 && !occ[c - 1]) s = s + p[c - 1];
-                        if (i < W - 1 && !occ[c + 1]) s = s + p[c + 1];
-                        if (j > 0 && !occ[c - sy]) s = s + p[c - sy];
-                        if (j < H - 1 && !occ[c + sy]) s = s + p[c + sy];
-                        if (k > 0 && !occ[c - sz]) s = s + p[c - sz];
-                        if (k < D - 1 && !occ[c + sz]) s = s + p[c + sz];
+                        const R xm = (i > 0 && !occ[c - 1]) ? p[c - 1] : R(0);
+                        const R xp = (i < W - 1 && !occ[c + 1]) ? p[c + 1] : R(0);
+                        const R ym = (j > 0 && !occ[c - sy]) ? p[c - sy] : R(0);
+                        const R yp = (j < H - 1 && !occ[c + sy]) ? p[c + sy] : R(0);
+                        const R zm = (k > 0 && !occ[c - sz]) ? p[c - sz] : R(0);
+                        const R zp = (k < D - 1 && !occ[c + sz]) ? p[c + sz] : R(0);
+                        const R s = ((xm + xp) + (ym + yp)) + (zm + zp);
                         const R wc = omega / cnt[c];
                         p[c] = std::fma(wc, s - div[c], om1 * p[c]);
                     }

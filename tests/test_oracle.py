@@ -171,7 +171,9 @@ def _fma(a, b, c):
 
 
 def _py_sor(div, occ, K, omega, open_):
-    """Pure-Python red-black SOR on a tiny grid (same operation order)."""
+    """Pure-Python red-black SOR on a tiny grid (same operation order: the
+    neighbour sum ((x- + x+) + (y- + y+)) + (z- + z+) with 0 for excluded
+    neighbours, then fma(omega/cnt, s - div, (1-omega) p))."""
     D, H, W = occ.shape
     p = np.zeros((D, H, W))
     nb = [(-1, 0, 0), (1, 0, 0), (0, -1, 0), (0, 1, 0), (0, 0, -1), (0, 0, 1)]
@@ -182,17 +184,20 @@ def _py_sor(div, occ, K, omega, open_):
                     for i in range(W):
                         if (i + j + k) % 2 != colour or occ[k, j, i]:
                             continue
-                        s, cnt = 0.0, 0
+                        vals, cnt = [], 0
                         for di, dj, dk in nb:
                             a, b, c = i + di, j + dj, k + dk
+                            val = 0.0
                             if 0 <= a < W and 0 <= b < H and 0 <= c < D:
                                 if not occ[c, b, a]:
-                                    s = s + p[c, b, a]
+                                    val = p[c, b, a]
                                     cnt += 1
                             elif open_:
                                 cnt += 1
+                            vals.append(val)
                         if cnt == 0:
                             continue
+                        s = ((vals[0] + vals[1]) + (vals[2] + vals[3])) + (vals[4] + vals[5])
                         p[k, j, i] = _fma(omega / cnt, s - div[k, j, i], (1.0 - omega) * p[k, j, i])
     return p
 

@@ -6,12 +6,12 @@
 // oracle states (oracle/zqs_oracle.cpp, project()):
 //   div  = ((((u[i+1]-u[i]) + v[j+1]) - v[j]) + w[k+1]) - w[k]   (closed: minus the FP64 mean)
 //   red cells ((i+j+k)&1)==0 then black, each free cell:
-//     s  = p[x-] + p[x+] + p[y-] + p[y+] + p[z-] + p[z+]   (left to right)
-//     p  = (1-omega)*p + omega*((s - div)/cnt)
+//     s  = ((p[x-] + p[x+]) + (p[y-] + p[y+])) + (p[z-] + p[z+])
+//     p  = fma(omega/cnt, s - div, (1-omega)*p)   (omega/cnt rounded once)
 //   u -= p_R - p_L on live faces (open domain faces use p = 0 outside).
 // Non-free cells and everything outside the domain hold p = +0 permanently,
-// so summing all six neighbours equals summing the free ones bit for bit (a
-// running sum that starts at +0 is never -0, and x + (+0) == x otherwise).
+// so summing all six neighbours equals the oracle's sum, which substitutes +0
+// for the neighbours it excludes.
 //
 // Two SOR kernels:
 //   k_sor_colour  one launch per colour, in place: the plain form, and the
@@ -153,13 +153,7 @@ __global__ void k_sor_colour(Layout L, float* __restrict__ p, const float* __res
     const int cnt = (f & F_CNT_MASK) >> F_CNT_SHIFT;
     if (!(f & F_FREE) || cnt == 0) return;
     const int px = L.px, pl = (int)L.plane;
-    float s = 0.0f;
-    s = s + p[c - 1];
-    s = s + p[c + 1];
-    s = s + p[c - px];
-    s = s + p[c + px];
-    s = s + p[c - pl];
-    s = s + p[c + pl];
+    const float s = ((p[c - 1] + p[c + 1]) + (p[c - px] + p[c + px])) + (p[c - pl] + p[c + pl]);
     p[c] = sor_update(p[c], s, __ldg(div + c), omega / (float)cnt, om1);
 }
 
@@ -288,13 +282,9 @@ __global__ void __launch_bounds__(RbShape<S, TX, TY, PPT>::NT)
                                 const int cnt = (sf[(sz * 2 + c) * CA + me[q]] >> F_CNT_SHIFT) & 7;
                                 if (cnt) {  // zero for cells that are not free
                                     const float* Po = sp + (sz * 2 + (c ^ 1)) * CA + me[q];
-                                    float sum = 0.0f;
-                                    sum = sum + Po[o - 1];
-                                    sum = sum + Po[o];
-                                    sum = sum + Po[-PW];
-                                    sum = sum + Po[PW];
-                                    sum = sum + sp[(szm * 2 + (c ^ 1)) * CA + me[q]];
-                                    sum = sum + sp[(szp * 2 + (c ^ 1)) * CA + me[q]];
+                                    const float sum = ((Po[o - 1] + Po[o]) + (Po[-PW] + Po[PW])) +
+                                                      (sp[(szm * 2 + (c ^ 1)) * CA + me[q]] +
+                                                       sp[(szp * 2 + (c ^ 1)) * CA + me[q]]);
                                     float* Pc = sp + (sz * 2 + c) * CA + me[q];
                                     *Pc = sor_update(*Pc, sum, sd[(sz * 2 + c) * CA + me[q]], omega / (float)cnt, om1);
                                 }
@@ -371,8 +361,8 @@ __device__ __forceinline__ void sor_reg_tile(const Layout& L, const float* __res
         __syncthreads();
     }
 
-    int me[PPT], jrow[PPT], gaddr[PPT];
-    unsigned amask[PPT];
+    int me[PPT], jrow[PPT], gaddr[PPT], bpar[PPT];
+    unsigned amask[PPT], act[PPT][2];
     bool pin_ok[PPT], out_ok[PPT];
 #pragma unroll
     for (int q = 0; q < PPT; q++) {
@@ -395,6 +385,21 @@ __device__ __forceinline__ void sor_reg_tile(const Layout& L, const float* __res
         pin_ok[q] = xl >= 0 && xl < L.W && j >= 0 && j < L.H;
         out_ok[q] = pin_ok[q] && ly >= 0 && ly < TY && lxl >= 0 && lxl < TX;
         gaddr[q] = pin_ok[q] ? lidx(L, xl, j, z0 - S) : 0;
+        // plane t has parity z0 + (ring slot) since t = z0 - S + (multiple of
+        // NP) + slot with S and NP even: the left cell is black at slot qs when
+        // bpar ^ (qs & 1); act[q][qs & 1] bit s-1: half-sweep s updates this pair
+        bpar[q] = (j + z0) & 1;
+#pragma unroll
+        for (int par = 0; par < 2; par++) {
+            unsigned a = 0;
+#pragma unroll
+            for (int sw = 1; sw <= S; sw++) {
+                const int cs = ((sw - 1) & 1) ^ (ADJ ? 1 : 0);
+                const int o = bpar[q] ^ par ^ cs;
+                if ((mk >> (2 * (S - sw) + o)) & 1u) a |= 1u << (sw - 1);
+            }
+            act[q][par] = a;
+        }
     }
 
     const int tbeg = z0 - S;
@@ -435,7 +440,7 @@ __device__ __forceinline__ void sor_reg_tile(const Layout& L, const float* __res
                 // 1. plane t: registers by colour, and publish
 #pragma unroll
                 for (int q = 0; q < PPT; q++) {
-                    const bool lc = ((jrow[q] + t) & 1) != 0;  // the left cell is black
+                    const bool lc = (bpar[q] ^ (qs & 1)) != 0;  // the left cell is black
                     P[q][qs][0] = lc ? np_[q].y : np_[q].x;
                     P[q][qs][1] = lc ? np_[q].x : np_[q].y;
                     F[q][qs] = lc ? (((nf[q] & 0xffu) << 8) | (nf[q] >> 8)) : nf[q];
@@ -480,20 +485,15 @@ __device__ __forceinline__ void sor_reg_tile(const Layout& L, const float* __res
                         const int szp = (sz + 1) % NP;
 #pragma unroll
                         for (int q = 0; q < PPT; q++) {
-                            const int o = ((jrow[q] + t) & 1) ^ c;
+                            const int o = bpar[q] ^ (qs & 1) ^ c;
                             const int cnt = ADJ ? 1 : (F[q][sz] >> (8 * c + F_CNT_SHIFT)) & 7;
                             const float wgt = ADJ ? sd[(sz * 2 + c) * CA + me[q]] : 0.0f;
-                            if (((amask[q] >> (2 * r + o)) & 1u) && cnt && (!ADJ || wgt != 0.0f)) {
+                            if (((act[q][qs & 1] >> (s - 1)) & 1u) && cnt && (!ADJ || wgt != 0.0f)) {
                                 const float* Po = sp + (sz * 2 + (c ^ 1)) * CA + me[q];
                                 const float own = P[q][sz][c ^ 1];
                                 const float adj = o ? Po[1] : Po[-1];
-                                float sum = 0.0f;
-                                sum = sum + (o ? own : adj);
-                                sum = sum + (o ? adj : own);
-                                sum = sum + Po[-PW];
-                                sum = sum + Po[PW];
-                                sum = sum + P[q][szm][c ^ 1];
-                                sum = sum + P[q][szp][c ^ 1];
+                                const float sum =
+                                    ((own + adj) + (Po[-PW] + Po[PW])) + (P[q][szm][c ^ 1] + P[q][szp][c ^ 1]);
                                 float nv;
                                 if (ADJ) {
                                     const float old = P[q][sz][c];
@@ -516,7 +516,7 @@ __device__ __forceinline__ void sor_reg_tile(const Layout& L, const float* __res
 #pragma unroll
                     for (int q = 0; q < PPT; q++) {
                         if (out_ok[q]) {
-                            const bool lc = ((jrow[q] + zo) & 1) != 0;
+                            const bool lc = (bpar[q] ^ (qs & 1) ^ 1) != 0;  // zo = t - 2S - 1
                             const float a = lc ? P[q][so][1] : P[q][so][0];
                             const float b = lc ? P[q][so][0] : P[q][so][1];
                             *reinterpret_cast<float2*>(pout + gaddr[q] - (2 * S + 2) * plane) = make_float2(a, b);
