@@ -47,11 +47,11 @@ def parse():
     ap.add_argument("--cpu-sample", default="plain128", help="grid of the bounded CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--batch", default="batch64", help="mixed-size batch measured beside the plain step ('' = skip)")
+    ap.add_argument("--batch", default="batch64", help="mixed-size batch measured beside the plain step ('' or none = skip)")
     ap.add_argument("--batch-steps", type=int, default=10)
     ap.add_argument("--batch-variant", type=int, default=-1)
     ap.add_argument("--batch-zchunk", type=int, default=0)
-    ap.add_argument("--adjoint", default="64,128", help="control-problem sizes timed for the reverse mode ('' = skip)")
+    ap.add_argument("--adjoint", default="64,128", help="control-problem sizes timed for the reverse mode ('' or none = skip)")
     ap.add_argument("--adjoint-steps", type=int, default=64)
     ap.add_argument("--checkpoint-every", type=int, default=8)
     return ap.parse_args()
@@ -436,10 +436,10 @@ def run_ours(args):
                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                "path": "zqs_grid_upload x5 (pinned host) + zqs_grid_step + zqs_grid_download x5"}
     batch = None
-    if args.batch and world == 1:
+    if args.batch not in ("", "none") and world == 1:
         batch = measure_batch(args, stream)
     adjoint = None
-    if args.adjoint and world == 1:
+    if args.adjoint not in ("", "none") and world == 1:
         adjoint = {f"control{n}": measure_adjoint(args, stream, int(n)) for n in args.adjoint.split(",") if n}
     clocks = sampler.stop()
 

@@ -842,8 +842,9 @@ RbVariant reg_variant() {
 constexpr int kNumVariants = 18;
 RbVariant g_var[kNumVariants];
 // default variant per depth 1..4
-// (measured at 256^3 on GB300: register-column 64x16 at depth 2 is fastest)
-const int kDefaultVariant[5] = {-1, 16, 13, 15, 7};
+// (measured at 256^3 on GB300: register-column 32x32 at depth 2 is fastest,
+// 54.5 us per iteration; depth 1: register-column 64x16, 62.6 us)
+const int kDefaultVariant[5] = {-1, 11, 14, 15, 7};
 // batched default: register-column 32x16 at depth 2 (small tiles suit 32..128 edges)
 const int kBatchDefaultVariant = 12;
 // reversed SOR of the adjoint: register-column variants in order of preference
