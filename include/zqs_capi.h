@@ -193,10 +193,12 @@ ZQS_API int zqs_grid_set_sor_config(zqs_grid* g, int temporal_depth, int split_c
 
 /* Fused SOR kernel variants (for tuning): iterations fused per HBM pass, xy
  * tile, cell pairs per thread, threads and shared memory per CTA, CTAs that fit
- * on one SM of the current device (0: does not fit). */
+ * on one SM of the current device (0: does not fit), whether the update
+ * weights are held in registers, registers per thread. */
 typedef struct zqs_sor_variant {
     int32_t depth, tile_x, tile_y, pairs_per_thread, threads, ctas_per_sm;
     int64_t smem_bytes;
+    int32_t weights_in_registers, registers;
 } zqs_sor_variant;
 ZQS_API int zqs_sor_variant_count(void);
 ZQS_API int zqs_sor_variant_info(int index, zqs_sor_variant* out);

@@ -223,6 +223,22 @@ def test_sor_fused_variants_equal_split(zqs_lib, variant, case):
         assert_same(b, a, keys=("p", "v"), what=f"variant {variant} zchunk {zchunk}")
 
 
+@pytest.mark.parametrize("shape", [(160, 96, 120), (96, 96, 300), (128, 256, 128)])
+@pytest.mark.parametrize("depth", [1, 2])
+def test_sor_default_partition_equal_split(zqs_lib, shape, depth):
+    """The default fused pass with its automatic z chunk reproduces one-colour
+    sweeps bit for bit on grids whose tiles and z chunks are ragged, with an
+    obstacle; K=5 also runs the depth-1 remainder pass."""
+    w = wl.small_case(*shape, K=5, vel_amp=0.3)
+    g1 = gpu_grid(w, sor=(1, True))
+    g1.project()
+    g2 = gpu_grid(w, sor=(depth, False))
+    g2.project()
+    a = {k: g1.download(f) for k, f in (("p", capi.FIELD_PRESSURE), ("v", capi.FIELD_V))}
+    b = {k: g2.download(f) for k, f in (("p", capi.FIELD_PRESSURE), ("v", capi.FIELD_V))}
+    assert_same(b, a, keys=("p", "v"), what=f"{shape} depth {depth}")
+
+
 def test_plain256_one_step_vs_oracle(zqs_lib, oracle32):
     w = wl.make("plain256", K=8)
     g = gpu_grid(w)

@@ -281,7 +281,7 @@ ZQS_API int zqs_adjoint_create(zqs_adjoint** out, zqs_grid* g, int nsteps, int c
     e = cudaStreamSynchronize(w->own);
     if (e != cudaSuccess) return fail(cuda_fail(e, "zqs_adjoint_create: work grid"));
     // sizes: the work grid's own allocation counts too
-    a->bytes += (size_t)fe * 4 * 13 + (size_t)fe * 16 * 2 + (size_t)fe + (size_t)L.W * L.H * L.D;
+    a->bytes += (size_t)fe * 4 * 13 + (size_t)fe * 16 * 5 + (size_t)fe + (size_t)L.W * L.H * L.D;
     *out = a;
     return ZQS_OK;
 }

@@ -181,6 +181,9 @@ int build_table(zqs_batch* b) {
         d.flags = G.flags;
         d.t4a = G.t4a;
         d.t4b = G.t4b;
+        d.q4[0] = G.qu;
+        d.q4[1] = G.qv;
+        d.q4[2] = G.qw;
         d.red = G.red;
         d.red_len = G.red_len;
         d.kp = g->kp;
@@ -251,10 +254,14 @@ int issue_batch_step(zqs_batch* b, int par, cudaStream_t s, LaunchCounter& lc, i
     for (int c = 0; c < TC_COUNT; c++) bl[c] = BatchLaunch{b->d_desc, b->d_pre[c], b->n, b->total[c]};
     int rc = launch_force_batch(bl[TC_CELL], bl[TC_FACE], par, par, b->blocks, s, lc);
     if (rc) return rc;
+    rc = launch_mac_quads_batch(bl[TC_FACE], par, b->blocks, s, lc);
+    if (rc) return rc;
     rc = launch_advect_velocity_batch(bl[TC_ADVF], par, b->blocks, s, lc);
     if (rc) return rc;
     rc = launch_project_batch(bl[TC_CELL], bl[TC_FACE], bl[TC_SORM], bl[TC_SORR], b->plan, b->K, b->any_closed,
                               par ^ 1, b->blocks, s, lc, pfin);
+    if (rc) return rc;
+    rc = launch_mac_quads_batch(bl[TC_FACE], par ^ 1, b->blocks, s, lc);
     if (rc) return rc;
     return launch_advect_scalar_batch(bl[TC_CELL], par ^ 1, par, b->blocks, s, lc);
 }

@@ -226,12 +226,12 @@ ZQS_API int zqs_grid_create(zqs_grid** out, int W, int H, int D) {
     }
     zqs_grid* g = new zqs_grid();
     g->g.L = L;
-    // 13 float fields + 2 float4 fields + flags + FP64 scratch
+    // 13 float fields + 5 float4 fields (2 temporaries, 3 velocity quads) + flags + FP64 scratch
     const size_t fbytes = (size_t)L.elems * 4;
     const size_t nflt = 13;
     const long long nblocks = (long long)((W + 31) / 32) * ((H + 7) / 8) * D;
     g->g.red_len = 3 * nblocks + 16;
-    size_t total = nflt * fbytes + 2 * (size_t)L.elems * 16 + (((size_t)L.elems + 255) / 256) * 256 +
+    size_t total = nflt * fbytes + 5 * (size_t)L.elems * 16 + (((size_t)L.elems + 255) / 256) * 256 +
                    (size_t)g->g.red_len * 8 + 256;
     cudaError_t e = cudaMalloc(&g->base, total);
     if (e != cudaSuccess) {
@@ -292,6 +292,12 @@ ZQS_API int zqs_grid_create(zqs_grid** out, int W, int H, int D) {
     g->g.t4a = (float4*)b + L.plane;
     b += (size_t)L.elems * 16;
     g->g.t4b = (float4*)b + L.plane;
+    b += (size_t)L.elems * 16;
+    g->g.qu = (float4*)b + L.plane;
+    b += (size_t)L.elems * 16;
+    g->g.qv = (float4*)b + L.plane;
+    b += (size_t)L.elems * 16;
+    g->g.qw = (float4*)b + L.plane;
     b += (size_t)L.elems * 16;
     g->g.flags = (uint8_t*)b + L.plane;
     b += (((size_t)L.elems + 255) / 256) * 256;

@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(256) k_adj_scalar(Layout L, AdjFwd f, AdjBufs 
     const float gT = b.gT[c], gD = b.grho[c];
     if (gT == 0.0f && gD == 0.0f) return;
     float xs[3 * (kAdjMaxSubsteps + 1)];
-    const MacVel mv{L, f.u4, f.v4, f.w4};
+    const MacVel mv{L, {f.u4}, {f.v4}, {f.w4}};
     const int m = backtrace_record(L, f.flags, mv, kp, (float)i + 0.5f, (float)j + 0.5f, (float)k + 0.5f, xs);
     const float x = xs[3 * m], y = xs[3 * m + 1], z = xs[3 * m + 2];
     const Corners cc = corners_c(L, x, y, z);
@@ -366,7 +366,7 @@ __global__ void __launch_bounds__(256) k_adj_advect_vel(Layout L, AdjFwd f, AdjB
     const float py0 = (comp == 1) ? (float)j : (float)j + 0.5f;
     const float pz0 = (comp == 2) ? (float)k : (float)k + 0.5f;
     float xs[3 * (kAdjMaxSubsteps + 1)];
-    const MacVel mv{L, f.u2, f.v2, f.w2};
+    const MacVel mv{L, {f.u2}, {f.v2}, {f.w2}};
     const int m = backtrace_record(L, f.flags, mv, kp, px0, py0, pz0, xs);
     const float x = xs[3 * m], y = xs[3 * m + 1], z = xs[3 * m + 2];
     float gx[3];

@@ -22,13 +22,39 @@ namespace zqs {
 
 namespace {
 
+// Quad copies (zqs_sample.cuh, tri0_quad) of the three face components, one
+// thread per face index (i <= W, j <= H, k <= D): q[c][r] = (f[r],
+// f[r + plane], f[r + 1], f[r + plane + 1]).
+__device__ __forceinline__ void mac_quads_tile(const Layout& L, const float* __restrict__ u,
+                                               const float* __restrict__ v, const float* __restrict__ w,
+                                               float4* __restrict__ qu, float4* __restrict__ qv,
+                                               float4* __restrict__ qw, int bx, int by, int bz) {
+    const int i = bx * 32 + threadIdx.x;
+    const int j = by * 8 + threadIdx.y;
+    const int k = bz;
+    if (i > L.W || j > L.H || k > L.D) return;
+    const int c = lidx(L, i, j, k);
+    const int pl = (int)L.plane;
+    qu[c] = make_float4(__ldg(u + c), __ldg(u + c + pl), __ldg(u + c + 1), __ldg(u + c + pl + 1));
+    qv[c] = make_float4(__ldg(v + c), __ldg(v + c + pl), __ldg(v + c + 1), __ldg(v + c + pl + 1));
+    qw[c] = make_float4(__ldg(w + c), __ldg(w + c + pl), __ldg(w + c + 1), __ldg(w + c + pl + 1));
+}
+
+__global__ void __launch_bounds__(256) k_mac_quads(Layout L, const float* __restrict__ u,
+                                                   const float* __restrict__ v, const float* __restrict__ w,
+                                                   float4* __restrict__ qu, float4* __restrict__ qv,
+                                                   float4* __restrict__ qw) {
+    mac_quads_tile(L, u, v, w, qu, qv, qw, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
 // One thread per face: bz = comp*(D+1) + k, comp 0/1/2 = u/v/w.
 // REGIN selects the regular (cell-centre float4) velocity for both the
-// backtrace and the final sample (inRegular_outMAC), else MAC (inMAC_outMAC).
+// backtrace and the final sample (inRegular_outMAC), else MAC (inMAC_outMAC),
+// whose samples read the quad copies q (built from u, v, w).
 template <bool REGIN>
 __device__ __forceinline__ void advect_vel_macout_tile(const Layout& L, const float* __restrict__ u,
                                                        const float* __restrict__ v, const float* __restrict__ w,
-                                                       const float4* __restrict__ vel4,
+                                                       const float4* __restrict__ vel4, const float4* const* q,
                                                        const uint8_t* __restrict__ flags, float* __restrict__ u2,
                                                        float* __restrict__ v2, float* __restrict__ w2,
                                                        const KParams& kp, int open, int bx, int by, int bz) {
@@ -58,24 +84,29 @@ __device__ __forceinline__ void advect_vel_macout_tile(const Layout& L, const fl
             backtrace(L, flags, rv, kp, px, py, pz);
             out = tri4c(vel4, comp, corners(L, L.W, L.H, L.D, px - 0.5f, py - 0.5f, pz - 0.5f));
         } else {
-            MacVel mv{L, u, v, w};
+            const MacVelQ mv{L, {q[0]}, {q[1]}, {q[2]}};
             backtrace(L, flags, mv, kp, px, py, pz);
-            if (comp == 0) out = tri0_sample(u, L, tri0(L, L.W + 1, L.H, L.D, px, py - 0.5f, pz - 0.5f));
-            else if (comp == 1) out = tri0_sample(v, L, tri0(L, L.W, L.H + 1, L.D, px - 0.5f, py, pz - 0.5f));
-            else out = tri0_sample(w, L, tri0(L, L.W, L.H, L.D + 1, px - 0.5f, py - 0.5f, pz));
+            if (comp == 0) out = tri0_quad(q[0], L, tri0(L, L.W + 1, L.H, L.D, px, py - 0.5f, pz - 0.5f));
+            else if (comp == 1) out = tri0_quad(q[1], L, tri0(L, L.W, L.H + 1, L.D, px - 0.5f, py, pz - 0.5f));
+            else out = tri0_quad(q[2], L, tri0(L, L.W, L.H, L.D + 1, px - 0.5f, py - 0.5f, pz));
         }
     }
     dst[c] = out;
 }
 
+struct Quads {
+    const float4* q[3];
+};
+
 template <bool REGIN>
 __global__ void __launch_bounds__(256) k_advect_vel_macout(Layout L, const float* __restrict__ u,
                                                            const float* __restrict__ v, const float* __restrict__ w,
-                                                           const float4* __restrict__ vel4,
+                                                           const float4* __restrict__ vel4, Quads Q,
                                                            const uint8_t* __restrict__ flags, float* __restrict__ u2,
                                                            float* __restrict__ v2, float* __restrict__ w2, KParams kp,
                                                            int open) {
-    advect_vel_macout_tile<REGIN>(L, u, v, w, vel4, flags, u2, v2, w2, kp, open, blockIdx.x, blockIdx.y, blockIdx.z);
+    advect_vel_macout_tile<REGIN>(L, u, v, w, vel4, Q.q, flags, u2, v2, w2, kp, open, blockIdx.x, blockIdx.y,
+                                  blockIdx.z);
 }
 
 // Advect_Velocity_inRegular_outRegular_Kernel (Adv3D:76-113): per cell.
@@ -154,9 +185,8 @@ __device__ __forceinline__ void reinject_cell(const SourceList& src, int i, int 
 // attenuation factors applied to the interpolation corners and the sources
 // reinjected in the epilogue.
 template <bool REGIN>
-__device__ __forceinline__ void advect_scalar_tile(const Layout& L, const float* __restrict__ u,
-                                                   const float* __restrict__ v, const float* __restrict__ w,
-                                                   const float4* __restrict__ vel4, const uint8_t* __restrict__ flags,
+__device__ __forceinline__ void advect_scalar_tile(const Layout& L, const float4* __restrict__ vel4,
+                                                   const float4* const* q, const uint8_t* __restrict__ flags,
                                                    const float* __restrict__ T, const float* __restrict__ rho,
                                                    float* __restrict__ T2, float* __restrict__ rho2,
                                                    const KParams& kp, float aT, float aD, const SourceList& src,
@@ -170,7 +200,7 @@ __device__ __forceinline__ void advect_scalar_tile(const Layout& L, const float*
         RegVel rv{L, vel4};
         backtrace(L, flags, rv, kp, px, py, pz);
     } else {
-        MacVel mv{L, u, v, w};
+        const MacVelQ mv{L, {q[0]}, {q[1]}, {q[2]}};
         backtrace(L, flags, mv, kp, px, py, pz);
     }
     const Tri0 cs = tri0(L, L.W, L.H, L.D, px - 0.5f, py - 0.5f, pz - 0.5f);
@@ -183,18 +213,28 @@ __device__ __forceinline__ void advect_scalar_tile(const Layout& L, const float*
 }
 
 template <bool REGIN>
-__global__ void __launch_bounds__(256) k_advect_scalar(Layout L, const float* __restrict__ u,
-                                                       const float* __restrict__ v, const float* __restrict__ w,
-                                                       const float4* __restrict__ vel4,
+__global__ void __launch_bounds__(256) k_advect_scalar(Layout L, const float4* __restrict__ vel4, Quads Q,
                                                        const uint8_t* __restrict__ flags,
                                                        const float* __restrict__ T, const float* __restrict__ rho,
                                                        float* __restrict__ T2, float* __restrict__ rho2, KParams kp,
                                                        float aT, float aD, SourceList src) {
-    advect_scalar_tile<REGIN>(L, u, v, w, vel4, flags, T, rho, T2, rho2, kp, aT, aD, src, blockIdx.x, blockIdx.y,
+    advect_scalar_tile<REGIN>(L, vel4, Q.q, flags, T, rho, T2, rho2, kp, aT, aD, src, blockIdx.x, blockIdx.y,
                               blockIdx.z);
 }
 
 // ---- batched forms (MAC velocity) ----
+
+// Quad copies of velocity buffer vcur, over the FACE tile class.
+__global__ void __launch_bounds__(256) k_mac_quads_batch(BatchLaunch B, int vcur) {
+    for (int t = blockIdx.x; t < B.total; t += gridDim.x) {
+        const int i = batch_find(B.pre, B.n, t);
+        const InstDesc& d = B.desc[i];
+        const int lt = t - __ldg(B.pre + i);
+        const int gx = (d.L.W + 1 + 31) / 32, gy = (d.L.H + 1 + 7) / 8;
+        const int bx = lt % gx, r = lt / gx, by = r % gy, bz = r / gy;
+        mac_quads_tile(d.L, d.vel[vcur][0], d.vel[vcur][1], d.vel[vcur][2], d.q4[0], d.q4[1], d.q4[2], bx, by, bz);
+    }
+}
 
 __global__ void __launch_bounds__(256) k_advect_vel_batch(BatchLaunch B, int vcur) {
     for (int t = blockIdx.x; t < B.total; t += gridDim.x) {
@@ -205,7 +245,8 @@ __global__ void __launch_bounds__(256) k_advect_vel_batch(BatchLaunch B, int vcu
         const int bx = lt % gx, r = lt / gx, by = r % gy, bz = r / gy;
         const KParams kp = d.kp;
         const int nxt = vcur ^ 1;
-        advect_vel_macout_tile<false>(d.L, d.vel[vcur][0], d.vel[vcur][1], d.vel[vcur][2], d.t4a, d.flags,
+        const float4* q[3] = {d.q4[0], d.q4[1], d.q4[2]};
+        advect_vel_macout_tile<false>(d.L, d.vel[vcur][0], d.vel[vcur][1], d.vel[vcur][2], d.t4a, q, d.flags,
                                       d.vel[nxt][0], d.vel[nxt][1], d.vel[nxt][2], kp, 1, bx, by, bz);
     }
 }
@@ -219,9 +260,9 @@ __global__ void __launch_bounds__(256) k_advect_scalar_batch(BatchLaunch B, int 
         const int bx = lt % gx, r = lt / gx, by = r % gy, bz = r / gy;
         const KParams kp = d.kp;
         const int nxt = scur ^ 1;
-        advect_scalar_tile<false>(d.L, d.vel[vcur][0], d.vel[vcur][1], d.vel[vcur][2], d.t4a, d.flags,
-                                  d.sca[scur][0], d.sca[scur][1], d.sca[nxt][0], d.sca[nxt][1], kp, kp.temp_atten,
-                                  kp.dens_atten, d.src, bx, by, bz);
+        const float4* q[3] = {d.q4[0], d.q4[1], d.q4[2]};
+        advect_scalar_tile<false>(d.L, d.t4a, q, d.flags, d.sca[scur][0], d.sca[scur][1], d.sca[nxt][0],
+                                  d.sca[nxt][1], kp, kp.temp_atten, kp.dens_atten, d.src, bx, by, bz);
     }
 }
 
@@ -239,18 +280,33 @@ __global__ void k_reinject(Layout L, float* __restrict__ T, float* __restrict__ 
 
 }  // namespace
 
+int launch_mac_quads(const DevGrid& g, cudaStream_t s, LaunchCounter& lc) {
+    const Layout& L = g.L;
+    dim3 b(32, 8, 1);
+    dim3 gf((L.W + 1 + 31) / 32, (L.H + 1 + 7) / 8, L.D + 1);
+    k_mac_quads<<<gf, b, 0, s>>>(L, g.u, g.v, g.w, g.qu, g.qv, g.qw);
+    lc.n++;
+    ZQS_LAUNCH_CHECK("k_mac_quads");
+    return ZQS_OK;
+}
+
 int launch_advect_velocity(DevGrid& g, const KParams& kp, int mode, bool open, cudaStream_t s, LaunchCounter& lc) {
     const Layout& L = g.L;
     dim3 b(32, 8, 1);
     if (mode == ZQS_ADV_VEL_INMAC_OUTMAC || mode == ZQS_ADV_VEL_INREG_OUTMAC) {
         int nxb = (L.W + 1 + 31) / 32, nyb = (L.H + 1 + 7) / 8;
         dim3 gr(nxb, nyb, 3 * (L.D + 1));
+        const Quads Q{{g.qu, g.qv, g.qw}};
         if (mode == ZQS_ADV_VEL_INREG_OUTMAC) {
             int rc = launch_mac_to_reg4(g, g.u, g.v, g.w, g.t4a, s, lc);
             if (rc) return rc;
-            k_advect_vel_macout<true><<<gr, b, 0, s>>>(L, g.u, g.v, g.w, g.t4a, g.flags, g.u2, g.v2, g.w2, kp, open);
+            k_advect_vel_macout<true><<<gr, b, 0, s>>>(L, g.u, g.v, g.w, g.t4a, Q, g.flags, g.u2, g.v2, g.w2, kp,
+                                                       open);
         } else {
-            k_advect_vel_macout<false><<<gr, b, 0, s>>>(L, g.u, g.v, g.w, g.t4a, g.flags, g.u2, g.v2, g.w2, kp, open);
+            int rc = launch_mac_quads(g, s, lc);
+            if (rc) return rc;
+            k_advect_vel_macout<false><<<gr, b, 0, s>>>(L, g.u, g.v, g.w, g.t4a, Q, g.flags, g.u2, g.v2, g.w2, kp,
+                                                        open);
         }
         lc.n++;
         ZQS_LAUNCH_CHECK("k_advect_vel_macout");
@@ -281,21 +337,30 @@ int launch_advect_scalar(const DevGrid& g, const KParams& kp, int mode, bool fol
     const SourceList& sl = src ? *src : none;
     float aT = fold_atten ? kp.temp_atten : 1.0f;
     float aD = fold_atten ? kp.dens_atten : 1.0f;
+    const Quads Q{{g.qu, g.qv, g.qw}};
     if (mode == ZQS_ADV_SCA_MAC) {
-        k_advect_scalar<false><<<gc, b, 0, s>>>(L, g.u, g.v, g.w, g.t4a, g.flags, g.T, g.rho, g.T2, g.rho2, kp, aT,
-                                                aD, sl);
+        int rc = launch_mac_quads(g, s, lc);
+        if (rc) return rc;
+        k_advect_scalar<false><<<gc, b, 0, s>>>(L, g.t4a, Q, g.flags, g.T, g.rho, g.T2, g.rho2, kp, aT, aD, sl);
     } else if (mode == ZQS_ADV_SCA_REG) {
         DevGrid& gm = const_cast<DevGrid&>(g);
         int rc = launch_mac_to_reg4(gm, g.u, g.v, g.w, g.t4a, s, lc);
         if (rc) return rc;
-        k_advect_scalar<true><<<gc, b, 0, s>>>(L, g.u, g.v, g.w, g.t4a, g.flags, g.T, g.rho, g.T2, g.rho2, kp, aT,
-                                               aD, sl);
+        k_advect_scalar<true><<<gc, b, 0, s>>>(L, g.t4a, Q, g.flags, g.T, g.rho, g.T2, g.rho2, kp, aT, aD, sl);
     } else {
         set_error("advect_scalar: mode " + std::to_string(mode) + " (BFECC) is not implemented");
         return ZQS_EUNSUPPORTED;
     }
     lc.n++;
     ZQS_LAUNCH_CHECK("k_advect_scalar");
+    return ZQS_OK;
+}
+
+int launch_mac_quads_batch(const BatchLaunch& face, int vcur, int blocks, cudaStream_t s, LaunchCounter& lc) {
+    dim3 b(32, 8, 1);
+    k_mac_quads_batch<<<std::min(blocks, face.total), b, 0, s>>>(face, vcur);
+    lc.n++;
+    ZQS_LAUNCH_CHECK("k_mac_quads_batch");
     return ZQS_OK;
 }
 

@@ -330,20 +330,29 @@ struct RegShape {
     static constexpr size_t smem = (size_t)NP * 2 * CA * (4 + 4);
 };
 
-// One CTA tile (bx, by) of TX x TY columns and z chunk bz; every thread of the
-// block takes part (barriers inside), and the last step ends with a barrier,
-// so a persistent block may run the next tile on the same shared memory.
+// One CTA tile (bx, by) of TX x TY columns over output planes [z0, z1); every
+// thread of the block takes part (barriers inside), and the last step ends
+// with a barrier, so a persistent block may run the next tile on the same
+// shared memory.  The result of a plane does not depend on how the column's
+// planes are split into ranges (each range recomputes its z halo).
+//
+// WREG (forward): each ring plane's update weights omega/cnt are kept in
+// registers by colour (formed once when the plane arrives) and the x
+// neighbour in the adjacent pair is read at one of two per-thread offsets;
+// without it the flags stay in registers and each half-sweep extracts the
+// stencil count and reads the weight table.  WREG takes ~10 more registers:
+// it suits the one-CTA-per-SM tiles, the plain form the two-CTA ones.
 //
 // ADJ: the reversed SOR of the adjoint in its scaled variable q (see
 // kernels_adjoint.cu): `div` carries wt = omega/cnt (0 where the forward never
 // updates), flags are not read, the half-sweeps run black first, each update
 // is q = (1-omega) q + wt * sum(q_n), and every cell's value before each
 // update is added to acc (read and written in place by the owning thread).
-template <int S, int TX, int TY, int PPT, bool ADJ = false>
+template <int S, int TX, int TY, int PPT, bool ADJ = false, bool WREG = false>
 __device__ __forceinline__ void sor_reg_tile(const Layout& L, const float* __restrict__ pin,
                                              float* __restrict__ pout, const float* __restrict__ div,
-                                             const uint8_t* __restrict__ flags, float omega, float om1, int zc,
-                                             int bx, int by, int bz, float* __restrict__ acc = nullptr) {
+                                             const uint8_t* __restrict__ flags, float omega, float om1, int bx,
+                                             int by, int z0, int z1, float* __restrict__ acc = nullptr) {
     using Sh = RegShape<S, TX, TY, PPT>;
     constexpr int PW = Sh::PW, NP = Sh::NP, CA = Sh::CA, NT = Sh::NT;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -351,8 +360,6 @@ __device__ __forceinline__ void sor_reg_tile(const Layout& L, const float* __res
     float* sd = sp + NP * 2 * CA;                      // [NP][2][CA] divergence
 
     const int x0 = bx * TX, y0 = by * TY;
-    const int z0 = bz * zc;
-    const int z1 = min(z0 + zc, L.D);
     const int plane = (int)L.plane;
     // forward: the update weight omega/cnt by stencil weight (entry 0 unused)
     __shared__ float wtab[8];
@@ -361,7 +368,8 @@ __device__ __forceinline__ void sor_reg_tile(const Layout& L, const float* __res
         __syncthreads();
     }
 
-    int me[PPT], jrow[PPT], gaddr[PPT], bpar[PPT];
+    constexpr bool WR = WREG && !ADJ;
+    int me[PPT], jrow[PPT], gaddr[PPT], bpar[PPT], xoff[PPT][WR ? 2 : 1];
     unsigned amask[PPT], act[PPT][2];
     bool pin_ok[PPT], out_ok[PPT];
 #pragma unroll
@@ -389,6 +397,12 @@ __device__ __forceinline__ void sor_reg_tile(const Layout& L, const float* __res
         // NP) + slot with S and NP even: the left cell is black at slot qs when
         // bpar ^ (qs & 1); act[q][qs & 1] bit s-1: half-sweep s updates this pair
         bpar[q] = (j + z0) & 1;
+        // x neighbour in the adjacent pair: right pair (+1) when the updated
+        // cell is the right one of its pair (o = bpar ^ x = 1), else left (-1)
+        if (WR) {
+            xoff[q][0] = e + (bpar[q] ? 1 : -1);
+            xoff[q][WR ? 1 : 0] = e + (bpar[q] ? -1 : 1);
+        }
 #pragma unroll
         for (int par = 0; par < 2; par++) {
             unsigned a = 0;
@@ -407,17 +421,19 @@ __device__ __forceinline__ void sor_reg_tile(const Layout& L, const float* __res
     const int flo = max(0, z0 - S), fhi = min(L.D, z1 + S);
 
     float P[PPT][NP][2];     // pressure by colour, ring of planes
-    unsigned F[PPT][NP];     // flags by colour: byte c = flags of the colour-c cell
+    float Wc[PPT][WR ? NP : 1][2];   // WREG: omega/cnt by colour (0: never updated)
+    unsigned F[PPT][(ADJ || WR) ? 1 : NP];  // else: flags by colour, byte c = the colour-c cell's
     float A[PPT][ADJ ? NP : 1][2];  // ADJ: acc by colour, ring of planes
     float2 np_[PPT], nd[PPT], na[PPT];
     unsigned nf[PPT];
 #pragma unroll
     for (int q = 0; q < PPT; q++) {
 #pragma unroll
-        for (int a = 0; a < NP; a++) {
-            P[q][a][0] = P[q][a][1] = 0.0f;
-            F[q][a] = 0u;
-        }
+        for (int a = 0; a < NP; a++) P[q][a][0] = P[q][a][1] = 0.0f;
+#pragma unroll
+        for (int a = 0; a < (WR ? NP : 1); a++) Wc[q][a][0] = Wc[q][a][1] = 0.0f;
+#pragma unroll
+        for (int a = 0; a < ((ADJ || WR) ? 1 : NP); a++) F[q][a] = 0u;
 #pragma unroll
         for (int a = 0; a < (ADJ ? NP : 1); a++) A[q][a][0] = A[q][a][1] = 0.0f;
         np_[q] = make_float2(0.0f, 0.0f);
@@ -443,7 +459,14 @@ __device__ __forceinline__ void sor_reg_tile(const Layout& L, const float* __res
                     const bool lc = (bpar[q] ^ (qs & 1)) != 0;  // the left cell is black
                     P[q][qs][0] = lc ? np_[q].y : np_[q].x;
                     P[q][qs][1] = lc ? np_[q].x : np_[q].y;
-                    F[q][qs] = lc ? (((nf[q] & 0xffu) << 8) | (nf[q] >> 8)) : nf[q];
+                    if (WR) {
+                        const float wl = wtab[(nf[q] >> F_CNT_SHIFT) & 7u];
+                        const float wr = wtab[(nf[q] >> (8 + F_CNT_SHIFT)) & 7u];
+                        Wc[q][WR ? qs : 0][0] = lc ? wr : wl;
+                        Wc[q][WR ? qs : 0][1] = lc ? wl : wr;
+                    } else if (!ADJ) {
+                        F[q][ADJ ? 0 : qs] = lc ? (((nf[q] & 0xffu) << 8) | (nf[q] >> 8)) : nf[q];
+                    }
                     if (ADJ) {
                         A[q][ADJ ? qs : 0][0] = lc ? na[q].y : na[q].x;
                         A[q][ADJ ? qs : 0][1] = lc ? na[q].x : na[q].y;
@@ -485,13 +508,33 @@ __device__ __forceinline__ void sor_reg_tile(const Layout& L, const float* __res
                         const int szp = (sz + 1) % NP;
 #pragma unroll
                         for (int q = 0; q < PPT; q++) {
-                            const int o = bpar[q] ^ (qs & 1) ^ c;
-                            const int cnt = ADJ ? 1 : (F[q][sz] >> (8 * c + F_CNT_SHIFT)) & 7;
-                            const float wgt = ADJ ? sd[(sz * 2 + c) * CA + me[q]] : 0.0f;
-                            if (((act[q][qs & 1] >> (s - 1)) & 1u) && cnt && (!ADJ || wgt != 0.0f)) {
+                            // weight: wt from shared memory (ADJ), omega/cnt from registers
+                            // (WREG), else the stencil count from the flags and the table
+                            bool on = ((act[q][qs & 1] >> (s - 1)) & 1u) != 0;
+                            float wgt = 0.0f;
+                            unsigned cnt = 0;
+                            if (ADJ) {
+                                wgt = sd[(sz * 2 + c) * CA + me[q]];
+                                on = on && wgt != 0.0f;
+                            } else if (WR) {
+                                wgt = Wc[q][WR ? sz : 0][c];
+                                on = on && wgt != 0.0f;
+                            } else {
+                                cnt = (F[q][(ADJ || WR) ? 0 : sz] >> (8 * c + F_CNT_SHIFT)) & 7u;
+                                on = on && cnt != 0;
+                            }
+                            if (on) {
                                 const float* Po = sp + (sz * 2 + (c ^ 1)) * CA + me[q];
                                 const float own = P[q][sz][c ^ 1];
-                                const float adj = o ? Po[1] : Po[-1];
+                                // the other x neighbour, in the adjacent pair: right of the pair
+                                // when o = bpar ^ (qs & 1) ^ c is 1, else left
+                                float adj;
+                                if (WR) {
+                                    adj = sp[(sz * 2 + (c ^ 1)) * CA + xoff[q][WR ? ((qs & 1) ^ c) : 0]];
+                                } else {
+                                    const int o = bpar[q] ^ (qs & 1) ^ c;
+                                    adj = o ? Po[1] : Po[-1];
+                                }
                                 const float sum =
                                     ((own + adj) + (Po[-PW] + Po[PW])) + (P[q][szm][c ^ 1] + P[q][szp][c ^ 1]);
                                 float nv;
@@ -500,8 +543,8 @@ __device__ __forceinline__ void sor_reg_tile(const Layout& L, const float* __res
                                     nv = om1 * old + wgt * sum;
                                     A[q][ADJ ? sz : 0][c] += old;
                                 } else {
-                                    nv = sor_update(P[q][sz][c], sum, sd[(sz * 2 + c) * CA + me[q]], wtab[cnt],
-                                                    om1);
+                                    nv = sor_update(P[q][sz][c], sum, sd[(sz * 2 + c) * CA + me[q]],
+                                                    WR ? wgt : wtab[cnt], om1);
                                 }
                                 P[q][sz][c] = nv;
                                 sp[(sz * 2 + c) * CA + me[q]] = nv;
@@ -535,17 +578,19 @@ __device__ __forceinline__ void sor_reg_tile(const Layout& L, const float* __res
     }
 }
 
-template <int S, int TX, int TY, int PPT>
+template <int S, int TX, int TY, int PPT, bool WREG>
 __global__ void __launch_bounds__(RegShape<S, TX, TY, PPT>::NT)
     k_sor_reg(Layout L, const float* __restrict__ pin, float* __restrict__ pout, const float* __restrict__ div,
               const uint8_t* __restrict__ flags, float omega, float om1, int zc) {
-    sor_reg_tile<S, TX, TY, PPT>(L, pin, pout, div, flags, omega, om1, zc, blockIdx.x, blockIdx.y, blockIdx.z);
+    const int z0 = blockIdx.z * zc;
+    sor_reg_tile<S, TX, TY, PPT, false, WREG>(L, pin, pout, div, flags, omega, om1, blockIdx.x, blockIdx.y, z0,
+                                              min(z0 + zc, L.D));
 }
 
 // Persistent batched pass: tile t of the flat SOR tile space belongs to the
 // instance found in the prefix array; pressure goes p[pcur] -> p[pcur^1], z
 // chunk zc[which].
-template <int S, int TX, int TY, int PPT>
+template <int S, int TX, int TY, int PPT, bool WREG>
 __global__ void __launch_bounds__(RegShape<S, TX, TY, PPT>::NT)
     k_sor_reg_batch(BatchLaunch B, int pcur, int which) {
     for (int t = blockIdx.x; t < B.total; t += gridDim.x) {
@@ -555,8 +600,9 @@ __global__ void __launch_bounds__(RegShape<S, TX, TY, PPT>::NT)
         const int tx = (d.L.W + TX - 1) / TX, ty = (d.L.H + TY - 1) / TY;
         const int bx = local % tx, r = local / tx;
         const int by = r % ty, bz = r / ty;
-        sor_reg_tile<S, TX, TY, PPT>(d.L, d.p[pcur], d.p[pcur ^ 1], d.div, d.flags, d.kp.omega, d.kp.om1,
-                                     d.zc[which], bx, by, bz);
+        const int z0 = bz * d.zc[which];
+        sor_reg_tile<S, TX, TY, PPT, false, WREG>(d.L, d.p[pcur], d.p[pcur ^ 1], d.div, d.flags, d.kp.omega,
+                                                  d.kp.om1, bx, by, z0, min(z0 + d.zc[which], d.L.D));
     }
 }
 
@@ -565,8 +611,9 @@ template <int S, int TX, int TY, int PPT>
 __global__ void __launch_bounds__(RegShape<S, TX, TY, PPT>::NT)
     k_sor_reg_adj(Layout L, const float* __restrict__ qin, float* __restrict__ qout, const float* __restrict__ wt,
                   float* __restrict__ acc, float om1, int zc) {
-    sor_reg_tile<S, TX, TY, PPT, true>(L, qin, qout, wt, nullptr, 0.0f, om1, zc, blockIdx.x, blockIdx.y,
-                                       blockIdx.z, acc);
+    const int z0 = blockIdx.z * zc;
+    sor_reg_tile<S, TX, TY, PPT, true>(L, qin, qout, wt, nullptr, 0.0f, om1, blockIdx.x, blockIdx.y, z0,
+                                       min(z0 + zc, L.D), acc);
 }
 
 // u -= p_R - p_L on live faces; OPEN also updates domain faces with p = 0 outside.
@@ -759,6 +806,8 @@ struct RbVariant {
                               cudaStream_t);
     const void* fn_adj;
     int ctas_per_sm_adj;
+    int wreg;       // update weights in registers (k_sor_reg WREG form)
+    int regs;       // registers per thread of fn
 };
 
 template <int S, int TX, int TY, int PPT>
@@ -787,22 +836,24 @@ RbVariant rb_variant() {
     v.launch_batch = nullptr;
     v.fn_batch = nullptr;
     v.ctas_per_sm_batch = 0;
+    v.wreg = 0;
+    v.regs = 0;
     v.fn = (const void*)k_sor_rb<S, TX, TY, PPT>;
     return v;
 }
 
-template <int S, int TX, int TY, int PPT>
+template <int S, int TX, int TY, int PPT, bool WREG>
 cudaError_t reg_launch(dim3 gr, const Layout& L, const float* pin, float* pout, const float* div,
                        const uint8_t* flags, float omega, float om1, int zc, cudaStream_t st) {
     using Sh = RegShape<S, TX, TY, PPT>;
-    k_sor_reg<S, TX, TY, PPT><<<gr, Sh::NT, Sh::smem, st>>>(L, pin, pout, div, flags, omega, om1, zc);
+    k_sor_reg<S, TX, TY, PPT, WREG><<<gr, Sh::NT, Sh::smem, st>>>(L, pin, pout, div, flags, omega, om1, zc);
     return cudaGetLastError();
 }
 
-template <int S, int TX, int TY, int PPT>
+template <int S, int TX, int TY, int PPT, bool WREG>
 cudaError_t reg_launch_batch(int blocks, const BatchLaunch& B, int pcur, int which, cudaStream_t st) {
     using Sh = RegShape<S, TX, TY, PPT>;
-    k_sor_reg_batch<S, TX, TY, PPT><<<blocks, Sh::NT, Sh::smem, st>>>(B, pcur, which);
+    k_sor_reg_batch<S, TX, TY, PPT, WREG><<<blocks, Sh::NT, Sh::smem, st>>>(B, pcur, which);
     return cudaGetLastError();
 }
 
@@ -814,7 +865,7 @@ cudaError_t reg_launch_adj(dim3 gr, const Layout& L, const float* qin, float* qo
     return cudaGetLastError();
 }
 
-template <int S, int TX, int TY, int PPT>
+template <int S, int TX, int TY, int PPT, bool WREG = false>
 RbVariant reg_variant() {
     using Sh = RegShape<S, TX, TY, PPT>;
     RbVariant v;
@@ -825,10 +876,12 @@ RbVariant reg_variant() {
     v.nt = Sh::NT;
     v.smem = Sh::smem;
     v.ctas_per_sm = 0;
-    v.launch = &reg_launch<S, TX, TY, PPT>;
-    v.fn = (const void*)k_sor_reg<S, TX, TY, PPT>;
-    v.launch_batch = &reg_launch_batch<S, TX, TY, PPT>;
-    v.fn_batch = (const void*)k_sor_reg_batch<S, TX, TY, PPT>;
+    v.launch = &reg_launch<S, TX, TY, PPT, WREG>;
+    v.fn = (const void*)k_sor_reg<S, TX, TY, PPT, WREG>;
+    v.launch_batch = &reg_launch_batch<S, TX, TY, PPT, WREG>;
+    v.fn_batch = (const void*)k_sor_reg_batch<S, TX, TY, PPT, WREG>;
+    v.wreg = WREG ? 1 : 0;
+    v.regs = 0;
     v.ctas_per_sm_batch = 0;
     v.launch_adj = &reg_launch_adj<S, TX, TY, PPT>;
     v.fn_adj = (const void*)k_sor_reg_adj<S, TX, TY, PPT>;
@@ -838,15 +891,18 @@ RbVariant reg_variant() {
 
 // The registry of fused SOR variants (temporal depth S/2, tile, pairs per thread);
 // 0-9 keep every plane in shared memory (k_sor_rb), 10-17 keep the thread's own
-// column in registers (k_sor_reg).
-constexpr int kNumVariants = 18;
+// column in registers (k_sor_reg), 18-20 also the update weights (WREG).
+constexpr int kNumVariants = 21;
 RbVariant g_var[kNumVariants];
 // default variant per depth 1..4
-// (measured at 256^3 on GB300: register-column 32x32 at depth 2 is fastest,
-// 54.5 us per iteration; depth 1: register-column 64x16, 62.6 us)
-const int kDefaultVariant[5] = {-1, 11, 14, 15, 7};
-// batched default: register-column 32x16 at depth 2 (small tiles suit 32..128 edges)
-const int kBatchDefaultVariant = 12;
+// (measured at 256^3 on GB300: register-column 32x32 at depth 2 with the
+// weights in registers is fastest, 51.2 us per iteration; depth 1:
+// register-column 64x16 at two CTAs per SM, 61.7 us)
+const int kDefaultVariant[5] = {-1, 11, 18, 20, 7};
+// batched default: register-column 32x32 at depth 2 with the weights in
+// registers (measured on the 64-instance mixed batch: 75.2 ms per step against
+// 79.1 ms for 32x16 tiles at two CTAs per SM)
+const int kBatchDefaultVariant = 18;
 // reversed SOR of the adjoint: register-column variants in order of preference
 const int kAdjVariants[] = {13, 12, 11, 10};
 int g_num_sms = 0;
@@ -871,6 +927,15 @@ int choose_zc(const Layout& L, const RbVariant& v) {
     return best;
 }
 
+// One fused pass on the uniform grid of tiles x z chunks (zc_forced 0: the
+// chunk from choose_zc).
+cudaError_t launch_pass(const RbVariant& v, const Layout& L, const float* pin, float* pout, const float* div,
+                        const uint8_t* flags, float omega, float om1, int zc_forced, cudaStream_t s) {
+    const int zc = zc_forced > 0 ? std::min(zc_forced, L.D) : choose_zc(L, v);
+    dim3 gr((L.W + v.TX - 1) / v.TX, (L.H + v.TY - 1) / v.TY, (L.D + zc - 1) / zc);
+    return v.launch(gr, L, pin, pout, div, flags, omega, om1, zc, s);
+}
+
 }  // namespace
 
 int sor_prepare() {
@@ -893,6 +958,9 @@ int sor_prepare() {
     g_var[15] = reg_variant<6, 32, 16, 1>();
     g_var[16] = reg_variant<2, 32, 16, 2>();
     g_var[17] = reg_variant<4, 32, 16, 2>();
+    g_var[18] = reg_variant<4, 32, 32, 1, true>();
+    g_var[19] = reg_variant<4, 64, 16, 1, true>();
+    g_var[20] = reg_variant<6, 32, 16, 1, true>();
     int dev = 0;
     ZQS_CUDA_TRY(cudaGetDevice(&dev));
     ZQS_CUDA_TRY(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
@@ -902,6 +970,9 @@ int sor_prepare() {
         int n = 0;
         ZQS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, v.fn, v.nt, v.smem));
         v.ctas_per_sm = n;  // 0: does not fit (never selected)
+        cudaFuncAttributes fa;
+        ZQS_CUDA_TRY(cudaFuncGetAttributes(&fa, v.fn));
+        v.regs = fa.numRegs;
         if (v.fn_batch) {
             ZQS_CUDA_TRY(
                 cudaFuncSetAttribute(v.fn_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)v.smem));
@@ -937,6 +1008,8 @@ int sor_variant_info(int i, zqs_sor_variant* out) {
     out->threads = v.nt;
     out->ctas_per_sm = v.ctas_per_sm;
     out->smem_bytes = (int64_t)v.smem;
+    out->weights_in_registers = v.wreg;
+    out->registers = v.regs;
     return ZQS_OK;
 }
 
@@ -983,9 +1056,8 @@ int launch_project(DevGrid& g, const KParams& kp, int K, const SorConfig& cfg, c
         while (remaining > 0) {
             const int d = std::min(dmain, remaining);
             const RbVariant& v = (d == dmain) ? g_var[vmain] : g_var[kDefaultVariant[d]];
-            const int zc = (d == dmain && cfg.zchunk > 0) ? std::min(cfg.zchunk, L.D) : choose_zc(L, v);
-            dim3 gr((L.W + v.TX - 1) / v.TX, (L.H + v.TY - 1) / v.TY, (L.D + zc - 1) / zc);
-            cudaError_t e = v.launch(gr, L, cur, nxt, g.div, g.flags, kp.omega, kp.om1, zc, s);
+            cudaError_t e =
+                launch_pass(v, L, cur, nxt, g.div, g.flags, kp.omega, kp.om1, d == dmain ? cfg.zchunk : 0, s);
             if (e != cudaSuccess) return cuda_fail(e, "k_sor_rb");
             lc.n++;
             std::swap(cur, nxt);

@@ -22,6 +22,7 @@ struct InstDesc {
     uint8_t* flags;
     float4* t4a;
     float4* t4b;
+    float4* q4[3];      // quad copies of the current velocity (MAC sampler)
     double* red;
     long long red_len;
     KParams kp;
@@ -68,6 +69,7 @@ bool sor_variant_batchable(int variant);
 
 int launch_force_batch(const BatchLaunch& cell, const BatchLaunch& face, int vcur, int scur, int blocks,
                        cudaStream_t s, LaunchCounter& lc);
+int launch_mac_quads_batch(const BatchLaunch& face, int vcur, int blocks, cudaStream_t s, LaunchCounter& lc);
 int launch_advect_velocity_batch(const BatchLaunch& advf, int vcur, int blocks, cudaStream_t s, LaunchCounter& lc);
 int launch_advect_scalar_batch(const BatchLaunch& cell, int vcur, int scur, int blocks, cudaStream_t s,
                                LaunchCounter& lc);

@@ -79,6 +79,7 @@ struct DevGrid {
     float *div;                // projection right-hand side
     uint8_t* flags;
     float4 *t4a, *t4b;         // float4 temporaries (vorticity/force or centre velocity)
+    float4 *qu, *qv, *qw;      // quad copies of the velocity for the MAC sampler (tri0_quad)
     double* red;               // FP64 reduction scratch (the closed-solver mean sits in the last 2)
     long long red_len;
 };

@@ -141,13 +141,43 @@ __device__ __forceinline__ float tri0_sample(const float* __restrict__ f, const 
     return lerpf(lerpf(c00, c10, c.ty), lerpf(c01, c11, c.ty), c.tz);
 }
 
-struct MacVel {
+// Quad copy of a face component for the forward sampler:
+//   Q[r] = (f[r], f[r + plane], f[r + 1], f[r + plane + 1])
+// so the eight corners of tri0_sample at base r are the two 16-byte loads
+// Q[r] and Q[r + px]; the interpolation tree is tri0_sample's.  Q is built for
+// every face index (i <= W, j <= H, k <= D) and zero elsewhere; Q[r + px] at
+// j = H lies in the next plane's first row, or in the zero tail after the
+// last face plane, and enters only with weight ty = 0.
+__device__ __forceinline__ float tri0_quad(const float4* __restrict__ q, const Layout& L, const Tri0& c) {
+    const float4 a = __ldg(q + c.r);
+    const float4 b = __ldg(q + c.r + L.px);
+    const float c00 = lerpf(a.x, a.z, c.tx);
+    const float c10 = lerpf(b.x, b.z, c.tx);
+    const float c01 = lerpf(a.y, a.w, c.tx);
+    const float c11 = lerpf(b.y, b.w, c.tx);
+    return lerpf(lerpf(c00, c10, c.ty), lerpf(c01, c11, c.ty), c.tz);
+}
+
+// Corner fetch policies of the MAC sampler: the field itself, or its quads.
+struct FieldTri {
+    const float* f;
+    __device__ __forceinline__ float operator()(const Layout& L, const Tri0& c) const {
+        return tri0_sample(f, L, c);
+    }
+};
+struct QuadTri {
+    const float4* q;
+    __device__ __forceinline__ float operator()(const Layout& L, const Tri0& c) const { return tri0_quad(q, L, c); }
+};
+
+template <class Tri>
+struct MacVelT {
     Layout L;
-    const float *u, *v, *w;
+    Tri u, v, w;
     __device__ __forceinline__ void operator()(float px, float py, float pz, float& vx, float& vy, float& vz) const {
-        vx = tri0_sample(u, L, tri0(L, L.W + 1, L.H, L.D, px, py - 0.5f, pz - 0.5f));
-        vy = tri0_sample(v, L, tri0(L, L.W, L.H + 1, L.D, px - 0.5f, py, pz - 0.5f));
-        vz = tri0_sample(w, L, tri0(L, L.W, L.H, L.D + 1, px - 0.5f, py - 0.5f, pz));
+        vx = u(L, tri0(L, L.W + 1, L.H, L.D, px, py - 0.5f, pz - 0.5f));
+        vy = v(L, tri0(L, L.W, L.H + 1, L.D, px - 0.5f, py, pz - 0.5f));
+        vz = w(L, tri0(L, L.W, L.H, L.D + 1, px - 0.5f, py - 0.5f, pz));
     }
     // Also returns the cell containing the point when it lies in the domain:
     // the u grid's x corner floor(clamp(x, 0, W)), the v grid's y and the w
@@ -171,14 +201,16 @@ struct MacVel {
         cw.tx = xc.t;
         cw.ty = yc.t;
         cw.tz = zw.t;
-        vx = tri0_sample(u, L, cu);
-        vy = tri0_sample(v, L, cv);
-        vz = tri0_sample(w, L, cw);
+        vx = u(L, cu);
+        vy = v(L, cv);
+        vz = w(L, cw);
         ci = min(xu.i0, L.W - 1);
         cj = min(yv.i0, L.H - 1);
         ck = min(zw.i0, L.D - 1);
     }
 };
+using MacVel = MacVelT<FieldTri>;   // corners from the fields
+using MacVelQ = MacVelT<QuadTri>;   // corners from the quad copies
 struct RegVel {
     Layout L;
     const float4* vel4;
@@ -244,8 +276,10 @@ __device__ __forceinline__ void backtrace(const Layout& L, const uint8_t* __rest
 
 // backtrace() for the MAC sampler: the occupancy test reuses the cell index
 // that the velocity sample at the same point already floored.
-__device__ __forceinline__ void backtrace(const Layout& L, const uint8_t* __restrict__ flags, const MacVel& vel,
-                                          const KParams& kp, float& px, float& py, float& pz) {
+template <class Tri>
+__device__ __forceinline__ void backtrace(const Layout& L, const uint8_t* __restrict__ flags,
+                                          const MacVelT<Tri>& vel, const KParams& kp, float& px, float& py,
+                                          float& pz) {
     float vx, vy, vz;
     int ci, cj, ck;
     vel(px, py, pz, vx, vy, vz, ci, cj, ck);
