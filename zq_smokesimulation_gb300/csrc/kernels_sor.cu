@@ -327,7 +327,11 @@ struct RegShape {
     static constexpr int CA = PW * RH;
     static constexpr int NT = CA / PPT;
     static constexpr int NP = 2 * S + 2;
-    static constexpr size_t smem = (size_t)NP * 2 * CA * (4 + 4);
+    // floats ahead of the pressure ring: the branch-free half-sweep of the
+    // WREG form reads its neighbours before it knows whether the pair updates,
+    // and the row -1 / x -1 neighbours of the first slot fall here
+    static constexpr int GUARD = (PW + 1 + 3) / 4 * 4;
+    static constexpr size_t smem = (size_t)NP * 2 * CA * (4 + 4) + (size_t)GUARD * 4;
 };
 
 // One CTA tile (bx, by) of TX x TY columns over output planes [z0, z1); every
@@ -356,8 +360,8 @@ __device__ __forceinline__ void sor_reg_tile(const Layout& L, const float* __res
     using Sh = RegShape<S, TX, TY, PPT>;
     constexpr int PW = Sh::PW, NP = Sh::NP, CA = Sh::CA, NT = Sh::NT;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    float* sp = reinterpret_cast<float*>(smem_raw);  // [NP][2][CA] published pressure
-    float* sd = sp + NP * 2 * CA;                      // [NP][2][CA] divergence
+    float* sp = reinterpret_cast<float*>(smem_raw) + Sh::GUARD;  // [NP][2][CA] published pressure
+    float* sd = sp + NP * 2 * CA;                                  // [NP][2][CA] divergence
 
     const int x0 = bx * TX, y0 = by * TY;
     const int plane = (int)L.plane;
@@ -523,18 +527,27 @@ __device__ __forceinline__ void sor_reg_tile(const Layout& L, const float* __res
                                 cnt = (F[q][(ADJ || WR) ? 0 : sz] >> (8 * c + F_CNT_SHIFT)) & 7u;
                                 on = on && cnt != 0;
                             }
-                            if (on) {
+                            if (WR) {
+                                // branch-free: every pair forms the update and keeps its old
+                                // value where the half-sweep leaves it (outside the active
+                                // ring, obstacles, the domain edge); the x neighbour in the
+                                // adjacent pair is right of the pair when bpar ^ (qs & 1) ^ c
+                                const float* Po = sp + (sz * 2 + (c ^ 1)) * CA + me[q];
+                                const float adj = sp[(sz * 2 + (c ^ 1)) * CA + xoff[q][WR ? ((qs & 1) ^ c) : 0]];
+                                const float sum = ((P[q][sz][c ^ 1] + adj) + (Po[-PW] + Po[PW])) +
+                                                  (P[q][szm][c ^ 1] + P[q][szp][c ^ 1]);
+                                const float old = P[q][sz][c];
+                                const float nv = sor_update(old, sum, sd[(sz * 2 + c) * CA + me[q]], wgt, om1);
+                                const float res = on ? nv : old;
+                                P[q][sz][c] = res;
+                                sp[(sz * 2 + c) * CA + me[q]] = res;
+                            } else if (on) {
                                 const float* Po = sp + (sz * 2 + (c ^ 1)) * CA + me[q];
                                 const float own = P[q][sz][c ^ 1];
                                 // the other x neighbour, in the adjacent pair: right of the pair
                                 // when o = bpar ^ (qs & 1) ^ c is 1, else left
-                                float adj;
-                                if (WR) {
-                                    adj = sp[(sz * 2 + (c ^ 1)) * CA + xoff[q][WR ? ((qs & 1) ^ c) : 0]];
-                                } else {
-                                    const int o = bpar[q] ^ (qs & 1) ^ c;
-                                    adj = o ? Po[1] : Po[-1];
-                                }
+                                const int o = bpar[q] ^ (qs & 1) ^ c;
+                                const float adj = o ? Po[1] : Po[-1];
                                 const float sum =
                                     ((own + adj) + (Po[-PW] + Po[PW])) + (P[q][szm][c ^ 1] + P[q][szp][c ^ 1]);
                                 float nv;
@@ -543,8 +556,8 @@ __device__ __forceinline__ void sor_reg_tile(const Layout& L, const float* __res
                                     nv = om1 * old + wgt * sum;
                                     A[q][ADJ ? sz : 0][c] += old;
                                 } else {
-                                    nv = sor_update(P[q][sz][c], sum, sd[(sz * 2 + c) * CA + me[q]],
-                                                    WR ? wgt : wtab[cnt], om1);
+                                    nv = sor_update(P[q][sz][c], sum, sd[(sz * 2 + c) * CA + me[q]], wtab[cnt],
+                                                    om1);
                                 }
                                 P[q][sz][c] = nv;
                                 sp[(sz * 2 + c) * CA + me[q]] = nv;
