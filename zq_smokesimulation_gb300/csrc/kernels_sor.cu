@@ -585,10 +585,18 @@ __device__ __forceinline__ void sor_reg_tile(const Layout& L, const float* __res
                         }
                     }
                 }
-                __syncthreads();
+                // One barrier per two steps.  Shared data written at step t is first
+                // read at step t+2 (half-sweep s reads, on plane t+2-2s, the colour
+                // half-sweep s-1 wrote there at step t; half-sweep 1 reads the plane
+                // published at step t), and a slot's old content was last read at
+                // step t-2 (the slot published at step t held plane t-NP, last read
+                // by half-sweep S at step t-2).  A barrier after every odd ring slot
+                // (NP is even) separates every such pair of steps.
+                if (qs & 1) __syncthreads();
             }
         }
     }
+    __syncthreads();
 }
 
 template <int S, int TX, int TY, int PPT, bool WREG>
