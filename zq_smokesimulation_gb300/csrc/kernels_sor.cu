@@ -513,10 +513,13 @@ __device__ __forceinline__ void sor_reg_tile(const Layout& L, const float* __res
 #pragma unroll
                         for (int q = 0; q < PPT; q++) {
                             // weight: wt from shared memory (ADJ), omega/cnt from registers
-                            // (WREG), else the stencil count from the flags and the table
+                            // (WREG), else the stencil count from the flags and the table.
+                            // Branch-free: every pair forms the update and keeps its old
+                            // value where the half-sweep leaves it (outside the active ring,
+                            // obstacles, the domain edge), so the independent half-sweeps of
+                            // a step interleave.
                             bool on = ((act[q][qs & 1] >> (s - 1)) & 1u) != 0;
-                            float wgt = 0.0f;
-                            unsigned cnt = 0;
+                            float wgt;
                             if (ADJ) {
                                 wgt = sd[(sz * 2 + c) * CA + me[q]];
                                 on = on && wgt != 0.0f;
@@ -524,44 +527,34 @@ __device__ __forceinline__ void sor_reg_tile(const Layout& L, const float* __res
                                 wgt = Wc[q][WR ? sz : 0][c];
                                 on = on && wgt != 0.0f;
                             } else {
-                                cnt = (F[q][(ADJ || WR) ? 0 : sz] >> (8 * c + F_CNT_SHIFT)) & 7u;
+                                const unsigned cnt = (F[q][(ADJ || WR) ? 0 : sz] >> (8 * c + F_CNT_SHIFT)) & 7u;
                                 on = on && cnt != 0;
+                                wgt = wtab[cnt];
                             }
+                            const float* Po = sp + (sz * 2 + (c ^ 1)) * CA + me[q];
+                            // the x neighbour in the adjacent pair: right of the pair when
+                            // bpar ^ (qs & 1) ^ c is 1, else left
+                            float adj;
                             if (WR) {
-                                // branch-free: every pair forms the update and keeps its old
-                                // value where the half-sweep leaves it (outside the active
-                                // ring, obstacles, the domain edge); the x neighbour in the
-                                // adjacent pair is right of the pair when bpar ^ (qs & 1) ^ c
-                                const float* Po = sp + (sz * 2 + (c ^ 1)) * CA + me[q];
-                                const float adj = sp[(sz * 2 + (c ^ 1)) * CA + xoff[q][WR ? ((qs & 1) ^ c) : 0]];
-                                const float sum = ((P[q][sz][c ^ 1] + adj) + (Po[-PW] + Po[PW])) +
-                                                  (P[q][szm][c ^ 1] + P[q][szp][c ^ 1]);
-                                const float old = P[q][sz][c];
-                                const float nv = sor_update(old, sum, sd[(sz * 2 + c) * CA + me[q]], wgt, om1);
-                                const float res = on ? nv : old;
-                                P[q][sz][c] = res;
-                                sp[(sz * 2 + c) * CA + me[q]] = res;
-                            } else if (on) {
-                                const float* Po = sp + (sz * 2 + (c ^ 1)) * CA + me[q];
-                                const float own = P[q][sz][c ^ 1];
-                                // the other x neighbour, in the adjacent pair: right of the pair
-                                // when o = bpar ^ (qs & 1) ^ c is 1, else left
+                                adj = sp[(sz * 2 + (c ^ 1)) * CA + xoff[q][WR ? ((qs & 1) ^ c) : 0]];
+                            } else {
                                 const int o = bpar[q] ^ (qs & 1) ^ c;
-                                const float adj = o ? Po[1] : Po[-1];
-                                const float sum =
-                                    ((own + adj) + (Po[-PW] + Po[PW])) + (P[q][szm][c ^ 1] + P[q][szp][c ^ 1]);
-                                float nv;
-                                if (ADJ) {
-                                    const float old = P[q][sz][c];
-                                    nv = om1 * old + wgt * sum;
-                                    A[q][ADJ ? sz : 0][c] += old;
-                                } else {
-                                    nv = sor_update(P[q][sz][c], sum, sd[(sz * 2 + c) * CA + me[q]], wtab[cnt],
-                                                    om1);
-                                }
-                                P[q][sz][c] = nv;
-                                sp[(sz * 2 + c) * CA + me[q]] = nv;
+                                adj = Po[o ? 1 : -1];
                             }
+                            const float sum = ((P[q][sz][c ^ 1] + adj) + (Po[-PW] + Po[PW])) +
+                                              (P[q][szm][c ^ 1] + P[q][szp][c ^ 1]);
+                            const float old = P[q][sz][c];
+                            float nv;
+                            if (ADJ) {
+                                nv = om1 * old + wgt * sum;
+                                const float a0 = A[q][ADJ ? sz : 0][c];
+                                A[q][ADJ ? sz : 0][c] = on ? a0 + old : a0;
+                            } else {
+                                nv = sor_update(old, sum, sd[(sz * 2 + c) * CA + me[q]], wgt, om1);
+                            }
+                            const float res = on ? nv : old;
+                            P[q][sz][c] = res;
+                            sp[(sz * 2 + c) * CA + me[q]] = res;
                         }
                     }
                 }
