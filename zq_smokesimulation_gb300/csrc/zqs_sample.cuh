@@ -148,14 +148,41 @@ __device__ __forceinline__ float tri0_sample(const float* __restrict__ f, const 
 // every face index (i <= W, j <= H, k <= D) and zero elsewhere; Q[r + px] at
 // j = H lies in the next plane's first row, or in the zero tail after the
 // last face plane, and enters only with weight ty = 0.
+//
+// The x and y steps pair two interpolations each on the Blackwell FP32x2
+// instructions: the differences and the products are packed (sub/mul
+// .rn.f32x2), the final sums stay scalar (__fadd_rn).  A packed multiply
+// followed by a packed add is contracted into a packed fma by the assembler,
+// which would round once instead of twice; scalar adds of the product's
+// halves are not, so every value is the separately rounded a + t*(b - a) of
+// lerpf, bit for bit.
+__device__ __forceinline__ unsigned long long pack2(float a, float b) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ float2 unpack2(unsigned long long r) {
+    float2 a;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a.x), "=f"(a.y) : "l"(r));
+    return a;
+}
+// (t0 * (b0 - a0), t1 * (b1 - a1)), each rounded once per operation
+__device__ __forceinline__ float2 lerp_step2(float a0, float a1, float b0, float b1, float t0, float t1) {
+    unsigned long long d, m;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pack2(b0, b1)), "l"(pack2(a0, a1)));
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(m) : "l"(pack2(t0, t1)), "l"(d));
+    return unpack2(m);
+}
 __device__ __forceinline__ float tri0_quad(const float4* __restrict__ q, const Layout& L, const Tri0& c) {
     const float4 a = __ldg(q + c.r);
     const float4 b = __ldg(q + c.r + L.px);
-    const float c00 = lerpf(a.x, a.z, c.tx);
-    const float c10 = lerpf(b.x, b.z, c.tx);
-    const float c01 = lerpf(a.y, a.w, c.tx);
-    const float c11 = lerpf(b.y, b.w, c.tx);
-    return lerpf(lerpf(c00, c10, c.ty), lerpf(c01, c11, c.ty), c.tz);
+    const float2 ma = lerp_step2(a.x, a.y, a.z, a.w, c.tx, c.tx);
+    const float2 mb = lerp_step2(b.x, b.y, b.z, b.w, c.tx, c.tx);
+    const float c00 = __fadd_rn(a.x, ma.x), c01 = __fadd_rn(a.y, ma.y);  // lerpf(a.x, a.z), lerpf(a.y, a.w)
+    const float c10 = __fadd_rn(b.x, mb.x), c11 = __fadd_rn(b.y, mb.y);  // lerpf(b.x, b.z), lerpf(b.y, b.w)
+    const float2 my = lerp_step2(c00, c01, c10, c11, c.ty, c.ty);
+    const float c0 = __fadd_rn(c00, my.x), c1 = __fadd_rn(c01, my.y);  // lerpf(c00, c10), lerpf(c01, c11)
+    return lerpf(c0, c1, c.tz);
 }
 
 // Corner fetch policies of the MAC sampler: the field itself, or its quads.
