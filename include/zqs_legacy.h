@@ -10,9 +10,11 @@
  *   - no per-call cudaMalloc: device buffers are cached per grid size;
  *   - CUDA errors do not exit the process: the shim returns a negative value
  *     (-zqs_status) and zqs_last_error() has the message;
- *   - BFECC modes, which this build does not implement yet, return
- *     -ZQS_EUNSUPPORTED and leave every array untouched (the reference's
- *     Advect_Scalar silently returns zeros for them, Adv3D:1786-1794).
+ *   - Advect_Scalar with a BFECC type runs the three BFECC passes of the
+ *     reference's cu_Advect_Scalar_*_BFECC (Adv3D:1507-1554, 1586-1648); the
+ *     reference's entry point never calls them and returns zeros for those
+ *     types (Adv3D:1786-1794).  Advect_Velocity runs all six types as the
+ *     reference does; an unknown type returns -ZQS_EINVAL, arrays untouched.
  * Not re-entrant: ZQ_Cuda_Prepare_Advection sets process-wide state exactly
  * like the reference (ZQ_CUDA_Advection3D.cu:1652-1668).
  */

@@ -13,9 +13,9 @@
  *
  * Differences, kept as parameters or documented: the projection is always the
  * fine-grid red-black SOR (the coarse, octree and flux solvers of the reference
- * map to the SOR of the same open/closed kind, with a notice); BFECC
- * advection, moving objects, guiding control and the wavelet / compressed
- * export formats are not available (Init or the export returns false). */
+ * map to the SOR of the same open/closed kind, with a notice); moving objects,
+ * guiding control and the wavelet / compressed export formats are not
+ * available (Init or the export returns false). */
 #ifndef ZQS_SMOKE3D_H
 #define ZQS_SMOKE3D_H
 

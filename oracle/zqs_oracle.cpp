@@ -344,26 +344,40 @@ void attenuate(const Dims& d, R* u, R* v, R* w, R* T, R* rho, const uint8_t* occ
 /* Velocity samplers.  MAC: u texel (i,j,k) sits at (i, j+.5, k+.5), so the
  * texel-index coordinate of a point p is (p.x, p.y-.5, p.z-.5); v and w
  * likewise (ZQ_CUDA_Advection3D.cu:244-246 normalised by W+1 etc.).
- * Regular: the float4 centre field sits at (i+.5, j+.5, k+.5). */
+ * Regular: the float4 centre field sits at (i+.5, j+.5, k+.5).
+ * sg = -1 samples the negated field (the BFECC backward pass negates the
+ * velocity arrays in place, Adv3D:1284, and negation is exact). */
 template <class R> struct MacSampler {
     Dims d;
     const R *u, *v, *w;
+    R sg = R(1);
     void operator()(R px, R py, R pz, R& vx, R& vy, R& vz) const {
         const R hf = R(0.5);
         vx = trilinear<R>(u, d.W + 1, d.H, d.D, 1, 0, px, py - hf, pz - hf);
         vy = trilinear<R>(v, d.W, d.H + 1, d.D, 1, 0, px - hf, py, pz - hf);
         vz = trilinear<R>(w, d.W, d.H, d.D + 1, 1, 0, px - hf, py - hf, pz);
+        if (sg < R(0)) {
+            vx = -vx;
+            vy = -vy;
+            vz = -vz;
+        }
     }
 };
 template <class R> struct RegSampler {
     Dims d;
     const R* vel4;
+    R sg = R(1);
     void operator()(R px, R py, R pz, R& vx, R& vy, R& vz) const {
         const R hf = R(0.5);
         R gx = px - hf, gy = py - hf, gz = pz - hf;
         vx = trilinear<R>(vel4, d.W, d.H, d.D, 4, 0, gx, gy, gz);
         vy = trilinear<R>(vel4, d.W, d.H, d.D, 4, 1, gx, gy, gz);
         vz = trilinear<R>(vel4, d.W, d.H, d.D, 4, 2, gx, gy, gz);
+        if (sg < R(0)) {
+            vx = -vx;
+            vy = -vy;
+            vz = -vz;
+        }
     }
 };
 
@@ -429,82 +443,158 @@ template <class R> static AdvCtx<R> adv_ctx(const zqs_params& P) {
     return c;
 }
 
-/* Advect_Velocity (ZQ_CUDA_Advection3D.cu:1686-1749) for the three non-BFECC
- * modes; the write-back follows cu_Apply_Advect_Velocity_Result_{Open,Closed}. */
+/* One pass of Advect_Velocity_inMAC_outMAC_{u,v,w}_Kernel (Adv3D:232-377):
+ * every face backtraces through the MAC velocity `vel` and samples the MAC
+ * input (iu, iv, iw) at the end point; no write-back. */
+template <class R>
+void mac_pass(const Dims& d, const uint8_t* occ, const AdvCtx<R>& a, const MacSampler<R>& s, const R* iu,
+              const R* iv, const R* iw, R* ou, R* ov, R* ow) {
+    const R hf = R(0.5);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int k = 0; k <= d.D; k++)
+        for (int j = 0; j <= d.H; j++)
+            for (int i = 0; i <= d.W; i++) {
+                if (j < d.H && k < d.D) {
+                    R px = (R)i, py = (R)j + hf, pz = (R)k + hf;
+                    backtrace(d, occ, s, a.steps, a.dt, a.h, a.full, px, py, pz);
+                    ou[d.uix(i, j, k)] = trilinear<R>(iu, d.W + 1, d.H, d.D, 1, 0, px, py - hf, pz - hf);
+                }
+                if (i < d.W && k < d.D) {
+                    R px = (R)i + hf, py = (R)j, pz = (R)k + hf;
+                    backtrace(d, occ, s, a.steps, a.dt, a.h, a.full, px, py, pz);
+                    ov[d.vix(i, j, k)] = trilinear<R>(iv, d.W, d.H + 1, d.D, 1, 0, px - hf, py, pz - hf);
+                }
+                if (i < d.W && j < d.H) {
+                    R px = (R)i + hf, py = (R)j + hf, pz = (R)k;
+                    backtrace(d, occ, s, a.steps, a.dt, a.h, a.full, px, py, pz);
+                    ow[d.wix(i, j, k)] = trilinear<R>(iw, d.W, d.H, d.D + 1, 1, 0, px - hf, py - hf, pz);
+                }
+            }
+}
+
+/* One pass of Advect_Velocity_inRegular_outMAC_{u,v,w}_Kernel (Adv3D:115-230):
+ * faces backtrace through the regular velocity and sample channel q of the
+ * regular input in4 at the end point. */
+template <class R>
+void regmac_pass(const Dims& d, const uint8_t* occ, const AdvCtx<R>& a, const RegSampler<R>& s, const R* in4,
+                 R* ou, R* ov, R* ow) {
+    const R hf = R(0.5);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int k = 0; k <= d.D; k++)
+        for (int j = 0; j <= d.H; j++)
+            for (int i = 0; i <= d.W; i++) {
+                if (j < d.H && k < d.D) {
+                    R px = (R)i, py = (R)j + hf, pz = (R)k + hf;
+                    backtrace(d, occ, s, a.steps, a.dt, a.h, a.full, px, py, pz);
+                    ou[d.uix(i, j, k)] = trilinear<R>(in4, d.W, d.H, d.D, 4, 0, px - hf, py - hf, pz - hf);
+                }
+                if (i < d.W && k < d.D) {
+                    R px = (R)i + hf, py = (R)j, pz = (R)k + hf;
+                    backtrace(d, occ, s, a.steps, a.dt, a.h, a.full, px, py, pz);
+                    ov[d.vix(i, j, k)] = trilinear<R>(in4, d.W, d.H, d.D, 4, 1, px - hf, py - hf, pz - hf);
+                }
+                if (i < d.W && j < d.H) {
+                    R px = (R)i + hf, py = (R)j + hf, pz = (R)k;
+                    backtrace(d, occ, s, a.steps, a.dt, a.h, a.full, px, py, pz);
+                    ow[d.wix(i, j, k)] = trilinear<R>(in4, d.W, d.H, d.D, 4, 2, px - hf, py - hf, pz - hf);
+                }
+            }
+}
+
+/* One pass of Advect_Velocity_inRegular_outRegular_Kernel (Adv3D:76-113):
+ * cell centres backtrace through the regular velocity and sample the regular
+ * input in4 (channels 0-2; channel 3 is written 0). */
+template <class R>
+void regreg_pass(const Dims& d, const uint8_t* occ, const AdvCtx<R>& a, const RegSampler<R>& s, const R* in4,
+                 R* out4) {
+    const R hf = R(0.5);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int k = 0; k < d.D; k++)
+        for (int j = 0; j < d.H; j++)
+            for (int i = 0; i < d.W; i++) {
+                R px = (R)i + hf, py = (R)j + hf, pz = (R)k + hf;
+                backtrace(d, occ, s, a.steps, a.dt, a.h, a.full, px, py, pz);
+                size_t c = d.cell(i, j, k);
+                for (int q = 0; q < 3; q++)
+                    out4[c * 4 + q] = trilinear<R>(in4, d.W, d.H, d.D, 4, q, px - hf, py - hf, pz - hf);
+                out4[c * 4 + 3] = R(0);
+            }
+}
+
+/* The BFECC corrections (Adv3D:56-74).  Input_Increment_Kernel works on float
+ * arrays with double constants, so the expression is evaluated in double and
+ * rounded once to float; the float4 form multiplies by float constants and
+ * rounds each operation.  In FP64 both are the plain expression. */
+template <class R> static inline R bfecc_inc(R in, R star) {
+    if (sizeof(R) == 4) return (R)((double)in * 1.5 - (double)star * 0.5);
+    return in * R(1.5) - star * R(0.5);
+}
+template <class R> static inline R bfecc_inc4(R in, R star) {
+    const R a = in * R(1.5);
+    const R b = star * R(0.5);
+    return a - b;
+}
+
+/* Advect_Velocity (ZQ_CUDA_Advection3D.cu:1686-1749); the write-back follows
+ * cu_Apply_Advect_Velocity_Result_{Open,Closed}.  BFECC (Adv3D:1108-1182,
+ * 1240-1336, 1389-1474): a forward pass, a pass through the negated velocity
+ * from its result, the correction in = 1.5 in - 0.5 in** and a forward pass
+ * from the corrected field (the velocity of the passes is the original one
+ * throughout).  In the MAC form the correction is written into u, v, w in
+ * place, so faces the write-back leaves alone end with the corrected value. */
 template <class R>
 int advect_velocity(const Dims& d, R* u, R* v, R* w, const uint8_t* occ, const zqs_params& P, int mode,
                     bool open) {
     AdvCtx<R> a = adv_ctx<R>(P);
     std::vector<R> ou(d.nu(), R(0)), ov(d.nv(), R(0)), ow(d.nw(), R(0));
-    const R hf = R(0.5);
     if (mode == ZQS_ADV_VEL_INMAC_OUTMAC) {
-        /* Advect_Velocity_inMAC_outMAC_{u,v,w}_Kernel, Adv3D:232-377 */
         MacSampler<R> s{d, u, v, w};
-#pragma omp parallel for schedule(dynamic, 1)
-        for (int k = 0; k <= d.D; k++)
-            for (int j = 0; j <= d.H; j++)
-                for (int i = 0; i <= d.W; i++) {
-                    if (j < d.H && k < d.D) {
-                        R px = (R)i, py = (R)j + hf, pz = (R)k + hf;
-                        backtrace(d, occ, s, a.steps, a.dt, a.h, a.full, px, py, pz);
-                        ou[d.uix(i, j, k)] = trilinear<R>(u, d.W + 1, d.H, d.D, 1, 0, px, py - hf, pz - hf);
-                    }
-                    if (i < d.W && k < d.D) {
-                        R px = (R)i + hf, py = (R)j, pz = (R)k + hf;
-                        backtrace(d, occ, s, a.steps, a.dt, a.h, a.full, px, py, pz);
-                        ov[d.vix(i, j, k)] = trilinear<R>(v, d.W, d.H + 1, d.D, 1, 0, px - hf, py, pz - hf);
-                    }
-                    if (i < d.W && j < d.H) {
-                        R px = (R)i + hf, py = (R)j + hf, pz = (R)k;
-                        backtrace(d, occ, s, a.steps, a.dt, a.h, a.full, px, py, pz);
-                        ow[d.wix(i, j, k)] = trilinear<R>(w, d.W, d.H, d.D + 1, 1, 0, px - hf, py - hf, pz);
-                    }
-                }
-    } else if (mode == ZQS_ADV_VEL_INREG_OUTMAC) {
-        /* Advect_Velocity_inRegular_outMAC_{u,v,w}_Kernel, Adv3D:115-230 */
+        mac_pass(d, occ, a, s, u, v, w, ou.data(), ov.data(), ow.data());
+    } else if (mode == ZQS_ADV_VEL_INMAC_OUTMAC_BFECC) {
+        std::vector<R> u0(u, u + d.nu()), v0(v, v + d.nv()), w0(w, w + d.nw());
+        std::vector<R> su(d.nu(), R(0)), sv(d.nv(), R(0)), sw(d.nw(), R(0));
+        MacSampler<R> fwd{d, u0.data(), v0.data(), w0.data()};
+        MacSampler<R> bwd = fwd;
+        bwd.sg = R(-1);
+        mac_pass(d, occ, a, fwd, u0.data(), v0.data(), w0.data(), ou.data(), ov.data(), ow.data());
+        mac_pass(d, occ, a, bwd, ou.data(), ov.data(), ow.data(), su.data(), sv.data(), sw.data());
+        for (size_t x = 0; x < d.nu(); x++) u[x] = bfecc_inc(u[x], su[x]);
+        for (size_t x = 0; x < d.nv(); x++) v[x] = bfecc_inc(v[x], sv[x]);
+        for (size_t x = 0; x < d.nw(); x++) w[x] = bfecc_inc(w[x], sw[x]);
+        mac_pass(d, occ, a, fwd, u, v, w, ou.data(), ov.data(), ow.data());
+    } else if (mode == ZQS_ADV_VEL_INREG_OUTMAC || mode == ZQS_ADV_VEL_INREG_OUTMAC_BFECC) {
         std::vector<R> vel4(d.ncell() * 4);
         mac_to_regular4(d, u, v, w, vel4.data());
-        RegSampler<R> s{d, vel4.data()};
-#pragma omp parallel for schedule(dynamic, 1)
-        for (int k = 0; k <= d.D; k++)
-            for (int j = 0; j <= d.H; j++)
-                for (int i = 0; i <= d.W; i++) {
-                    if (j < d.H && k < d.D) {
-                        R px = (R)i, py = (R)j + hf, pz = (R)k + hf;
-                        backtrace(d, occ, s, a.steps, a.dt, a.h, a.full, px, py, pz);
-                        ou[d.uix(i, j, k)] =
-                            trilinear<R>(vel4.data(), d.W, d.H, d.D, 4, 0, px - hf, py - hf, pz - hf);
-                    }
-                    if (i < d.W && k < d.D) {
-                        R px = (R)i + hf, py = (R)j, pz = (R)k + hf;
-                        backtrace(d, occ, s, a.steps, a.dt, a.h, a.full, px, py, pz);
-                        ov[d.vix(i, j, k)] =
-                            trilinear<R>(vel4.data(), d.W, d.H, d.D, 4, 1, px - hf, py - hf, pz - hf);
-                    }
-                    if (i < d.W && j < d.H) {
-                        R px = (R)i + hf, py = (R)j + hf, pz = (R)k;
-                        backtrace(d, occ, s, a.steps, a.dt, a.h, a.full, px, py, pz);
-                        ow[d.wix(i, j, k)] =
-                            trilinear<R>(vel4.data(), d.W, d.H, d.D, 4, 2, px - hf, py - hf, pz - hf);
-                    }
-                }
-    } else if (mode == ZQS_ADV_VEL_INREG_OUTREG) {
-        /* Advect_Velocity_inRegular_outRegular_Kernel (Adv3D:76-113), then
-         * Regular4_to_MAC and the write-back (Adv3D:1061-1106) */
+        RegSampler<R> fwd{d, vel4.data()};
+        if (mode == ZQS_ADV_VEL_INREG_OUTMAC) {
+            regmac_pass(d, occ, a, fwd, vel4.data(), ou.data(), ov.data(), ow.data());
+        } else {
+            RegSampler<R> bwd = fwd;
+            bwd.sg = R(-1);
+            std::vector<R> t4(d.ncell() * 4);
+            regmac_pass(d, occ, a, fwd, vel4.data(), ou.data(), ov.data(), ow.data());
+            mac_to_regular4(d, ou.data(), ov.data(), ow.data(), t4.data());
+            regmac_pass(d, occ, a, bwd, t4.data(), ou.data(), ov.data(), ow.data());
+            mac_to_regular4(d, ou.data(), ov.data(), ow.data(), t4.data());
+            for (size_t x = 0; x < t4.size(); x++) t4[x] = bfecc_inc4(vel4[x], t4[x]);
+            regmac_pass(d, occ, a, fwd, t4.data(), ou.data(), ov.data(), ow.data());
+        }
+    } else if (mode == ZQS_ADV_VEL_INREG_OUTREG || mode == ZQS_ADV_VEL_INREG_OUTREG_BFECC) {
+        /* then Regular4_to_MAC and the write-back (Adv3D:1061-1106) */
         std::vector<R> vel4(d.ncell() * 4), out4(d.ncell() * 4);
         mac_to_regular4(d, u, v, w, vel4.data());
-        RegSampler<R> s{d, vel4.data()};
-#pragma omp parallel for schedule(dynamic, 1)
-        for (int k = 0; k < d.D; k++)
-            for (int j = 0; j < d.H; j++)
-                for (int i = 0; i < d.W; i++) {
-                    R px = (R)i + hf, py = (R)j + hf, pz = (R)k + hf;
-                    backtrace(d, occ, s, a.steps, a.dt, a.h, a.full, px, py, pz);
-                    size_t c = d.cell(i, j, k);
-                    for (int q = 0; q < 3; q++)
-                        out4[c * 4 + q] = trilinear<R>(vel4.data(), d.W, d.H, d.D, 4, q, px - hf, py - hf, pz - hf);
-                    out4[c * 4 + 3] = R(0);
-                }
+        RegSampler<R> fwd{d, vel4.data()};
+        if (mode == ZQS_ADV_VEL_INREG_OUTREG) {
+            regreg_pass(d, occ, a, fwd, vel4.data(), out4.data());
+        } else {
+            RegSampler<R> bwd = fwd;
+            bwd.sg = R(-1);
+            std::vector<R> s4(d.ncell() * 4);
+            regreg_pass(d, occ, a, fwd, vel4.data(), out4.data());
+            regreg_pass(d, occ, a, bwd, out4.data(), s4.data());
+            for (size_t x = 0; x < s4.size(); x++) s4[x] = bfecc_inc4(vel4[x], s4[x]);
+            regreg_pass(d, occ, a, fwd, s4.data(), out4.data());
+        }
         regular4_to_mac(d, out4.data(), ou.data(), ov.data(), ow.data());
     } else {
         return ZQS_EUNSUPPORTED;
@@ -513,35 +603,70 @@ int advect_velocity(const Dims& d, R* u, R* v, R* w, const uint8_t* occ, const z
     return ZQS_OK;
 }
 
-/* Advect_Scalar (Adv3D:1751-1821): backtrace from cell centres through MAC
- * (Adv3D:420-469) or regular (Adv3D:379-418) velocity, sample T and rho at the
- * final point; every cell is written, occupied ones included. */
-template <class R>
-int advect_scalar(const Dims& d, const R* u, const R* v, const R* w, const uint8_t* occ, const R* Tin,
-                  const R* Din, R* Tout, R* Dout, const zqs_params& P, int mode) {
-    AdvCtx<R> a = adv_ctx<R>(P);
+/* One pass of Advect_Scalar_{MAC,Regular}_Velocity_Kernel (Adv3D:379-469):
+ * backtrace from cell centres, sample T and rho at the final point; every
+ * cell is written, occupied ones included. */
+template <class R, class VelF>
+void scalar_pass(const Dims& d, const uint8_t* occ, const AdvCtx<R>& a, const VelF& s, const R* Tin, const R* Din,
+                 R* Tout, R* Dout) {
     const R hf = R(0.5);
-    std::vector<R> tt(d.ncell()), dd(d.ncell());
-    std::vector<R> vel4;
-    if (mode == ZQS_ADV_SCA_REG) {
-        vel4.resize(d.ncell() * 4);
-        mac_to_regular4(d, u, v, w, vel4.data());
-    } else if (mode != ZQS_ADV_SCA_MAC) {
-        return ZQS_EUNSUPPORTED;
-    }
-    MacSampler<R> ms{d, u, v, w};
-    RegSampler<R> rs{d, vel4.data()};
 #pragma omp parallel for schedule(dynamic, 1)
     for (int k = 0; k < d.D; k++)
         for (int j = 0; j < d.H; j++)
             for (int i = 0; i < d.W; i++) {
                 R px = (R)i + hf, py = (R)j + hf, pz = (R)k + hf;
-                if (mode == ZQS_ADV_SCA_MAC) backtrace(d, occ, ms, a.steps, a.dt, a.h, a.full, px, py, pz);
-                else backtrace(d, occ, rs, a.steps, a.dt, a.h, a.full, px, py, pz);
+                backtrace(d, occ, s, a.steps, a.dt, a.h, a.full, px, py, pz);
                 size_t c = d.cell(i, j, k);
-                tt[c] = trilinear<R>(Tin, d.W, d.H, d.D, 1, 0, px - hf, py - hf, pz - hf);
-                dd[c] = trilinear<R>(Din, d.W, d.H, d.D, 1, 0, px - hf, py - hf, pz - hf);
+                Tout[c] = trilinear<R>(Tin, d.W, d.H, d.D, 1, 0, px - hf, py - hf, pz - hf);
+                Dout[c] = trilinear<R>(Din, d.W, d.H, d.D, 1, 0, px - hf, py - hf, pz - hf);
             }
+}
+
+/* Advect_Scalar (Adv3D:1751-1821) through MAC or regular velocity.  BFECC
+ * follows cu_Advect_Scalar_{MAC,Regular}_Velocity_BFECC (Adv3D:1507-1554,
+ * 1586-1648): forward pass, negated-velocity pass from its result, the
+ * correction of the inputs (double expression, written into Tin/Din as the
+ * reference does), forward pass from the corrected fields.  (The reference's
+ * Advect_Scalar entry point never calls these and returns zeros for the BFECC
+ * types, Adv3D:1786-1794; this restates the intended three passes.) */
+template <class R>
+int advect_scalar(const Dims& d, const R* u, const R* v, const R* w, const uint8_t* occ, const R* Tin,
+                  const R* Din, R* Tout, R* Dout, const zqs_params& P, int mode) {
+    AdvCtx<R> a = adv_ctx<R>(P);
+    std::vector<R> tt(d.ncell()), dd(d.ncell());
+    const bool reg = mode == ZQS_ADV_SCA_REG || mode == ZQS_ADV_SCA_REG_BFECC;
+    const bool bfecc = mode == ZQS_ADV_SCA_MAC_BFECC || mode == ZQS_ADV_SCA_REG_BFECC;
+    if (mode < ZQS_ADV_SCA_MAC || mode > ZQS_ADV_SCA_REG_BFECC) return ZQS_EUNSUPPORTED;
+    std::vector<R> vel4;
+    if (reg) {
+        vel4.resize(d.ncell() * 4);
+        mac_to_regular4(d, u, v, w, vel4.data());
+    }
+    MacSampler<R> ms{d, u, v, w};
+    RegSampler<R> rs{d, vel4.data()};
+    auto pass = [&](R sg, const R* ti, const R* di, R* to, R* dout) {
+        if (reg) {
+            RegSampler<R> s = rs;
+            s.sg = sg;
+            scalar_pass(d, occ, a, s, ti, di, to, dout);
+        } else {
+            MacSampler<R> s = ms;
+            s.sg = sg;
+            scalar_pass(d, occ, a, s, ti, di, to, dout);
+        }
+    };
+    if (!bfecc) {
+        pass(R(1), Tin, Din, tt.data(), dd.data());
+    } else {
+        std::vector<R> t1(d.ncell()), d1(d.ncell()), ti(Tin, Tin + d.ncell()), di(Din, Din + d.ncell());
+        pass(R(1), ti.data(), di.data(), t1.data(), d1.data());
+        pass(R(-1), t1.data(), d1.data(), tt.data(), dd.data());
+        for (size_t x = 0; x < d.ncell(); x++) {
+            ti[x] = bfecc_inc(ti[x], tt[x]);
+            di[x] = bfecc_inc(di[x], dd[x]);
+        }
+        pass(R(1), ti.data(), di.data(), tt.data(), dd.data());
+    }
     std::copy(tt.begin(), tt.end(), Tout);
     std::copy(dd.begin(), dd.end(), Dout);
     return ZQS_OK;

@@ -68,7 +68,11 @@ def test_stage_attenuate(zqs_lib, oracle32, dims):
     assert_same(g.state(), st, what="attenuate")
 
 
-@pytest.mark.parametrize("mode", [capi.ADV_VEL_INMAC_OUTMAC, capi.ADV_VEL_INREG_OUTMAC, capi.ADV_VEL_INREG_OUTREG])
+VEL_MODES = [capi.ADV_VEL_INMAC_OUTMAC, capi.ADV_VEL_INREG_OUTMAC, capi.ADV_VEL_INREG_OUTREG,
+             capi.ADV_VEL_INMAC_OUTMAC_BFECC, capi.ADV_VEL_INREG_OUTMAC_BFECC, capi.ADV_VEL_INREG_OUTREG_BFECC]
+
+
+@pytest.mark.parametrize("mode", VEL_MODES)
 @pytest.mark.parametrize("is_open", [True, False])
 @pytest.mark.parametrize("dims", SMALL[:3])
 def test_stage_advect_velocity(zqs_lib, oracle32, mode, is_open, dims):
@@ -81,7 +85,7 @@ def test_stage_advect_velocity(zqs_lib, oracle32, mode, is_open, dims):
     assert_same(g.state(), st, keys=("u", "v", "w"), what=f"advect_velocity mode {mode}")
 
 
-@pytest.mark.parametrize("mode", [capi.ADV_SCA_MAC, capi.ADV_SCA_REG])
+@pytest.mark.parametrize("mode", [capi.ADV_SCA_MAC, capi.ADV_SCA_REG, capi.ADV_SCA_MAC_BFECC, capi.ADV_SCA_REG_BFECC])
 @pytest.mark.parametrize("full", [0, 1])
 @pytest.mark.parametrize("dims", SMALL[:3])
 def test_stage_advect_scalar(zqs_lib, oracle32, mode, full, dims):
@@ -135,7 +139,10 @@ def test_mac_to_regular4(zqs_lib, oracle32):
 
 
 COMBOS = [(capi.ADV_VEL_INMAC_OUTMAC, capi.ADV_SCA_MAC), (capi.ADV_VEL_INREG_OUTREG, capi.ADV_SCA_REG),
-          (capi.ADV_VEL_INREG_OUTMAC, capi.ADV_SCA_MAC)]
+          (capi.ADV_VEL_INREG_OUTMAC, capi.ADV_SCA_MAC),
+          (capi.ADV_VEL_INMAC_OUTMAC_BFECC, capi.ADV_SCA_MAC_BFECC),
+          (capi.ADV_VEL_INREG_OUTREG_BFECC, capi.ADV_SCA_REG_BFECC),
+          (capi.ADV_VEL_INREG_OUTMAC_BFECC, capi.ADV_SCA_MAC)]
 
 
 @pytest.mark.parametrize("vm,sm", COMBOS)
@@ -315,11 +322,26 @@ def test_legacy_advect_velocity_and_scalar(zqs_lib, oracle32):
     assert ms >= 0, capi.last_error()
     oracle32.advect_scalar(w.W, w.H, w.D, ref, w.occ, w.params, capi.ADV_SCA_REG)
     assert np.array_equal(outT, ref["T"]) and np.array_equal(outD, ref["rho"])
-    # BFECC is refused and leaves the arrays untouched
+    # BFECC through the same entry points (the reference's Advect_Scalar
+    # returns zeros for these types; here the three passes run)
+    ms = lib.Advect_Velocity(st["u"].ctypes.data, st["v"].ctypes.data, st["w"].ctypes.data, occ.ctypes.data, False,
+                             capi.ADV_VEL_INMAC_OUTMAC_BFECC)
+    assert ms >= 0, capi.last_error()
+    oracle32.advect_velocity(w.W, w.H, w.D, ref, w.occ, w.params, capi.ADV_VEL_INMAC_OUTMAC_BFECC, False)
+    assert_same(st, ref, keys=("u", "v", "w"), what="Advect_Velocity BFECC")
+    ms = lib.Advect_Scalar(st["u"].ctypes.data, st["v"].ctypes.data, st["w"].ctypes.data, occ.ctypes.data,
+                           st["T"].ctypes.data, st["rho"].ctypes.data, outT.ctypes.data, outD.ctypes.data,
+                           capi.ADV_SCA_MAC_BFECC)
+    assert ms >= 0, capi.last_error()
+    ref["T"], ref["rho"] = st["T"].copy(), st["rho"].copy()   # the inputs (the REG call above wrote ref's)
+    oracle32.advect_scalar(w.W, w.H, w.D, ref, w.occ, w.params, capi.ADV_SCA_MAC_BFECC)
+    assert np.array_equal(outT, ref["T"]) and np.array_equal(outD, ref["rho"])
+    assert float(np.abs(outD).sum()) > 0.0
+    # an unknown type is refused and leaves the arrays untouched
     before = st["u"].copy()
     ms = lib.Advect_Velocity(st["u"].ctypes.data, st["v"].ctypes.data, st["w"].ctypes.data, occ.ctypes.data, True,
-                             capi.ADV_VEL_INMAC_OUTMAC_BFECC)
-    assert ms == -capi.ZQS_EUNSUPPORTED and np.array_equal(st["u"], before)
+                             6)
+    assert ms == -capi.ZQS_EINVAL and np.array_equal(st["u"], before)
 
 
 def test_legacy_addforce_attenuation_projection(zqs_lib, oracle32):
@@ -409,12 +431,14 @@ def test_errors_are_reported(zqs_lib):
         g.set_params(p)
     assert e.value.code == capi.ZQS_EINVAL
     p.substeps = 2
+    p.adv_vel_mode = 6
+    with pytest.raises(capi.ZQSError) as e:
+        g.set_params(p)
+    assert e.value.code == capi.ZQS_EINVAL
     p.adv_vel_mode = capi.ADV_VEL_INMAC_OUTMAC_BFECC
     g.set_params(p)
     g.upload(capi.FIELD_OCCUPANCY, np.zeros((4, 4, 4), np.uint8))
-    with pytest.raises(capi.ZQSError) as e:
-        g.step(1)
-    assert e.value.code == capi.ZQS_EUNSUPPORTED
+    g.step(1)
     with pytest.raises(capi.ZQSError):
         g.set_sor_config(9)
     g.close()

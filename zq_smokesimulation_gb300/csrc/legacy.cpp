@@ -139,9 +139,9 @@ extern "C" ZQS_API float Advect_Velocity(float* u, float* v, float* w, const boo
         set_error("Advect_Velocity: call ZQ_Cuda_Prepare_Advection first with steps >= 1; pointers must be non-NULL");
         return fail(ZQS_EINVAL);
     }
-    if (type != ADV_VEL_INMAC_OUTMAC && type != ADV_VEL_INREG_OUTMAC && type != ADV_VEL_INREG_OUTREG) {
-        set_error("Advect_Velocity: BFECC modes are not implemented; arrays left untouched");
-        return fail(ZQS_EUNSUPPORTED);
+    if ((int)type < (int)ADV_VEL_INREG_OUTREG || (int)type > (int)ADV_VEL_INREG_OUTMAC_BFECC) {
+        set_error("Advect_Velocity: unknown advection type; arrays left untouched");
+        return fail(ZQS_EINVAL);
     }
     zqs_grid* g;
     LEG_TRY(cached_grid(g_adv.W, g_adv.H, g_adv.D, &g));
@@ -172,9 +172,9 @@ extern "C" ZQS_API float Advect_Scalar(const float* u, const float* v, const flo
         set_error("Advect_Scalar: call ZQ_Cuda_Prepare_Advection first with steps >= 1; pointers must be non-NULL");
         return fail(ZQS_EINVAL);
     }
-    if (type != ADV_SCA_MAC && type != ADV_SCA_REG) {
-        set_error("Advect_Scalar: BFECC modes are not implemented; outputs left untouched");
-        return fail(ZQS_EUNSUPPORTED);
+    if ((int)type < (int)ADV_SCA_MAC || (int)type > (int)ADV_SCA_REG_BFECC) {
+        set_error("Advect_Scalar: unknown advection type; outputs left untouched");
+        return fail(ZQS_EINVAL);
     }
     zqs_grid* g;
     LEG_TRY(cached_grid(g_adv.W, g_adv.H, g_adv.D, &g));

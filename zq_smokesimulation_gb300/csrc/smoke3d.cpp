@@ -763,12 +763,6 @@ bool ZQ_SmokeSimulation3D::Init(const char* file) {
     if (!ZQ_InitFineGrid3D(fineGrid, para)) return false;
     zqs_params p;
     if (!para.ToParams(&p)) return false;
-    if (p.adv_vel_mode == ZQS_ADV_VEL_INMAC_OUTMAC_BFECC || p.adv_vel_mode == ZQS_ADV_VEL_INREG_OUTREG_BFECC ||
-        p.adv_vel_mode == ZQS_ADV_VEL_INREG_OUTMAC_BFECC || p.adv_sca_mode == ZQS_ADV_SCA_MAC_BFECC ||
-        p.adv_sca_mode == ZQS_ADV_SCA_REG_BFECC) {
-        printf("BFECC advection is not available in this library\n");
-        return false;
-    }
     return prepare(fineGrid, para) != nullptr || fail("Init");
 }
 

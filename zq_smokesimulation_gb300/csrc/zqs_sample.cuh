@@ -197,7 +197,9 @@ struct QuadTri {
     __device__ __forceinline__ float operator()(const Layout& L, const Tri0& c) const { return tri0_quad(q, L, c); }
 };
 
-template <class Tri>
+// NEG samples the negated field (the BFECC backward pass); negation is exact
+// and commutes with the interpolation, so this equals sampling -u, -v, -w.
+template <class Tri, bool NEG = false>
 struct MacVelT {
     Layout L;
     Tri u, v, w;
@@ -205,6 +207,11 @@ struct MacVelT {
         vx = u(L, tri0(L, L.W + 1, L.H, L.D, px, py - 0.5f, pz - 0.5f));
         vy = v(L, tri0(L, L.W, L.H + 1, L.D, px - 0.5f, py, pz - 0.5f));
         vz = w(L, tri0(L, L.W, L.H, L.D + 1, px - 0.5f, py - 0.5f, pz));
+        if (NEG) {
+            vx = -vx;
+            vy = -vy;
+            vz = -vz;
+        }
     }
     // Also returns the cell containing the point when it lies in the domain:
     // the u grid's x corner floor(clamp(x, 0, W)), the v grid's y and the w
@@ -231,6 +238,11 @@ struct MacVelT {
         vx = u(L, cu);
         vy = v(L, cv);
         vz = w(L, cw);
+        if (NEG) {
+            vx = -vx;
+            vy = -vy;
+            vz = -vz;
+        }
         ci = min(xu.i0, L.W - 1);
         cj = min(yv.i0, L.H - 1);
         ck = min(zw.i0, L.D - 1);
@@ -238,16 +250,18 @@ struct MacVelT {
 };
 using MacVel = MacVelT<FieldTri>;   // corners from the fields
 using MacVelQ = MacVelT<QuadTri>;   // corners from the quad copies
-struct RegVel {
+template <bool NEG = false>
+struct RegVelT {
     Layout L;
     const float4* vel4;
     __device__ __forceinline__ void operator()(float px, float py, float pz, float& vx, float& vy, float& vz) const {
         float3 r = tri4(vel4, corners(L, L.W, L.H, L.D, px - 0.5f, py - 0.5f, pz - 0.5f));
-        vx = r.x;
-        vy = r.y;
-        vz = r.z;
+        vx = NEG ? -r.x : r.x;
+        vy = NEG ? -r.y : r.y;
+        vz = NEG ? -r.z : r.z;
     }
 };
+using RegVel = RegVelT<false>;
 
 // The reference backtrace (e.g. ZQ_CUDA_Advection3D.cu:253-273): test the
 // point (inside [0,W]x[0,H]x[0,D] and its clamped floor cell free), remember
@@ -303,9 +317,9 @@ __device__ __forceinline__ void backtrace(const Layout& L, const uint8_t* __rest
 
 // backtrace() for the MAC sampler: the occupancy test reuses the cell index
 // that the velocity sample at the same point already floored.
-template <class Tri>
+template <class Tri, bool NEG>
 __device__ __forceinline__ void backtrace(const Layout& L, const uint8_t* __restrict__ flags,
-                                          const MacVelT<Tri>& vel, const KParams& kp, float& px, float& py,
+                                          const MacVelT<Tri, NEG>& vel, const KParams& kp, float& px, float& py,
                                           float& pz) {
     float vx, vy, vz;
     int ci, cj, ck;
