@@ -49,7 +49,12 @@ typedef enum zqs_status {
  * OPEN   = cells outside the domain are Dirichlet p = 0 (TOTAL_OPEN_POISSON_SOR)
  * CLOSED = outside is Neumann and the mean divergence over free cells is
  *          removed first (TOTAL_CLOSED_POISSON_SOR).                          */
-typedef enum zqs_solver { ZQS_SOLVER_OPEN = 0, ZQS_SOLVER_CLOSED = 1 } zqs_solver;
+/* OPEN / CLOSED: the fine-grid red-black SOR (TOTAL_{OPEN,CLOSED}_POISSON_SOR).
+ * COARSE_OPEN: the coarse-grid projection of COARSE_{OPEN,CLOSED}_POISSON_SOR
+ * (the reference runs the open coarse solver for both, Utils3D:3732-3746):
+ * face-ratio SOR on the grid coarsened by sub_size, the correction mapped back,
+ * then an exact projection inside every sub_size^3 block (Utils3D:3688-3794). */
+typedef enum zqs_solver { ZQS_SOLVER_OPEN = 0, ZQS_SOLVER_CLOSED = 1, ZQS_SOLVER_COARSE_OPEN = 2 } zqs_solver;
 
 /* Numeric values are those of ZQ_CUDA_Advection3D.h:7-21 (the CUDA header,
  * not the ZQ_SmokeSimulationPara3D enum). */
@@ -110,6 +115,7 @@ typedef struct zqs_params {
                                move); 1: also test and use the final point       */
     int32_t n_sources;
     zqs_source sources[ZQS_MAX_SOURCES];
+    int32_t sub_size;       /* COARSE_OPEN: block edge (subSize); divides W, H, D */
 } zqs_params;
 
 /* Fields addressable by upload/download. */

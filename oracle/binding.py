@@ -93,6 +93,19 @@ class Oracle:
                            C.byref(stats))
         return (p, div, stats) if want else stats
 
+    def project_coarse(self, W, H, D, st, occ, params):
+        """Coarse-grid projection in place on st's u, v, w (ZQS_SOLVER_COARSE_OPEN)."""
+        return self._f("project_coarse")(W, H, D, _p(st["u"]), _p(st["v"]), _p(st["w"]), _p(occ),
+                                         C.byref(params))
+
+    def submatrix(self, s):
+        """The sub-projection matrix of block edge s as (3 s^2 (s-1), 3 s^2 (s+1)) float32."""
+        rows, cols = 3 * s * s * (s - 1), 3 * s * s * (s + 1)
+        out = np.zeros((rows, cols), np.float32)
+        n = self.lib.zqo_submatrix(s, _p(out), rows * cols)
+        assert n == rows * cols, n
+        return out
+
     def reinject(self, W, H, D, st, params):
         self._f("reinject")(W, H, D, _p(st["T"]), _p(st["rho"]), C.byref(params))
 

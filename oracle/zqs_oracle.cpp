@@ -863,6 +863,549 @@ void project(const Dims& d, R* u, R* v, R* w, const uint8_t* occ, const zqs_para
     if (div_out) std::copy(div.begin(), div.end(), div_out);
 }
 
+/* ---------------------------------------------------------------------- */
+/* Coarse-grid projection (COARSE_{OPEN,CLOSED}_POISSON_SOR)               */
+/* ---------------------------------------------------------------------- */
+/* ZQ_TotalProjection3D (Utils3D:3688-3794) for the coarse SOR solvers (the
+ * reference calls the open coarse solver for both, :3732-3746):
+ *   1. face un-occupancy ratios of the grid coarsened by s (ZQ_InitCoarseGrid3D,
+ *      Utils3D:1666-1888); a coarse cell with all six ratios 0 is occupied;
+ *   2. coarse velocity = mean of the fine faces on each coarse face
+ *      (ZQ_MapFine2Coarse3D, Utils3D:2170-2258);
+ *   3. red-black SOR on the face-ratio Poisson system of ZQ_InitMatOpenPoisson3D
+ *      (Utils3D:476-601: weight = ratio of the face to a free in-domain
+ *      neighbour, 1 with p = 0 for a domain face, diagonal = their sum in the
+ *      order out-of-domain count, z-, z+, y-, y+, x-, x+), then the velocity
+ *      correction of ZQ_AdjustOpenVelocity3D (Utils3D:2794-2866: u -= p_R - p_L
+ *      on faces with ratio > 0); the delta is (u - g) - u as the reference forms
+ *      it (Utils3D:2611-2642).  The solver itself (SolveOpenPoissonRedBlack-
+ *      withFaceRatio3D_MAC) is not in the reference tree; the update is the one
+ *      of the fine SOR: p <- fma(omega/diag, s - div, (1-omega) p);
+ *   4. the delta added to the fine faces of each coarse face whose fine cells
+ *      are free (ZQ_MapCoarse2Fine3D, Utils3D:3172-3296; the x = W face tests
+ *      the inside cell x = W-1, where the reference reads one past the row);
+ *   5. with s > 1, an exact projection inside every s^3 block
+ *      (ZQ_SubProjection3D, Utils3D:3298-3685): blocks without an occupied fine
+ *      cell apply the dense matrix of ZQ_InitSubMatPoisson3D (Utils3D:1151-
+ *      1391) to the block's faces; the others solve their closed Poisson
+ *      problem (ratio 1 between free cells, first free cell pinned) in the
+ *      least-squares sense (ZQ_SolveSubGrid3D, Utils3D:1393-1521), here by CG
+ *      on the normal equations in double, and correct the interior faces. */
+
+template <class R>
+struct CoarseGrid {
+    Dims c;                         // coarse dims
+    std::vector<R> ru, rv, rw;      // face un-occupancy ratios (coarse MAC layout)
+    std::vector<uint8_t> occ;       // coarse occupancy
+};
+
+template <class R>
+void coarse_init(const Dims& f, int s, const uint8_t* occ, CoarseGrid<R>& g) {
+    Dims c{f.W / s, f.H / s, f.D / s};
+    g.c = c;
+    g.ru.assign(c.nu(), R(0));
+    g.rv.assign(c.nv(), R(0));
+    g.rw.assign(c.nw(), R(0));
+    g.occ.assign(c.ncell(), 0);
+    const R area = (R)(s * s);
+    auto ratio = [&](int n) -> R { return R(1) - (R)n / area; };
+    for (int k = 0; k < c.D; k++)
+        for (int j = 0; j < c.H; j++)
+            for (int i = 0; i <= c.W; i++) {
+                int n = 0;
+                for (int sk = 0; sk < s; sk++)
+                    for (int sj = 0; sj < s; sj++) {
+                        const int y = j * s + sj, z = k * s + sk;
+                        if (i == 0) n += occ[f.cell(0, y, z)] ? 1 : 0;
+                        else if (i == c.W) n += occ[f.cell(f.W - 1, y, z)] ? 1 : 0;
+                        else n += (occ[f.cell(i * s, y, z)] || occ[f.cell(i * s - 1, y, z)]) ? 1 : 0;
+                    }
+                g.ru[c.uix(i, j, k)] = ratio(n);
+            }
+    for (int k = 0; k < c.D; k++)
+        for (int j = 0; j <= c.H; j++)
+            for (int i = 0; i < c.W; i++) {
+                int n = 0;
+                for (int sk = 0; sk < s; sk++)
+                    for (int si = 0; si < s; si++) {
+                        const int x = i * s + si, z = k * s + sk;
+                        if (j == 0) n += occ[f.cell(x, 0, z)] ? 1 : 0;
+                        else if (j == c.H) n += occ[f.cell(x, f.H - 1, z)] ? 1 : 0;
+                        else n += (occ[f.cell(x, j * s, z)] || occ[f.cell(x, j * s - 1, z)]) ? 1 : 0;
+                    }
+                g.rv[c.vix(i, j, k)] = ratio(n);
+            }
+    for (int k = 0; k <= c.D; k++)
+        for (int j = 0; j < c.H; j++)
+            for (int i = 0; i < c.W; i++) {
+                int n = 0;
+                for (int sj = 0; sj < s; sj++)
+                    for (int si = 0; si < s; si++) {
+                        const int x = i * s + si, y = j * s + sj;
+                        if (k == 0) n += occ[f.cell(x, y, 0)] ? 1 : 0;
+                        else if (k == c.D) n += occ[f.cell(x, y, f.D - 1)] ? 1 : 0;
+                        else n += (occ[f.cell(x, y, k * s)] || occ[f.cell(x, y, k * s - 1)]) ? 1 : 0;
+                    }
+                g.rw[c.wix(i, j, k)] = ratio(n);
+            }
+    for (int k = 0; k < c.D; k++)
+        for (int j = 0; j < c.H; j++)
+            for (int i = 0; i < c.W; i++)
+                g.occ[c.cell(i, j, k)] = (g.ru[c.uix(i, j, k)] == R(0) && g.ru[c.uix(i + 1, j, k)] == R(0) &&
+                                          g.rv[c.vix(i, j, k)] == R(0) && g.rv[c.vix(i, j + 1, k)] == R(0) &&
+                                          g.rw[c.wix(i, j, k)] == R(0) && g.rw[c.wix(i, j, k + 1)] == R(0))
+                                             ? 1
+                                             : 0;
+}
+
+/* Steps 2-4: the coarse correction added to the fine faces. */
+template <class R>
+void coarse_correct(const Dims& f, int s, const uint8_t* occ, const CoarseGrid<R>& g, R* u, R* v, R* w,
+                    const zqs_params& P) {
+    const Dims& c = g.c;
+    const R area = (R)(s * s);
+    std::vector<R> cu(c.nu()), cv(c.nv()), cw(c.nw());
+    for (int k = 0; k < c.D; k++)
+        for (int j = 0; j < c.H; j++)
+            for (int i = 0; i <= c.W; i++) {
+                R sum = R(0);
+                for (int sk = 0; sk < s; sk++)
+                    for (int sj = 0; sj < s; sj++) sum += u[f.uix(i * s, j * s + sj, k * s + sk)];
+                cu[c.uix(i, j, k)] = sum / area;
+            }
+    for (int k = 0; k < c.D; k++)
+        for (int j = 0; j <= c.H; j++)
+            for (int i = 0; i < c.W; i++) {
+                R sum = R(0);
+                for (int sk = 0; sk < s; sk++)
+                    for (int si = 0; si < s; si++) sum += v[f.vix(i * s + si, j * s, k * s + sk)];
+                cv[c.vix(i, j, k)] = sum / area;
+            }
+    for (int k = 0; k <= c.D; k++)
+        for (int j = 0; j < c.H; j++)
+            for (int i = 0; i < c.W; i++) {
+                R sum = R(0);
+                for (int sj = 0; sj < s; sj++)
+                    for (int si = 0; si < s; si++) sum += w[f.wix(i * s + si, j * s + sj, k * s)];
+                cw[c.wix(i, j, k)] = sum / area;
+            }
+    /* the face-ratio system */
+    const int W = c.W, H = c.H, D = c.D;
+    const size_t n = c.ncell();
+    std::vector<R> div(n, R(0)), diag(n, R(0)), p(n, R(0));
+    for (int k = 0; k < D; k++)
+        for (int j = 0; j < H; j++)
+            for (int i = 0; i < W; i++) {
+                const size_t cc = c.cell(i, j, k);
+                if (g.occ[cc]) continue;
+                div[cc] = ((((cu[c.uix(i + 1, j, k)] - cu[c.uix(i, j, k)]) + cv[c.vix(i, j + 1, k)]) -
+                            cv[c.vix(i, j, k)]) + cw[c.wix(i, j, k + 1)]) - cw[c.wix(i, j, k)];
+                const int nin = (k > 0) + (k < D - 1) + (j > 0) + (j < H - 1) + (i > 0) + (i < W - 1);
+                R cnt = (R)(6 - nin);
+                if (k > 0 && !g.occ[cc - (size_t)W * H]) cnt += g.rw[c.wix(i, j, k)];
+                if (k < D - 1 && !g.occ[cc + (size_t)W * H]) cnt += g.rw[c.wix(i, j, k + 1)];
+                if (j > 0 && !g.occ[cc - W]) cnt += g.rv[c.vix(i, j, k)];
+                if (j < H - 1 && !g.occ[cc + W]) cnt += g.rv[c.vix(i, j + 1, k)];
+                if (i > 0 && !g.occ[cc - 1]) cnt += g.ru[c.uix(i, j, k)];
+                if (i < W - 1 && !g.occ[cc + 1]) cnt += g.ru[c.uix(i + 1, j, k)];
+                diag[cc] = cnt;
+            }
+    const R omega = (R)P.omega;
+    const R om1 = R(1) - omega;
+    const size_t sy = (size_t)W, sz = (size_t)W * H;
+    auto term = [&](bool in, size_t nb, R r) -> R { return (in && !g.occ[nb]) ? r * p[nb] : R(0); };
+    for (int it = 0; it < P.sor_iters; it++)
+        for (int colour = 0; colour < 2; colour++)
+            for (int k = 0; k < D; k++)
+                for (int j = 0; j < H; j++)
+                    for (int i = (j + k + colour) & 1; i < W; i += 2) {
+                        const size_t cc = c.cell(i, j, k);
+                        if (g.occ[cc] || diag[cc] == R(0)) continue;
+                        const R xm = term(i > 0, cc - 1, g.ru[c.uix(i, j, k)]);
+                        const R xp = term(i < W - 1, cc + 1, g.ru[c.uix(i + 1, j, k)]);
+                        const R ym = term(j > 0, cc - sy, g.rv[c.vix(i, j, k)]);
+                        const R yp = term(j < H - 1, cc + sy, g.rv[c.vix(i, j + 1, k)]);
+                        const R zm = term(k > 0, cc - sz, g.rw[c.wix(i, j, k)]);
+                        const R zp = term(k < D - 1, cc + sz, g.rw[c.wix(i, j, k + 1)]);
+                        const R sum = ((xm + xp) + (ym + yp)) + (zm + zp);
+                        const R wc = omega / diag[cc];
+                        p[cc] = std::fma(wc, sum - div[cc], om1 * p[cc]);
+                    }
+    /* delta = (u - (p_R - p_L)) - u on faces with ratio > 0, p = 0 outside */
+    const R zero = R(0);
+    auto pc = [&](int i, int j, int k) -> R { return p[c.cell(i, j, k)]; };
+    std::vector<R> du(c.nu(), R(0)), dv(c.nv(), R(0)), dw(c.nw(), R(0));
+    for (int k = 0; k < D; k++)
+        for (int j = 0; j < H; j++)
+            for (int i = 0; i <= W; i++) {
+                const size_t x = c.uix(i, j, k);
+                if (!(g.ru[x] > R(0))) continue;
+                const R gr = i == 0 ? pc(0, j, k) - zero : (i == W ? zero - pc(W - 1, j, k) : pc(i, j, k) - pc(i - 1, j, k));
+                du[x] = (cu[x] - gr) - cu[x];
+            }
+    for (int k = 0; k < D; k++)
+        for (int j = 0; j <= H; j++)
+            for (int i = 0; i < W; i++) {
+                const size_t x = c.vix(i, j, k);
+                if (!(g.rv[x] > R(0))) continue;
+                const R gr = j == 0 ? pc(i, 0, k) - zero : (j == H ? zero - pc(i, H - 1, k) : pc(i, j, k) - pc(i, j - 1, k));
+                dv[x] = (cv[x] - gr) - cv[x];
+            }
+    for (int k = 0; k <= D; k++)
+        for (int j = 0; j < H; j++)
+            for (int i = 0; i < W; i++) {
+                const size_t x = c.wix(i, j, k);
+                if (!(g.rw[x] > R(0))) continue;
+                const R gr = k == 0 ? pc(i, j, 0) - zero : (k == D ? zero - pc(i, j, D - 1) : pc(i, j, k) - pc(i, j, k - 1));
+                dw[x] = (cw[x] - gr) - cw[x];
+            }
+    /* back to the fine faces whose fine cells are free */
+    for (int k = 0; k < c.D; k++)
+        for (int j = 0; j < c.H; j++)
+            for (int i = 0; i <= c.W; i++)
+                for (int sk = 0; sk < s; sk++)
+                    for (int sj = 0; sj < s; sj++) {
+                        const int x = i * s, y = j * s + sj, z = k * s + sk;
+                        bool ok;
+                        if (i == 0) ok = !occ[f.cell(0, y, z)];
+                        else if (i == c.W) ok = !occ[f.cell(f.W - 1, y, z)];
+                        else ok = !occ[f.cell(x, y, z)] && !occ[f.cell(x - 1, y, z)];
+                        if (ok) u[f.uix(x, y, z)] += du[c.uix(i, j, k)];
+                    }
+    for (int k = 0; k < c.D; k++)
+        for (int j = 0; j <= c.H; j++)
+            for (int i = 0; i < c.W; i++)
+                for (int sk = 0; sk < s; sk++)
+                    for (int si = 0; si < s; si++) {
+                        const int x = i * s + si, y = j * s, z = k * s + sk;
+                        bool ok;
+                        if (j == 0) ok = !occ[f.cell(x, 0, z)];
+                        else if (j == c.H) ok = !occ[f.cell(x, f.H - 1, z)];
+                        else ok = !occ[f.cell(x, y, z)] && !occ[f.cell(x, y - 1, z)];
+                        if (ok) v[f.vix(x, y, z)] += dv[c.vix(i, j, k)];
+                    }
+    for (int k = 0; k <= c.D; k++)
+        for (int j = 0; j < c.H; j++)
+            for (int i = 0; i < c.W; i++)
+                for (int sj = 0; sj < s; sj++)
+                    for (int si = 0; si < s; si++) {
+                        const int x = i * s + si, y = j * s + sj, z = k * s;
+                        bool ok;
+                        if (k == 0) ok = !occ[f.cell(x, y, 0)];
+                        else if (k == c.D) ok = !occ[f.cell(x, y, f.D - 1)];
+                        else ok = !occ[f.cell(x, y, z)] && !occ[f.cell(x, y, z - 1)];
+                        if (ok) w[f.wix(x, y, z)] += dw[c.wix(i, j, k)];
+                    }
+}
+
+/* Block face order of the sub-projection (Utils3D:3356-3385): u faces
+ * (k, j, i = 0..s), then v (k, j = 0..s, i), then w (k = 0..s, j, i); the
+ * interior faces (rows of the matrix, Utils3D:1348-1387) in the same order
+ * with i, j or k in 1..s-1. */
+struct BlockFaces {
+    int s, nf, ni;
+    int uix(int i, int j, int k) const { return (k * s + j) * (s + 1) + i; }
+    int vix(int i, int j, int k) const { return s * s * (s + 1) + (k * (s + 1) + j) * s + i; }
+    int wix(int i, int j, int k) const { return 2 * s * s * (s + 1) + (k * s + j) * s + i; }
+    explicit BlockFaces(int s_) : s(s_), nf(3 * s_ * s_ * (s_ + 1)), ni(3 * s_ * s_ * (s_ - 1)) {}
+    /* interior face r -> block face index */
+    std::vector<int> interior() const {
+        std::vector<int> r;
+        for (int k = 0; k < s; k++)
+            for (int j = 0; j < s; j++)
+                for (int i = 1; i < s; i++) r.push_back(uix(i, j, k));
+        for (int k = 0; k < s; k++)
+            for (int j = 1; j < s; j++)
+                for (int i = 0; i < s; i++) r.push_back(vix(i, j, k));
+        for (int k = 1; k < s; k++)
+            for (int j = 0; j < s; j++)
+                for (int i = 0; i < s; i++) r.push_back(wix(i, j, k));
+        return r;
+    }
+};
+
+/* ZQ_InitSubMatPoisson3D (Utils3D:1151-1391): the matrix I - D [0; P+ V]
+ * restricted to the interior faces, P the block's Neumann Laplacian without
+ * the column of cell 0, V the divergence, D the gradient on interior faces;
+ * P+ = (P^T P)^-1 P^T (P has full column rank; the reference forms P+ by SVD),
+ * with P^T P = (L^2) without row and column 0 and P^T V = L V without row 0
+ * (L symmetric).  Built in double, stored as float rows of nf columns. */
+static std::vector<float> submatrix(int s) {
+    const int n = s * s * s;
+    BlockFaces bf(s);
+    const int nf = bf.nf;
+    std::vector<double> L((size_t)n * n, 0.0);
+    auto cell = [&](int i, int j, int k) { return (k * s + j) * s + i; };
+    for (int k = 0; k < s; k++)
+        for (int j = 0; j < s; j++)
+            for (int i = 0; i < s; i++) {
+                const int c0 = cell(i, j, k);
+                int cnt = 0;
+                const int di[6] = {-1, 1, 0, 0, 0, 0}, dj[6] = {0, 0, -1, 1, 0, 0}, dk[6] = {0, 0, 0, 0, -1, 1};
+                for (int q = 0; q < 6; q++) {
+                    const int a = i + di[q], b = j + dj[q], e = k + dk[q];
+                    if (a < 0 || a >= s || b < 0 || b >= s || e < 0 || e >= s) continue;
+                    L[(size_t)c0 * n + cell(a, b, e)] = 1.0;
+                    cnt++;
+                }
+                L[(size_t)c0 * n + c0] = -(double)cnt;
+            }
+    /* V: divergence of cell c over the block faces */
+    std::vector<double> V((size_t)n * nf, 0.0);
+    for (int k = 0; k < s; k++)
+        for (int j = 0; j < s; j++)
+            for (int i = 0; i < s; i++) {
+                double* r = &V[(size_t)cell(i, j, k) * nf];
+                r[bf.uix(i, j, k)] -= 1.0;
+                r[bf.uix(i + 1, j, k)] += 1.0;
+                r[bf.vix(i, j, k)] -= 1.0;
+                r[bf.vix(i, j + 1, k)] += 1.0;
+                r[bf.wix(i, j, k)] -= 1.0;
+                r[bf.wix(i, j, k + 1)] += 1.0;
+            }
+    const int m = n - 1;
+    /* G = (L^2)[1:,1:], B = (L V)[1:, :] */
+    std::vector<double> G((size_t)m * m, 0.0), B((size_t)m * nf, 0.0);
+    for (int a = 1; a < n; a++) {
+        for (int b = 1; b < n; b++) {
+            double acc = 0.0;
+            for (int t = 0; t < n; t++) acc += L[(size_t)a * n + t] * L[(size_t)t * n + b];
+            G[(size_t)(a - 1) * m + (b - 1)] = acc;
+        }
+        for (int t = 0; t < n; t++) {
+            const double l = L[(size_t)a * n + t];
+            if (l == 0.0) continue;
+            const double* vr = &V[(size_t)t * nf];
+            double* br = &B[(size_t)(a - 1) * nf];
+            for (int q = 0; q < nf; q++) br[q] += l * vr[q];
+        }
+    }
+    /* Cholesky G = C C^T, then X = G^-1 B */
+    for (int a = 0; a < m; a++) {
+        for (int b = 0; b <= a; b++) {
+            double acc = G[(size_t)a * m + b];
+            for (int t = 0; t < b; t++) acc -= G[(size_t)a * m + t] * G[(size_t)b * m + t];
+            if (a == b) G[(size_t)a * m + a] = std::sqrt(acc);
+            else G[(size_t)a * m + b] = acc / G[(size_t)b * m + b];
+        }
+    }
+    for (int q = 0; q < nf; q++) {
+        for (int a = 0; a < m; a++) {
+            double acc = B[(size_t)a * nf + q];
+            for (int t = 0; t < a; t++) acc -= G[(size_t)a * m + t] * B[(size_t)t * nf + q];
+            B[(size_t)a * nf + q] = acc / G[(size_t)a * m + a];
+        }
+        for (int a = m - 1; a >= 0; a--) {
+            double acc = B[(size_t)a * nf + q];
+            for (int t = a + 1; t < m; t++) acc -= G[(size_t)t * m + a] * B[(size_t)t * nf + q];
+            B[(size_t)a * nf + q] = acc / G[(size_t)a * m + a];
+        }
+    }
+    /* rows: interior faces; row r of I - D [0; X] */
+    const std::vector<int> rows = bf.interior();
+    std::vector<float> M((size_t)rows.size() * nf);
+    auto pres = [&](int c0, int q) -> double { return c0 == 0 ? 0.0 : B[(size_t)(c0 - 1) * nf + q]; };
+    for (size_t r = 0; r < rows.size(); r++) {
+        const int fidx = rows[r];
+        int ca, cb;  // gradient p(cb) - p(ca)
+        if (fidx < s * s * (s + 1)) {
+            const int i = fidx % (s + 1), j = (fidx / (s + 1)) % s, k = fidx / (s * (s + 1));
+            ca = cell(i - 1, j, k);
+            cb = cell(i, j, k);
+        } else if (fidx < 2 * s * s * (s + 1)) {
+            const int x = fidx - s * s * (s + 1);
+            const int i = x % s, j = (x / s) % (s + 1), k = x / (s * (s + 1));
+            ca = cell(i, j - 1, k);
+            cb = cell(i, j, k);
+        } else {
+            const int x = fidx - 2 * s * s * (s + 1);
+            const int i = x % s, j = (x / s) % s, k = x / (s * s);
+            ca = cell(i, j, k - 1);
+            cb = cell(i, j, k);
+        }
+        for (int q = 0; q < nf; q++) {
+            const double v = (q == fidx ? 1.0 : 0.0) - (pres(cb, q) - pres(ca, q));
+            M[r * nf + q] = (float)v;
+        }
+    }
+    return M;
+}
+
+/* The closed least-squares projection of one block with occupied cells
+ * (ZQ_SolveSubGrid3D, Utils3D:1393-1521): A = Laplacian of the free cells
+ * (weight 1 between free neighbours inside the block), the first free cell
+ * (scan order) pinned; min |A p - div| over the other free cells by CG on the
+ * normal equations (double; the reference uses PCG to 1e-12), pressures rounded
+ * to float, interior faces between two free cells corrected by -(p_b - p_a). */
+template <class R>
+void block_solve(int s, const uint8_t* bocc, const std::vector<R>& in, std::vector<R>& out) {
+    const int n = s * s * s;
+    BlockFaces bf(s);
+    auto cell = [&](int i, int j, int k) { return (k * s + j) * s + i; };
+    int first = -1;
+    for (int c0 = 0; c0 < n; c0++)
+        if (!bocc[c0]) {
+            first = c0;
+            break;
+        }
+    out = in;
+    if (first < 0) return;
+    std::vector<double> b(n, 0.0);
+    for (int k = 0; k < s; k++)
+        for (int j = 0; j < s; j++)
+            for (int i = 0; i < s; i++) {
+                const int c0 = cell(i, j, k);
+                if (bocc[c0]) continue;
+                const R dv = ((((in[bf.uix(i + 1, j, k)] - in[bf.uix(i, j, k)]) + in[bf.vix(i, j + 1, k)]) -
+                               in[bf.vix(i, j, k)]) + in[bf.wix(i, j, k + 1)]) - in[bf.wix(i, j, k)];
+                b[c0] = (double)dv;
+            }
+    auto applyA = [&](const std::vector<double>& x, std::vector<double>& y) {
+        for (int k = 0; k < s; k++)
+            for (int j = 0; j < s; j++)
+                for (int i = 0; i < s; i++) {
+                    const int c0 = cell(i, j, k);
+                    if (bocc[c0]) {
+                        y[c0] = 0.0;
+                        continue;
+                    }
+                    double acc = 0.0;
+                    int cnt = 0;
+                    const int di[6] = {0, 0, 0, 0, -1, 1}, dj[6] = {0, 0, -1, 1, 0, 0}, dk[6] = {-1, 1, 0, 0, 0, 0};
+                    for (int q = 0; q < 6; q++) {
+                        const int a = i + di[q], bb = j + dj[q], e = k + dk[q];
+                        if (a < 0 || a >= s || bb < 0 || bb >= s || e < 0 || e >= s) continue;
+                        const int nb = cell(a, bb, e);
+                        if (bocc[nb]) continue;
+                        acc += x[nb];
+                        cnt++;
+                    }
+                    y[c0] = acc - (double)cnt * x[c0];
+                }
+    };
+    /* normal equations in p with p[first] = 0: N p = A (A p), b' = A b, both
+     * with the pinned and occupied entries zeroed */
+    auto mask = [&](std::vector<double>& x) {
+        for (int c0 = 0; c0 < n; c0++)
+            if (bocc[c0] || c0 == first) x[c0] = 0.0;
+    };
+    std::vector<double> x(n, 0.0), r(n), pdir(n), t(n), q(n);
+    applyA(b, r);
+    mask(r);
+    pdir = r;
+    double rr = 0.0;
+    for (int c0 = 0; c0 < n; c0++) rr += r[c0] * r[c0];
+    const double rr0 = rr;
+    const int maxit = 2 * (n + bf.nf + 1);
+    for (int it = 0; it < maxit && rr > 1e-24 * rr0 && rr > 0.0; it++) {
+        applyA(pdir, t);
+        applyA(t, q);
+        mask(q);
+        double pq = 0.0;
+        for (int c0 = 0; c0 < n; c0++) pq += pdir[c0] * q[c0];
+        if (!(pq > 0.0)) break;
+        const double alpha = rr / pq;
+        double rn = 0.0;
+        for (int c0 = 0; c0 < n; c0++) {
+            x[c0] += alpha * pdir[c0];
+            r[c0] -= alpha * q[c0];
+            rn += r[c0] * r[c0];
+        }
+        const double beta = rn / rr;
+        rr = rn;
+        for (int c0 = 0; c0 < n; c0++) pdir[c0] = r[c0] + beta * pdir[c0];
+    }
+    std::vector<R> p(n);
+    for (int c0 = 0; c0 < n; c0++) p[c0] = (R)x[c0];
+    for (int k = 0; k < s; k++)
+        for (int j = 0; j < s; j++)
+            for (int i = 1; i < s; i++)
+                if (!bocc[cell(i, j, k)] && !bocc[cell(i - 1, j, k)]) {
+                    const R d = -(p[cell(i, j, k)] - p[cell(i - 1, j, k)]);
+                    out[bf.uix(i, j, k)] = in[bf.uix(i, j, k)] + d;
+                }
+    for (int k = 0; k < s; k++)
+        for (int j = 1; j < s; j++)
+            for (int i = 0; i < s; i++)
+                if (!bocc[cell(i, j, k)] && !bocc[cell(i, j - 1, k)]) {
+                    const R d = -(p[cell(i, j, k)] - p[cell(i, j - 1, k)]);
+                    out[bf.vix(i, j, k)] = in[bf.vix(i, j, k)] + d;
+                }
+    for (int k = 1; k < s; k++)
+        for (int j = 0; j < s; j++)
+            for (int i = 0; i < s; i++)
+                if (!bocc[cell(i, j, k)] && !bocc[cell(i, j, k - 1)]) {
+                    const R d = -(p[cell(i, j, k)] - p[cell(i, j, k - 1)]);
+                    out[bf.wix(i, j, k)] = in[bf.wix(i, j, k)] + d;
+                }
+}
+
+template <class R>
+void sub_projection(const Dims& f, int s, const uint8_t* occ, const std::vector<float>& M, R* u, R* v, R* w) {
+    BlockFaces bf(s);
+    const std::vector<int> rows = bf.interior();
+    const int cW = f.W / s, cH = f.H / s, cD = f.D / s;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int K = 0; K < cD; K++)
+        for (int J = 0; J < cH; J++)
+            for (int I = 0; I < cW; I++) {
+                const int x0 = I * s, y0 = J * s, z0 = K * s;
+                std::vector<R> in(bf.nf), out;
+                std::vector<uint8_t> bocc(s * s * s);
+                bool any = false;
+                for (int k = 0; k < s; k++)
+                    for (int j = 0; j < s; j++)
+                        for (int i = 0; i < s; i++) {
+                            const uint8_t o = occ[f.cell(x0 + i, y0 + j, z0 + k)] ? 1 : 0;
+                            bocc[(k * s + j) * s + i] = o;
+                            any = any || o;
+                        }
+                for (int k = 0; k < s; k++)
+                    for (int j = 0; j < s; j++)
+                        for (int i = 0; i <= s; i++) in[bf.uix(i, j, k)] = u[f.uix(x0 + i, y0 + j, z0 + k)];
+                for (int k = 0; k < s; k++)
+                    for (int j = 0; j <= s; j++)
+                        for (int i = 0; i < s; i++) in[bf.vix(i, j, k)] = v[f.vix(x0 + i, y0 + j, z0 + k)];
+                for (int k = 0; k <= s; k++)
+                    for (int j = 0; j < s; j++)
+                        for (int i = 0; i < s; i++) in[bf.wix(i, j, k)] = w[f.wix(x0 + i, y0 + j, z0 + k)];
+                if (!any) {
+                    out = in;
+                    for (size_t r = 0; r < rows.size(); r++) {
+                        R acc = R(0);
+                        const float* mr = &M[r * bf.nf];
+                        for (int q = 0; q < bf.nf; q++) acc = acc + (R)mr[q] * in[q];
+                        out[rows[r]] = acc;
+                    }
+                } else {
+                    block_solve(s, bocc.data(), in, out);
+                }
+                for (int k = 0; k < s; k++)
+                    for (int j = 0; j < s; j++)
+                        for (int i = 1; i < s; i++) u[f.uix(x0 + i, y0 + j, z0 + k)] = out[bf.uix(i, j, k)];
+                for (int k = 0; k < s; k++)
+                    for (int j = 1; j < s; j++)
+                        for (int i = 0; i < s; i++) v[f.vix(x0 + i, y0 + j, z0 + k)] = out[bf.vix(i, j, k)];
+                for (int k = 1; k < s; k++)
+                    for (int j = 0; j < s; j++)
+                        for (int i = 0; i < s; i++) w[f.wix(x0 + i, y0 + j, z0 + k)] = out[bf.wix(i, j, k)];
+            }
+}
+
+template <class R>
+int project_coarse(const Dims& d, R* u, R* v, R* w, const uint8_t* occ, const zqs_params& P) {
+    const int s = P.sub_size;
+    if (s < 1 || d.W % s || d.H % s || d.D % s) return ZQS_EINVAL;
+    CoarseGrid<R> g;
+    coarse_init(d, s, occ, g);
+    coarse_correct(d, s, occ, g, u, v, w, P);
+    if (s > 1) {
+        const std::vector<float> M = submatrix(s);
+        sub_projection(d, s, occ, M, u, v, w);
+    }
+    return ZQS_OK;
+}
+
 /* One timestep in the order of ZQ_SmokeSimulation3D::UpdateOneFrame
  * (ZQ_SmokeSimulation3D.cpp:156-243): force, attenuation, velocity advection
  * (always with the open write-back, Utils3D:2163), projection, scalar
@@ -874,7 +1417,12 @@ int step(const Dims& d, R* u, R* v, R* w, R* T, R* rho, const uint8_t* occ, cons
     attenuate(d, u, v, w, T, rho, occ, P);
     int rc = advect_velocity(d, u, v, w, occ, P, P.adv_vel_mode, true);
     if (rc) return rc;
-    project(d, u, v, w, occ, P, p_out, (R*)nullptr, (zqs_stats*)nullptr);
+    if (P.solver == ZQS_SOLVER_COARSE_OPEN) {
+        rc = project_coarse(d, u, v, w, occ, P);
+        if (rc) return rc;
+    } else {
+        project(d, u, v, w, occ, P, p_out, (R*)nullptr, (zqs_stats*)nullptr);
+    }
     rc = advect_scalar(d, u, v, w, occ, T, rho, T, rho, P, P.adv_sca_mode);
     if (rc) return rc;
     reinject(d, T, rho, P);
@@ -1511,6 +2059,15 @@ int control_loss(const Dims& d, const R* u, const R* v, const R* w, const R* T, 
 
 #define ZQO_API extern "C" __attribute__((visibility("default")))
 
+/* The sub-projection matrix of block edge s: rows (3 s^2 (s-1)) x cols (3 s^2 (s+1)) floats. */
+ZQO_API int zqo_submatrix(int s, float* out, int cap) {
+    if (s < 2) return -1;
+    const std::vector<float> M = zqo::submatrix(s);
+    if ((int)M.size() > cap) return -(int)M.size();
+    std::copy(M.begin(), M.end(), out);
+    return (int)M.size();
+}
+
 #define ZQO_DEFINE(SFX, R)                                                                              \
     ZQO_API void zqo_mac_to_regular4_##SFX(int W, int H, int D, const R* u, const R* v, const R* w,     \
                                            R* vel4) {                                                   \
@@ -1543,6 +2100,10 @@ int control_loss(const Dims& d, const R* u, const R* v, const R* w, const R* T, 
     ZQO_API void zqo_project_##SFX(int W, int H, int D, R* u, R* v, R* w, const uint8_t* occ,           \
                                    const zqs_params* P, R* p_out, R* div_out, zqs_stats* st) {          \
         zqo::project<R>(zqo::Dims{W, H, D}, u, v, w, occ, *P, p_out, div_out, st);                      \
+    }                                                                                                   \
+    ZQO_API int zqo_project_coarse_##SFX(int W, int H, int D, R* u, R* v, R* w, const uint8_t* occ,     \
+                                         const zqs_params* P) {                                         \
+        return zqo::project_coarse<R>(zqo::Dims{W, H, D}, u, v, w, occ, *P);                            \
     }                                                                                                   \
     ZQO_API void zqo_reinject_##SFX(int W, int H, int D, R* T, R* rho, const zqs_params* P) {           \
         zqo::reinject<R>(zqo::Dims{W, H, D}, T, rho, *P);                                               \

@@ -1,0 +1,103 @@
+"""Known answers of the oracle's coarse-grid projection (no GPU).
+
+ZQS_SOLVER_COARSE_OPEN restates ZQ_TotalProjection3D for the coarse SOR
+solvers (Utils3D:3688-3794): face-ratio SOR on the grid coarsened by s, the
+correction mapped back to the fine faces, then an exact projection inside
+every s^3 block (dense matrix of ZQ_InitSubMatPoisson3D for blocks without
+obstacles, a least-squares solve for the others).
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+from zq_smokesimulation_gb300 import capi
+from zq_smokesimulation_gb300 import workloads as wl
+
+
+def block_faces(s):
+    """Block face index helpers in the matrix column order (u, v, w)."""
+    nu = s * s * (s + 1)
+    uix = lambda i, j, k: (k * s + j) * (s + 1) + i
+    vix = lambda i, j, k: nu + (k * (s + 1) + j) * s + i
+    wix = lambda i, j, k: 2 * nu + (k * s + j) * s + i
+    rows = ([uix(i, j, k) for k in range(s) for j in range(s) for i in range(1, s)] +
+            [vix(i, j, k) for k in range(s) for j in range(1, s) for i in range(s)] +
+            [wix(i, j, k) for k in range(1, s) for j in range(s) for i in range(s)])
+    return uix, vix, wix, rows
+
+
+def block_div(x, s):
+    uix, vix, wix, _ = block_faces(s)
+    return np.array([[[(x[uix(i + 1, j, k)] - x[uix(i, j, k)]) + (x[vix(i, j + 1, k)] - x[vix(i, j, k)]) +
+                       (x[wix(i, j, k + 1)] - x[wix(i, j, k)]) for i in range(s)] for j in range(s)]
+                     for k in range(s)])
+
+
+@pytest.mark.parametrize("s", [2, 3, 4])
+def test_submatrix_keeps_uniform_flow(oracle32, s):
+    M = oracle32.submatrix(s).astype(np.float64)
+    uix, vix, wix, rows = block_faces(s)
+    x = np.zeros(M.shape[1])
+    nu = s * s * (s + 1)
+    x[:nu], x[nu:2 * nu], x[2 * nu:] = 0.3, -0.7, 1.1
+    np.testing.assert_allclose(M @ x, x[rows], rtol=0, atol=1e-6)
+
+
+@pytest.mark.parametrize("s", [2, 4])
+def test_submatrix_leaves_the_mean_divergence(oracle32, s):
+    """The block least-squares projection leaves div = mean(div) in every cell
+    (the residual of the pinned Neumann problem is the constant component)."""
+    M = oracle32.submatrix(s).astype(np.float64)
+    _, _, _, rows = block_faces(s)
+    x = np.random.default_rng(3).standard_normal(M.shape[1])
+    y = x.copy()
+    y[rows] = M @ x
+    d0, d1 = block_div(x, s), block_div(y, s)
+    np.testing.assert_allclose(d1, np.full_like(d1, d0.mean()), atol=2e-5 * np.abs(d0).max())
+
+
+def coarse_case(W, H, D, s, K, seed=5, walls=True, omega=1.5):
+    occ = wl.walls_open_top(W, H, D) if walls else np.zeros((D, H, W), np.uint8)
+    p = wl.smoke_params(W, K, omega=omega, solver=capi.SOLVER_COARSE_OPEN)
+    p.sub_size = s
+    u, v, w = wl.initial_velocity(occ, seed, amp=1.0)
+    return occ, p, {"u": u.copy(), "v": v.copy(), "w": w.copy()}
+
+
+def max_div(st, occ):
+    u, v, w = st["u"].astype(np.float64), st["v"].astype(np.float64), st["w"].astype(np.float64)
+    d = (u[:, :, 1:] - u[:, :, :-1]) + (v[:, 1:, :] - v[:, :-1, :]) + (w[1:, :, :] - w[:-1, :, :])
+    return float(np.abs(d[occ == 0]).max())
+
+
+def test_coarse_s1_matches_the_fine_open_sor(oracle32):
+    """With s = 1 the coarse grid is the fine grid (ratios 0/1) and the same
+    SOR runs; only the correction is formed as u + ((u - g) - u)."""
+    occ, p, st = coarse_case(12, 10, 9, 1, K=30)
+    ref = {k: a.copy() for k, a in st.items()}
+    p_open = p.copy()
+    p_open.solver = capi.SOLVER_OPEN
+    oracle32.project(12, 10, 9, ref, occ, p_open)
+    assert oracle32.project_coarse(12, 10, 9, st, occ, p) == 0
+    for k in ("u", "v", "w"):
+        assert rel_l2(st[k], ref[k]) < 1e-6, k
+
+
+@pytest.mark.parametrize("walls", [False, True])
+def test_coarse_projection_removes_divergence(oracle32, walls):
+    """Without obstacles the result is divergence-free to rounding.  With walls
+    the coarse system of ZQ_InitMatOpenPoisson3D gives every domain face weight
+    1 whatever its un-occupancy ratio, while the correction moves only the free
+    fine faces, so blocks at the walls keep a residual (a property of the
+    formulation, as restated)."""
+    occ, p, st = coarse_case(16, 16, 16, 4, K=400, walls=walls)
+    before = max_div(st, occ)
+    assert oracle32.project_coarse(16, 16, 16, st, occ, p) == 0
+    after = max_div(st, occ)
+    assert after < (0.05 if walls else 1e-4) * before, (before, after)
+
+
+def test_coarse_rejects_sizes_not_divisible(oracle32):
+    occ, p, st = coarse_case(12, 12, 12, 4, K=2)
+    p.sub_size = 5
+    assert oracle32.project_coarse(12, 12, 12, st, occ, p) == capi.ZQS_EINVAL

@@ -19,7 +19,7 @@ ZQS_OK, ZQS_EINVAL, ZQS_ENOMEM, ZQS_EUNSUPPORTED, ZQS_ETIMEOUT, ZQS_ECUDA, ZQS_E
 STATUS_NAMES = {0: "ZQS_OK", 1: "ZQS_EINVAL", 2: "ZQS_ENOMEM", 3: "ZQS_EUNSUPPORTED", 4: "ZQS_ETIMEOUT",
                 5: "ZQS_ECUDA", 6: "ZQS_ENOTREADY"}
 
-SOLVER_OPEN, SOLVER_CLOSED = 0, 1
+SOLVER_OPEN, SOLVER_CLOSED, SOLVER_COARSE_OPEN = 0, 1, 2
 # ZQ_CUDA_Advection3D.h:7-21 numbering
 ADV_VEL_INREG_OUTREG, ADV_VEL_INREG_OUTREG_BFECC, ADV_VEL_INMAC_OUTMAC, ADV_VEL_INMAC_OUTMAC_BFECC, \
     ADV_VEL_INREG_OUTMAC, ADV_VEL_INREG_OUTMAC_BFECC = range(6)
@@ -43,7 +43,7 @@ class Params(C.Structure):
                 ("vel_atten", C.c_float), ("temp_atten", C.c_float), ("dens_atten", C.c_float),
                 ("solver", C.c_int32), ("sor_iters", C.c_int32), ("omega", C.c_float),
                 ("adv_vel_mode", C.c_int32), ("adv_sca_mode", C.c_int32), ("backtrace_full", C.c_int32),
-                ("n_sources", C.c_int32), ("sources", Source * MAX_SOURCES)]
+                ("n_sources", C.c_int32), ("sources", Source * MAX_SOURCES), ("sub_size", C.c_int32)]
 
     def copy(self) -> "Params":
         p = Params()

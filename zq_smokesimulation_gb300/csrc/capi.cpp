@@ -196,6 +196,7 @@ ZQS_API void zqs_params_default(zqs_params* p, int W, int H, int D) {
     p->adv_vel_mode = ZQS_ADV_VEL_INMAC_OUTMAC;
     p->adv_sca_mode = ZQS_ADV_SCA_MAC;
     p->backtrace_full = 0;
+    p->sub_size = 4;  // Utils3D:18 (subSize)
     p->n_sources = 1;
     zqs_source& s = p->sources[0];  // Utils3D:31-40, unit coordinates times W/H/D in float
     s.shape = ZQS_SOURCE_BOX;
