@@ -1,0 +1,110 @@
+"""GPU parity of the coarse-grid projection (ZQS_SOLVER_COARSE_OPEN) against
+the oracle's restatement of ZQ_TotalProjection3D (Utils3D:3688-3794).
+
+The coarse stages (ratios, fine->coarse map, face-ratio SOR, correction) and
+the dense block matrix are bit-identical to the oracle; blocks with obstacles
+are solved by CG in double on both sides with different reduction orders, so
+the comparison carries a floating-point tolerance (relative L2 1e-6).
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+from zq_smokesimulation_gb300 import capi
+from zq_smokesimulation_gb300 import workloads as wl
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-6
+
+
+def case(W, H, D, s, K, obstacle=True, walls=True, seed=9):
+    occ = wl.walls_open_top(W, H, D) if walls else np.zeros((D, H, W), np.uint8)
+    if obstacle:
+        wl.add_box(occ, W // 3, W // 3 + 2, H // 2, H // 2 + 1, D // 3, D // 2)
+    p = wl.smoke_params(W, K, omega=1.5, solver=capi.SOLVER_COARSE_OPEN)
+    p.sub_size = s
+    u, v, w = wl.initial_velocity(occ, seed, amp=1.0)
+    T = np.zeros((D, H, W), np.float32)
+    return occ, p, u, v, w, T
+
+
+def gpu_project(W, H, D, occ, p, u, v, w, T):
+    g = capi.Grid(W, H, D)
+    g.set_params(p)
+    g.load_state(occ, u, v, w, T, T)
+    g.project()
+    out = {"u": g.download(capi.FIELD_U), "v": g.download(capi.FIELD_V), "w": g.download(capi.FIELD_W)}
+    st = g.stats()
+    g.close()
+    return out, st
+
+
+@pytest.mark.parametrize("s", [1, 2, 4])
+@pytest.mark.parametrize("obstacle", [False, True])
+def test_coarse_projection_matches_oracle(zqs_lib, oracle32, s, obstacle):
+    W, H, D = 16, 12, 8
+    occ, p, u, v, w, T = case(W, H, D, s, K=30, obstacle=obstacle)
+    out, _ = gpu_project(W, H, D, occ, p, u, v, w, T)
+    ref = {"u": u.copy(), "v": v.copy(), "w": w.copy()}
+    assert oracle32.project_coarse(W, H, D, ref, occ, p) == 0
+    for k in ("u", "v", "w"):
+        e = rel_l2(out[k], ref[k])
+        assert e <= TOL, (k, e)
+        if s == 1:   # no block solves: the whole path is bit-identical
+            assert np.array_equal(out[k], ref[k]), k
+
+
+def test_coarse_fast_blocks_bit_identical(zqs_lib, oracle32):
+    """No obstacle anywhere: every block takes the dense matrix, so GPU and
+    oracle agree bit for bit (same matrix, same summation order)."""
+    W, H, D = 16, 16, 8
+    occ, p, u, v, w, T = case(W, H, D, 4, K=20, obstacle=False, walls=False)
+    out, _ = gpu_project(W, H, D, occ, p, u, v, w, T)
+    ref = {"u": u.copy(), "v": v.copy(), "w": w.copy()}
+    oracle32.project_coarse(W, H, D, ref, occ, p)
+    for k in ("u", "v", "w"):
+        assert np.array_equal(out[k], ref[k]), (k, rel_l2(out[k], ref[k]))
+
+
+def test_coarse_projection_removes_divergence(zqs_lib):
+    W, H, D = 32, 32, 32
+    occ, p, u, v, w, T = case(W, H, D, 4, K=300, obstacle=False, walls=False)
+    g = capi.Grid(W, H, D)
+    g.set_params(p)
+    g.load_state(occ, u, v, w, T, T)
+    before = g.stats().max_abs_div
+    g.project()
+    after = g.stats().max_abs_div
+    g.close()
+    assert after < 1e-4 * before, (before, after)
+
+
+def test_coarse_steps_match_oracle(zqs_lib, oracle32):
+    W, H, D = 16, 16, 16
+    w0 = wl.small_case(W, H, D, K=20, vel_amp=0.3)
+    w0.params.solver = capi.SOLVER_COARSE_OPEN
+    w0.params.sub_size = 4
+    g = capi.Grid(W, H, D)
+    g.set_params(w0.params)
+    g.load_state(w0.occ, w0.u, w0.v, w0.w, w0.T, w0.rho)
+    g.step(3)
+    out = g.state()
+    st = oracle32.state(w0)
+    rc, _ = oracle32.step(W, H, D, st, w0.occ, w0.params, 3)
+    assert rc == 0
+    for k in ("u", "v", "w", "T", "rho"):
+        assert rel_l2(out[k], st[k]) <= 1e-5, k
+    g.close()
+
+
+def test_coarse_parameter_checks(zqs_lib):
+    g = capi.Grid(12, 12, 12)
+    p = wl.smoke_params(12, 5, solver=capi.SOLVER_COARSE_OPEN)
+    p.sub_size = 5
+    with pytest.raises(capi.ZQSError) as e:
+        g.set_params(p)
+    assert e.value.code == capi.ZQS_EINVAL
+    p.sub_size = 3
+    g.set_params(p)
+    g.close()

@@ -198,6 +198,10 @@ ZQS_API int zqs_adjoint_create(zqs_adjoint** out, zqs_grid* g, int nsteps, int c
         set_error("zqs_adjoint_create: the reverse mode needs MAC velocity and MAC scalar advection");
         return ZQS_EUNSUPPORTED;
     }
+    if (g->params.solver == ZQS_SOLVER_COARSE_OPEN) {
+        set_error("zqs_adjoint_create: the reverse mode covers the fine-grid SOR solvers only");
+        return ZQS_EUNSUPPORTED;
+    }
     if (g->params.substeps > kAdjMaxSubsteps) {
         set_error("zqs_adjoint_create: at most 32 backtrace substeps are supported");
         return ZQS_EUNSUPPORTED;

@@ -67,6 +67,10 @@ int check_members(zqs_batch* b) {
                       " must use ZQS_ADV_VEL_INMAC_OUTMAC and ZQS_ADV_SCA_MAC advection");
             return ZQS_EUNSUPPORTED;
         }
+        if (g->params.solver == ZQS_SOLVER_COARSE_OPEN) {
+            set_error("zqs_batch: member " + std::to_string(i) + " uses the coarse-grid solver (not batched)");
+            return ZQS_EUNSUPPORTED;
+        }
         if (g->params.sor_iters != b->grids[0]->params.sor_iters) {
             set_error("zqs_batch: every member must use the same sor_iters");
             return ZQS_EUNSUPPORTED;

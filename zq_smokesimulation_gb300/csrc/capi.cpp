@@ -14,6 +14,7 @@
 #include <string>
 #include <utility>
 
+#include "zqs_coarse.h"
 #include "zqs_grid.h"
 
 namespace zqs {
@@ -75,8 +76,8 @@ int validate_params(const zqs_params& p) {
         set_error("sor_iters must be >= 0");
         return ZQS_EINVAL;
     }
-    if (p.solver != ZQS_SOLVER_OPEN && p.solver != ZQS_SOLVER_CLOSED) {
-        set_error("solver must be ZQS_SOLVER_OPEN or ZQS_SOLVER_CLOSED");
+    if (p.solver != ZQS_SOLVER_OPEN && p.solver != ZQS_SOLVER_CLOSED && p.solver != ZQS_SOLVER_COARSE_OPEN) {
+        set_error("solver must be ZQS_SOLVER_OPEN, ZQS_SOLVER_CLOSED or ZQS_SOLVER_COARSE_OPEN");
         return ZQS_EINVAL;
     }
     if (p.adv_vel_mode < 0 || p.adv_vel_mode > 5 || p.adv_sca_mode < 0 || p.adv_sca_mode > 3) {
@@ -314,6 +315,7 @@ ZQS_API int zqs_grid_destroy(zqs_grid* g) {
     cudaStreamDestroy(g->own);
     cudaFree(g->occ_dense);
     cudaFree(g->base);
+    coarse_free(g->g.coarse);
     if (g->fext_base) cudaFree(g->fext_base);
     delete g;
     return ZQS_OK;
@@ -343,6 +345,12 @@ ZQS_API int zqs_grid_set_params(zqs_grid* g, const zqs_params* p) {
     }
     int rc = validate_params(*p);
     if (rc) return rc;
+    if (p->solver == ZQS_SOLVER_COARSE_OPEN) {
+        rc = coarse_prepare(g->g.coarse, g->g.L, p->sub_size);
+        if (rc) return rc;
+    } else {
+        coarse_free(g->g.coarse);
+    }
     bool solver_changed = !g->has_params || g->params.solver != p->solver;
     g->params = *p;
     make_kparams(*p, g->kp);

@@ -1,0 +1,662 @@
+// Coarse-grid projection on the device (ZQS_SOLVER_COARSE_OPEN): the restated
+// ZQ_TotalProjection3D for COARSE_{OPEN,CLOSED}_POISSON_SOR (Utils3D:3688-3794).
+//
+//   k_coarse_ratios    face un-occupancy ratios (ZQ_InitCoarseGrid3D, Utils3D:1666-1888)
+//   k_coarse_cells     coarse occupancy (all six ratios 0) and per-block obstacle flags
+//   k_coarse_diag      diagonal of the face-ratio system (ZQ_InitMatOpenPoisson3D,
+//                      Utils3D:476-601: domain faces weight 1, free neighbours their ratio)
+//   k_fine2coarse      coarse face = mean of its fine faces (Utils3D:2170-2258)
+//   k_coarse_div / k_coarse_sor   red-black SOR of the coarse system
+//   k_coarse_delta     (u - grad p) - u on faces with ratio > 0 (Utils3D:2611-2642, 2794-2866)
+//   k_coarse2fine      the delta added to free fine faces (Utils3D:3172-3296)
+//   k_subproj_gather / k_subproj_fast / k_subproj_obstacle
+//                      exact projection inside every s^3 block (Utils3D:3298-3685):
+//                      dense matrix for obstacle-free blocks, CG in double on the
+//                      least-squares problem of ZQ_SolveSubGrid3D (Utils3D:1393-1521)
+//                      for the others.
+// Every expression follows the oracle's order (oracle/zqs_oracle.cpp,
+// project_coarse); the least-squares CG reduces in a fixed tree order and so
+// agrees with the oracle's sequential CG to rounding, not bit for bit.
+#include <algorithm>
+#include <map>
+#include <mutex>
+
+#include "zqs_coarse.h"
+
+namespace zqs {
+
+namespace {
+
+__device__ __forceinline__ bool fine_occ(const Layout& L, const uint8_t* __restrict__ flags, int x, int y, int z) {
+    return (__ldg(flags + lidx(L, x, y, z)) & F_FREE) == 0;
+}
+
+// One thread per coarse face index (i <= cW, j <= cH, k <= cD), three components.
+__global__ void k_coarse_ratios(Layout L, Layout Lc, int s, const uint8_t* __restrict__ flags,
+                                float* __restrict__ ru, float* __restrict__ rv, float* __restrict__ rw) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i > Lc.W || j > Lc.H || k > Lc.D) return;
+    const int c = lidx(Lc, i, j, k);
+    const float area = (float)(s * s);
+    if (j < Lc.H && k < Lc.D) {
+        int n = 0;
+        for (int sk = 0; sk < s; sk++)
+            for (int sj = 0; sj < s; sj++) {
+                const int y = j * s + sj, z = k * s + sk;
+                bool o;
+                if (i == 0) o = fine_occ(L, flags, 0, y, z);
+                else if (i == Lc.W) o = fine_occ(L, flags, L.W - 1, y, z);
+                else o = fine_occ(L, flags, i * s, y, z) || fine_occ(L, flags, i * s - 1, y, z);
+                n += o ? 1 : 0;
+            }
+        ru[c] = 1.0f - (float)n / area;
+    }
+    if (i < Lc.W && k < Lc.D) {
+        int n = 0;
+        for (int sk = 0; sk < s; sk++)
+            for (int si = 0; si < s; si++) {
+                const int x = i * s + si, z = k * s + sk;
+                bool o;
+                if (j == 0) o = fine_occ(L, flags, x, 0, z);
+                else if (j == Lc.H) o = fine_occ(L, flags, x, L.H - 1, z);
+                else o = fine_occ(L, flags, x, j * s, z) || fine_occ(L, flags, x, j * s - 1, z);
+                n += o ? 1 : 0;
+            }
+        rv[c] = 1.0f - (float)n / area;
+    }
+    if (i < Lc.W && j < Lc.H) {
+        int n = 0;
+        for (int sj = 0; sj < s; sj++)
+            for (int si = 0; si < s; si++) {
+                const int x = i * s + si, y = j * s + sj;
+                bool o;
+                if (k == 0) o = fine_occ(L, flags, x, y, 0);
+                else if (k == Lc.D) o = fine_occ(L, flags, x, y, L.D - 1);
+                else o = fine_occ(L, flags, x, y, k * s) || fine_occ(L, flags, x, y, k * s - 1);
+                n += o ? 1 : 0;
+            }
+        rw[c] = 1.0f - (float)n / area;
+    }
+}
+
+// Coarse occupancy and the per-block obstacle flag (dense block index).
+__global__ void k_coarse_cells(Layout L, Layout Lc, int s, const uint8_t* __restrict__ flags,
+                               const float* __restrict__ ru, const float* __restrict__ rv,
+                               const float* __restrict__ rw, uint8_t* __restrict__ occ, uint8_t* __restrict__ bobs) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i >= Lc.W || j >= Lc.H || k >= Lc.D) return;
+    const int c = lidx(Lc, i, j, k);
+    const int px = Lc.px, pl = (int)Lc.plane;
+    occ[c] = (ru[c] == 0.0f && ru[c + 1] == 0.0f && rv[c] == 0.0f && rv[c + px] == 0.0f && rw[c] == 0.0f &&
+              rw[c + pl] == 0.0f)
+                 ? 1
+                 : 0;
+    bool any = false;
+    for (int sk = 0; sk < s && !any; sk++)
+        for (int sj = 0; sj < s && !any; sj++)
+            for (int si = 0; si < s; si++)
+                if (fine_occ(L, flags, i * s + si, j * s + sj, k * s + sk)) {
+                    any = true;
+                    break;
+                }
+    bobs[((size_t)k * Lc.H + j) * Lc.W + i] = any ? 1 : 0;
+}
+
+// Diagonal: the count of domain faces, then the ratios of the faces to free
+// in-domain neighbours in the order z-, z+, y-, y+, x-, x+.
+__global__ void k_coarse_diag(Layout Lc, const float* __restrict__ ru, const float* __restrict__ rv,
+                              const float* __restrict__ rw, const uint8_t* __restrict__ occ,
+                              float* __restrict__ diag) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i >= Lc.W || j >= Lc.H || k >= Lc.D) return;
+    const int c = lidx(Lc, i, j, k);
+    const int px = Lc.px, pl = (int)Lc.plane;
+    float cnt = 0.0f;
+    if (!occ[c]) {
+        const int nin = (k > 0) + (k < Lc.D - 1) + (j > 0) + (j < Lc.H - 1) + (i > 0) + (i < Lc.W - 1);
+        cnt = (float)(6 - nin);
+        if (k > 0 && !occ[c - pl]) cnt += rw[c];
+        if (k < Lc.D - 1 && !occ[c + pl]) cnt += rw[c + pl];
+        if (j > 0 && !occ[c - px]) cnt += rv[c];
+        if (j < Lc.H - 1 && !occ[c + px]) cnt += rv[c + px];
+        if (i > 0 && !occ[c - 1]) cnt += ru[c];
+        if (i < Lc.W - 1 && !occ[c + 1]) cnt += ru[c + 1];
+    }
+    diag[c] = cnt;
+}
+
+// Coarse face = (sum of its s x s fine faces, outer loop first) / s^2.
+__global__ void k_fine2coarse(Layout L, Layout Lc, int s, const float* __restrict__ u, const float* __restrict__ v,
+                              const float* __restrict__ w, float* __restrict__ cu, float* __restrict__ cv,
+                              float* __restrict__ cw) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i > Lc.W || j > Lc.H || k > Lc.D) return;
+    const int c = lidx(Lc, i, j, k);
+    const float area = (float)(s * s);
+    if (j < Lc.H && k < Lc.D) {
+        float sum = 0.0f;
+        for (int sk = 0; sk < s; sk++)
+            for (int sj = 0; sj < s; sj++) sum += __ldg(u + lidx(L, i * s, j * s + sj, k * s + sk));
+        cu[c] = sum / area;
+    }
+    if (i < Lc.W && k < Lc.D) {
+        float sum = 0.0f;
+        for (int sk = 0; sk < s; sk++)
+            for (int si = 0; si < s; si++) sum += __ldg(v + lidx(L, i * s + si, j * s, k * s + sk));
+        cv[c] = sum / area;
+    }
+    if (i < Lc.W && j < Lc.H) {
+        float sum = 0.0f;
+        for (int sj = 0; sj < s; sj++)
+            for (int si = 0; si < s; si++) sum += __ldg(w + lidx(L, i * s + si, j * s + sj, k * s));
+        cw[c] = sum / area;
+    }
+}
+
+__global__ void k_coarse_div(Layout Lc, const float* __restrict__ cu, const float* __restrict__ cv,
+                             const float* __restrict__ cw, const uint8_t* __restrict__ occ, float* __restrict__ div,
+                             float* __restrict__ p) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i >= Lc.W || j >= Lc.H || k >= Lc.D) return;
+    const int c = lidx(Lc, i, j, k);
+    const int px = Lc.px, pl = (int)Lc.plane;
+    div[c] = occ[c] ? 0.0f : ((((cu[c + 1] - cu[c]) + cv[c + px]) - cv[c]) + cw[c + pl]) - cw[c];
+    p[c] = 0.0f;  // cold start every projection
+}
+
+// One colour of the face-ratio SOR: s = ((rx- px- + rx+ px+) + (ry- py- + ry+ py+))
+// + (rz- pz- + rz+ pz+) over free in-domain neighbours (+0 otherwise), then
+// p = fma(omega/diag, s - div, (1-omega) p).
+__global__ void k_coarse_sor(Layout Lc, const float* __restrict__ ru, const float* __restrict__ rv,
+                             const float* __restrict__ rw, const uint8_t* __restrict__ occ,
+                             const float* __restrict__ diag, const float* __restrict__ div, float* __restrict__ p,
+                             int colour, float omega, float om1) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i >= Lc.W || j >= Lc.H || k >= Lc.D) return;
+    if (((i + j + k) & 1) != colour) return;
+    const int c = lidx(Lc, i, j, k);
+    if (occ[c] || diag[c] == 0.0f) return;
+    const int px = Lc.px, pl = (int)Lc.plane;
+    const float xm = (i > 0 && !occ[c - 1]) ? ru[c] * p[c - 1] : 0.0f;
+    const float xp = (i < Lc.W - 1 && !occ[c + 1]) ? ru[c + 1] * p[c + 1] : 0.0f;
+    const float ym = (j > 0 && !occ[c - px]) ? rv[c] * p[c - px] : 0.0f;
+    const float yp = (j < Lc.H - 1 && !occ[c + px]) ? rv[c + px] * p[c + px] : 0.0f;
+    const float zm = (k > 0 && !occ[c - pl]) ? rw[c] * p[c - pl] : 0.0f;
+    const float zp = (k < Lc.D - 1 && !occ[c + pl]) ? rw[c + pl] * p[c + pl] : 0.0f;
+    const float sum = ((xm + xp) + (ym + yp)) + (zm + zp);
+    const float wc = omega / diag[c];
+    p[c] = __fmaf_rn(wc, sum - div[c], om1 * p[c]);
+}
+
+// delta = (u - g) - u with g = p_R - p_L (p = 0 outside the domain) on faces
+// whose ratio is > 0, else 0.
+__global__ void k_coarse_delta(Layout Lc, const float* __restrict__ ru, const float* __restrict__ rv,
+                               const float* __restrict__ rw, const float* __restrict__ cu,
+                               const float* __restrict__ cv, const float* __restrict__ cw,
+                               const float* __restrict__ p, float* __restrict__ du, float* __restrict__ dv,
+                               float* __restrict__ dw) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i > Lc.W || j > Lc.H || k > Lc.D) return;
+    const int c = lidx(Lc, i, j, k);
+    const int px = Lc.px, pl = (int)Lc.plane;
+    const float zero = 0.0f;
+    if (j < Lc.H && k < Lc.D) {
+        float d = 0.0f;
+        if (ru[c] > 0.0f) {
+            const float g = i == 0 ? p[c] - zero : (i == Lc.W ? zero - p[c - 1] : p[c] - p[c - 1]);
+            d = (cu[c] - g) - cu[c];
+        }
+        du[c] = d;
+    }
+    if (i < Lc.W && k < Lc.D) {
+        float d = 0.0f;
+        if (rv[c] > 0.0f) {
+            const float g = j == 0 ? p[c] - zero : (j == Lc.H ? zero - p[c - px] : p[c] - p[c - px]);
+            d = (cv[c] - g) - cv[c];
+        }
+        dv[c] = d;
+    }
+    if (i < Lc.W && j < Lc.H) {
+        float d = 0.0f;
+        if (rw[c] > 0.0f) {
+            const float g = k == 0 ? p[c] - zero : (k == Lc.D ? zero - p[c - pl] : p[c] - p[c - pl]);
+            d = (cw[c] - g) - cw[c];
+        }
+        dw[c] = d;
+    }
+}
+
+// One thread per fine face index; faces on coarse face planes whose fine
+// cells are free take the delta of their coarse face (the x = W face tests the
+// inside cell x = W-1).
+__global__ void k_coarse2fine(Layout L, Layout Lc, int s, const uint8_t* __restrict__ flags,
+                              const float* __restrict__ du, const float* __restrict__ dv,
+                              const float* __restrict__ dw, float* __restrict__ u, float* __restrict__ v,
+                              float* __restrict__ w) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i > L.W || j > L.H || k > L.D) return;
+    const int c = lidx(L, i, j, k);
+    if (j < L.H && k < L.D && i % s == 0) {
+        bool ok;
+        if (i == 0) ok = !fine_occ(L, flags, 0, j, k);
+        else if (i == L.W) ok = !fine_occ(L, flags, L.W - 1, j, k);
+        else ok = !fine_occ(L, flags, i, j, k) && !fine_occ(L, flags, i - 1, j, k);
+        if (ok) u[c] = u[c] + __ldg(du + lidx(Lc, i / s, j / s, k / s));
+    }
+    if (i < L.W && k < L.D && j % s == 0) {
+        bool ok;
+        if (j == 0) ok = !fine_occ(L, flags, i, 0, k);
+        else if (j == L.H) ok = !fine_occ(L, flags, i, L.H - 1, k);
+        else ok = !fine_occ(L, flags, i, j, k) && !fine_occ(L, flags, i, j - 1, k);
+        if (ok) v[c] = v[c] + __ldg(dv + lidx(Lc, i / s, j / s, k / s));
+    }
+    if (i < L.W && j < L.H && k % s == 0) {
+        bool ok;
+        if (k == 0) ok = !fine_occ(L, flags, i, j, 0);
+        else if (k == L.D) ok = !fine_occ(L, flags, i, j, L.D - 1);
+        else ok = !fine_occ(L, flags, i, j, k) && !fine_occ(L, flags, i, j, k - 1);
+        if (ok) w[c] = w[c] + __ldg(dw + lidx(Lc, i / s, j / s, k / s));
+    }
+}
+
+// Block face q (u: k, j, i <= s; v: k, j <= s, i; w: k <= s, j, i) of block
+// (bi, bj, bk) -> the fine face's padded index and component.
+__device__ __forceinline__ int block_face(const Layout& L, int s, int q, int bi, int bj, int bk, int& comp) {
+    const int nu = s * s * (s + 1);
+    int i, j, k;
+    if (q < nu) {
+        comp = 0;
+        i = q % (s + 1);
+        j = (q / (s + 1)) % s;
+        k = q / (s * (s + 1));
+    } else if (q < 2 * nu) {
+        comp = 1;
+        const int x = q - nu;
+        i = x % s;
+        j = (x / s) % (s + 1);
+        k = x / (s * (s + 1));
+    } else {
+        comp = 2;
+        const int x = q - 2 * nu;
+        i = x % s;
+        j = (x / s) % s;
+        k = x / (s * s);
+    }
+    return lidx(L, bi * s + i, bj * s + j, bk * s + k);
+}
+
+// Interior row r (u: k, j, i = 1..s-1; v: k, j = 1..s-1, i; w: k = 1..s-1, j, i)
+// -> block face index.
+__device__ __forceinline__ int interior_face(int s, int r) {
+    const int nu = s * s * (s + 1);
+    const int ni = s * s * (s - 1);
+    if (r < ni) {
+        const int i = 1 + r % (s - 1), j = (r / (s - 1)) % s, k = r / ((s - 1) * s);
+        return (k * s + j) * (s + 1) + i;
+    }
+    if (r < 2 * ni) {
+        const int x = r - ni;
+        const int i = x % s, j = 1 + (x / s) % (s - 1), k = x / (s * (s - 1));
+        return nu + (k * (s + 1) + j) * s + i;
+    }
+    const int x = r - 2 * ni;
+    const int i = x % s, j = (x / s) % s, k = 1 + x / (s * s);
+    return 2 * nu + (k * s + j) * s + i;
+}
+
+__device__ __forceinline__ float* comp_ptr(int comp, float* u, float* v, float* w) {
+    return comp == 0 ? u : (comp == 1 ? v : w);
+}
+
+// X[b * nf + q] = block face q of block b.
+__global__ void k_subproj_gather(Layout L, Layout Lc, int s, int nf, long long total, const float* __restrict__ u,
+                                 const float* __restrict__ v, const float* __restrict__ w, float* __restrict__ X) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= total) return;
+    const int b = (int)(e / nf), q = (int)(e - (long long)b * nf);
+    const int bi = b % Lc.W, bj = (b / Lc.W) % Lc.H, bk = b / (Lc.W * Lc.H);
+    int comp;
+    const int c = block_face(L, s, q, bi, bj, bk, comp);
+    X[e] = __ldg((comp == 0 ? u : (comp == 1 ? v : w)) + c);
+}
+
+constexpr int kFastRows = 256;   // rows per CTA (one per thread)
+constexpr int kFastBlocks = 16;  // blocks per CTA
+
+// Obstacle-free blocks: interior row r of block b = sum_q M[r][q] X[b][q] in q
+// order (separately rounded products and sums, from 0), written to the fine face.
+__global__ void __launch_bounds__(kFastRows) k_subproj_fast(Layout L, Layout Lc, int s, int nf, int rows,
+                                                            int nblocks, const float* __restrict__ MT,
+                                                            const float* __restrict__ X,
+                                                            const uint8_t* __restrict__ bobs, float* __restrict__ u,
+                                                            float* __restrict__ v, float* __restrict__ w) {
+    extern __shared__ float xs[];  // [kFastBlocks][nf]
+    const int b0 = blockIdx.y * kFastBlocks;
+    const int nb = min(kFastBlocks, nblocks - b0);
+    for (int e = threadIdx.x; e < nb * nf; e += blockDim.x) xs[e] = __ldg(X + (size_t)b0 * nf + e);
+    __syncthreads();
+    const int r = blockIdx.x * kFastRows + threadIdx.x;
+    if (r >= rows) return;
+    float acc[kFastBlocks];
+#pragma unroll
+    for (int b = 0; b < kFastBlocks; b++) acc[b] = 0.0f;
+    for (int q = 0; q < nf; q++) {
+        const float m = __ldg(MT + (size_t)q * rows + r);
+#pragma unroll
+        for (int b = 0; b < kFastBlocks; b++) acc[b] = __fadd_rn(acc[b], __fmul_rn(m, xs[b * nf + q]));
+    }
+    const int f = interior_face(s, r);
+#pragma unroll
+    for (int b = 0; b < kFastBlocks; b++) {
+        if (b >= nb) break;
+        const int gb = b0 + b;
+        if (bobs[gb]) continue;
+        const int bi = gb % Lc.W, bj = (gb / Lc.W) % Lc.H, bk = gb / (Lc.W * Lc.H);
+        int comp;
+        const int c = block_face(L, s, f, bi, bj, bk, comp);
+        comp_ptr(comp, u, v, w)[c] = acc[b];
+    }
+}
+
+// Blocks with an occupied fine cell: min |A p - div| with the first free cell
+// pinned, A the Laplacian of the block's free cells (weight 1 between free
+// neighbours); CG in double on the normal equations, one thread per cell.
+constexpr int kMaxBlockCells = 1024;
+
+__device__ double block_sum(double x, double* red) {
+    const int t = threadIdx.x;
+    red[t] = x;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {  // blockDim.x is a power of two
+        if (t < o) red[t] += red[t + o];
+        __syncthreads();
+    }
+    const double r = red[0];
+    __syncthreads();
+    return r;
+}
+
+__global__ void k_subproj_obstacle(Layout L, Layout Lc, int s, int nf, const uint8_t* __restrict__ flags,
+                                   const float* __restrict__ X, const uint8_t* __restrict__ bobs,
+                                   float* __restrict__ u, float* __restrict__ v, float* __restrict__ w) {
+    const int b = blockIdx.x;
+    if (!bobs[b]) return;
+    extern __shared__ double sm[];
+    const int nthr = blockDim.x;
+    double* xv = sm;             // [nthr] solution
+    double* rv = xv + nthr;      // residual
+    double* pd = rv + nthr;      // direction
+    double* tv = pd + nthr;      // A p
+    double* red = tv + nthr;     // reduction scratch
+    __shared__ int first_s;
+    const int n = s * s * s;
+    const int c = threadIdx.x;
+    const int bi = b % Lc.W, bj = (b / Lc.W) % Lc.H, bk = b / (Lc.W * Lc.H);
+    const int ci = c % s, cj = (c / s) % s, ck = c / (s * s);
+    const bool in = c < n;
+    const bool occ = in ? fine_occ(L, flags, bi * s + ci, bj * s + cj, bk * s + ck) : true;
+    if (c == 0) first_s = n;
+    __syncthreads();
+    if (in && !occ) atomicMin(&first_s, c);
+    __syncthreads();
+    const int first = first_s;
+    const float* xb = X + (size_t)b * nf;
+    const int nu = s * s * (s + 1);
+    auto fu = [&](int i, int j, int k) { return (k * s + j) * (s + 1) + i; };
+    auto fv = [&](int i, int j, int k) { return nu + (k * (s + 1) + j) * s + i; };
+    auto fw = [&](int i, int j, int k) { return 2 * nu + (k * s + j) * s + i; };
+    // right-hand side: the float divergence of the free cell
+    double bval = 0.0;
+    if (in && !occ) {
+        const float dvg = ((((__ldg(xb + fu(ci + 1, cj, ck)) - __ldg(xb + fu(ci, cj, ck))) + __ldg(xb + fv(ci, cj + 1, ck))) -
+                            __ldg(xb + fv(ci, cj, ck))) + __ldg(xb + fw(ci, cj, ck + 1))) - __ldg(xb + fw(ci, cj, ck));
+        bval = (double)dvg;
+    }
+    const bool pinned = !in || occ || c == first;
+    // y = A x for this thread's cell (neighbours in the order z-, z+, y-, y+, x-, x+)
+    auto applyA = [&](const double* x) -> double {
+        if (!in || occ) return 0.0;
+        double acc = 0.0;
+        int cnt = 0;
+        const int dk[6] = {-1, 1, 0, 0, 0, 0}, dj[6] = {0, 0, -1, 1, 0, 0}, di[6] = {0, 0, 0, 0, -1, 1};
+        for (int q = 0; q < 6; q++) {
+            const int a = ci + di[q], bb = cj + dj[q], e = ck + dk[q];
+            if (a < 0 || a >= s || bb < 0 || bb >= s || e < 0 || e >= s) continue;
+            const int nbc = (e * s + bb) * s + a;
+            if (fine_occ(L, flags, bi * s + a, bj * s + bb, bk * s + e)) continue;
+            acc += x[nbc];
+            cnt++;
+        }
+        return acc - (double)cnt * x[c];
+    };
+    // r0 = A b (masked), p0 = r0, x0 = 0
+    tv[c] = bval;
+    xv[c] = 0.0;
+    __syncthreads();
+    double r = pinned ? 0.0 : applyA(tv);
+    rv[c] = r;
+    pd[c] = r;
+    __syncthreads();
+    double rr = block_sum(r * r, red);
+    const double rr0 = rr;
+    const int maxit = 2 * (n + nf + 1);
+    for (int it = 0; it < maxit && rr > 1e-24 * rr0 && rr > 0.0; it++) {
+        tv[c] = applyA(pd);
+        __syncthreads();
+        const double q = pinned ? 0.0 : applyA(tv);
+        const double pq = block_sum(pd[c] * q, red);
+        if (!(pq > 0.0)) break;
+        const double alpha = rr / pq;
+        xv[c] += alpha * pd[c];
+        const double rn_c = rv[c] - alpha * q;
+        rv[c] = rn_c;
+        const double rn = block_sum(rn_c * rn_c, red);
+        const double beta = rn / rr;
+        rr = rn;
+        pd[c] = rn_c + beta * pd[c];
+        __syncthreads();
+    }
+    // pressures to float, then the interior faces between free cells
+    float* pf = reinterpret_cast<float*>(red);  // reuse: [nthr] floats
+    pf[c] = (float)xv[c];
+    __syncthreads();
+    if (!in || occ) return;
+    auto put = [&](int q, int comp, int lo) {
+        const float d = -(pf[c] - pf[lo]);
+        const int fc = lidx(L, bi * s + ci, bj * s + cj, bk * s + ck);
+        comp_ptr(comp, u, v, w)[fc] = __ldg(xb + q) + d;
+    };
+    if (ci > 0 && !fine_occ(L, flags, bi * s + ci - 1, bj * s + cj, bk * s + ck)) put(fu(ci, cj, ck), 0, c - 1);
+    if (cj > 0 && !fine_occ(L, flags, bi * s + ci, bj * s + cj - 1, bk * s + ck)) put(fv(ci, cj, ck), 1, c - s);
+    if (ck > 0 && !fine_occ(L, flags, bi * s + ci, bj * s + cj, bk * s + ck - 1)) put(fw(ci, cj, ck), 2, c - s * s);
+}
+
+// The sub-projection matrix per block edge, transposed on the device, shared by
+// every grid of the process.
+std::mutex g_mt_mu;
+std::map<int, float*> g_mt;
+
+int get_mt(int s, const float** out) {
+    std::lock_guard<std::mutex> lk(g_mt_mu);
+    auto it = g_mt.find(s);
+    if (it != g_mt.end()) {
+        *out = it->second;
+        return ZQS_OK;
+    }
+    const std::vector<float> M = coarse_submatrix(s);
+    const int nf = 3 * s * s * (s + 1), rows = 3 * s * s * (s - 1);
+    std::vector<float> MT((size_t)nf * rows);
+    for (int r = 0; r < rows; r++)
+        for (int q = 0; q < nf; q++) MT[(size_t)q * rows + r] = M[(size_t)r * nf + q];
+    float* d = nullptr;
+    ZQS_CUDA_TRY(cudaMalloc(&d, MT.size() * sizeof(float)));
+    cudaError_t e = cudaMemcpy(d, MT.data(), MT.size() * sizeof(float), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(d);
+        return cuda_fail(e, "coarse sub-projection matrix upload");
+    }
+    g_mt[s] = d;
+    *out = d;
+    return ZQS_OK;
+}
+
+Layout coarse_layout(int W, int H, int D) {
+    Layout L;
+    L.W = W;
+    L.H = H;
+    L.D = D;
+    L.px = ((W + 1) + 3) / 4 * 4;
+    L.py = H + 1;
+    L.pz = D + 1;
+    L.plane = (long long)L.px * L.py;
+    L.elems = L.plane * (L.pz + 2);
+    return L;
+}
+
+}  // namespace
+
+int coarse_prepare(CoarseState*& cs, const Layout& L, int s) {
+    if (s < 1 || L.W % s || L.H % s || L.D % s) {
+        set_error("sub_size must be >= 1 and divide the grid's width, height and depth");
+        return ZQS_EINVAL;
+    }
+    if (s * s * s > kMaxBlockCells) {
+        set_error("sub_size must be at most 10 (one thread per block cell)");
+        return ZQS_EINVAL;
+    }
+    if (cs && cs->s == s && cs->Lc.W == L.W / s && cs->Lc.H == L.H / s && cs->Lc.D == L.D / s) return ZQS_OK;
+    // the fast kernel's dynamic shared memory exceeds the 48 KB default for s > 4
+    ZQS_CUDA_TRY(cudaFuncSetAttribute(k_subproj_fast, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      kFastBlocks * 3 * 10 * 10 * 11 * (int)sizeof(float)));
+    coarse_free(cs);
+    CoarseState* c = new CoarseState();
+    c->s = s;
+    c->Lc = coarse_layout(L.W / s, L.H / s, L.D / s);
+    const Layout& Lc = c->Lc;
+    c->nblocks = Lc.W * Lc.H * Lc.D;
+    c->nf = 3 * s * s * (s + 1);
+    c->rows = 3 * s * s * (s - 1);
+    const size_t fb = (size_t)Lc.elems * 4;
+    const size_t ob = ((size_t)Lc.elems + 255) / 256 * 256;
+    const size_t bb = ((size_t)c->nblocks + 255) / 256 * 256;
+    const size_t xb = s > 1 ? (size_t)c->nblocks * c->nf * 4 : 0;
+    const size_t total = 12 * fb + ob + bb + xb;
+    cudaError_t e = cudaMalloc(&c->base, total);
+    if (e != cudaSuccess) {
+        delete c;
+        return cuda_fail(e, "coarse state allocation");
+    }
+    e = cudaMemset(c->base, 0, total);
+    if (e != cudaSuccess) {
+        cudaFree(c->base);
+        delete c;
+        return cuda_fail(e, "coarse state clear");
+    }
+    char* b = (char*)c->base;
+    auto take = [&]() -> float* {
+        float* p = (float*)b + Lc.plane;
+        b += fb;
+        return p;
+    };
+    c->ru = take();
+    c->rv = take();
+    c->rw = take();
+    c->cu = take();
+    c->cv = take();
+    c->cw = take();
+    c->du = take();
+    c->dv = take();
+    c->dw = take();
+    c->div = take();
+    c->diag = take();
+    c->p = take();
+    c->occ = (uint8_t*)b + Lc.plane;
+    b += ob;
+    c->bobs = (uint8_t*)b;
+    b += bb;
+    c->X = s > 1 ? (float*)b : nullptr;
+    if (s > 1) {
+        int rc = get_mt(s, &c->MT);
+        if (rc) {
+            cudaFree(c->base);
+            delete c;
+            return rc;
+        }
+    }
+    cs = c;
+    return ZQS_OK;
+}
+
+void coarse_free(CoarseState*& cs) {
+    if (!cs) return;
+    cudaFree(cs->base);
+    delete cs;
+    cs = nullptr;
+}
+
+int launch_project_coarse(DevGrid& g, const KParams& kp, int K, cudaStream_t st, LaunchCounter& lc) {
+    CoarseState* cs = g.coarse;
+    if (!cs) {
+        set_error("coarse projection: the grid has no coarse state (set the parameters first)");
+        return ZQS_ENOTREADY;
+    }
+    const Layout& L = g.L;
+    const Layout& Lc = cs->Lc;
+    const int s = cs->s;
+    dim3 b(32, 8, 1);
+    const dim3 gcf((Lc.W + 1 + 31) / 32, (Lc.H + 1 + 7) / 8, Lc.D + 1);  // coarse face box
+    const dim3 gcc((Lc.W + 31) / 32, (Lc.H + 7) / 8, Lc.D);               // coarse cells
+    const dim3 gff((L.W + 1 + 31) / 32, (L.H + 1 + 7) / 8, L.D + 1);      // fine face box
+    k_coarse_ratios<<<gcf, b, 0, st>>>(L, Lc, s, g.flags, cs->ru, cs->rv, cs->rw);
+    k_coarse_cells<<<gcc, b, 0, st>>>(L, Lc, s, g.flags, cs->ru, cs->rv, cs->rw, cs->occ, cs->bobs);
+    k_coarse_diag<<<gcc, b, 0, st>>>(Lc, cs->ru, cs->rv, cs->rw, cs->occ, cs->diag);
+    k_fine2coarse<<<gcf, b, 0, st>>>(L, Lc, s, g.u, g.v, g.w, cs->cu, cs->cv, cs->cw);
+    k_coarse_div<<<gcc, b, 0, st>>>(Lc, cs->cu, cs->cv, cs->cw, cs->occ, cs->div, cs->p);
+    lc.n += 5;
+    for (int it = 0; it < K; it++)
+        for (int colour = 0; colour < 2; colour++) {
+            k_coarse_sor<<<gcc, b, 0, st>>>(Lc, cs->ru, cs->rv, cs->rw, cs->occ, cs->diag, cs->div, cs->p, colour,
+                                            kp.omega, kp.om1);
+            lc.n++;
+        }
+    k_coarse_delta<<<gcf, b, 0, st>>>(Lc, cs->ru, cs->rv, cs->rw, cs->cu, cs->cv, cs->cw, cs->p, cs->du, cs->dv,
+                                      cs->dw);
+    k_coarse2fine<<<gff, b, 0, st>>>(L, Lc, s, g.flags, cs->du, cs->dv, cs->dw, g.u, g.v, g.w);
+    lc.n += 2;
+    ZQS_LAUNCH_CHECK("coarse correction");
+    if (s > 1) {
+        const long long total = (long long)cs->nblocks * cs->nf;
+        k_subproj_gather<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(L, Lc, s, cs->nf, total, g.u, g.v, g.w,
+                                                                            cs->X);
+        const dim3 gf((cs->rows + kFastRows - 1) / kFastRows, (cs->nblocks + kFastBlocks - 1) / kFastBlocks, 1);
+        const size_t smf = (size_t)kFastBlocks * cs->nf * sizeof(float);
+        k_subproj_fast<<<gf, kFastRows, smf, st>>>(L, Lc, s, cs->nf, cs->rows, cs->nblocks, cs->MT, cs->X, cs->bobs,
+                                                   g.u, g.v, g.w);
+        int nthr = 32;
+        while (nthr < s * s * s) nthr <<= 1;
+        const size_t smo = (size_t)5 * nthr * sizeof(double);
+        k_subproj_obstacle<<<cs->nblocks, nthr, smo, st>>>(L, Lc, s, cs->nf, g.flags, cs->X, cs->bobs, g.u, g.v,
+                                                           g.w);
+        lc.n += 3;
+        ZQS_LAUNCH_CHECK("block sub-projection");
+    }
+    return ZQS_OK;
+}
+
+}  // namespace zqs

@@ -152,7 +152,7 @@ int launch_dense_reg4_to_mac(int W, int H, int D, const float4* vel4, float* u, 
 int launch_build_flags(const DevGrid& g, const uint8_t* occ_dense, int solver, cudaStream_t s, LaunchCounter& lc) {
     const Layout& L = g.L;
     dim3 b(32, 8, 1), gr((L.px + 31) / 32, (L.py + 7) / 8, L.pz);
-    k_build_flags<<<gr, b, 0, s>>>(L, occ_dense, g.flags, solver == ZQS_SOLVER_OPEN ? 1 : 0);
+    k_build_flags<<<gr, b, 0, s>>>(L, occ_dense, g.flags, solver != ZQS_SOLVER_CLOSED ? 1 : 0);
     lc.n++;
     ZQS_LAUNCH_CHECK("k_build_flags");
     return ZQS_OK;

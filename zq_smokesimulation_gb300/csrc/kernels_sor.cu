@@ -28,6 +28,7 @@
 //                 right sweep.  Results equal S/2 iterations of k_sor_colour.
 #include "zqs_adjoint.h"
 #include "zqs_batch.h"
+#include "zqs_coarse.h"
 
 #include <algorithm>
 #include <vector>
@@ -1031,6 +1032,14 @@ int launch_project(DevGrid& g, const KParams& kp, int K, const SorConfig& cfg, c
                    float** p_final) {
     const Layout& L = g.L;
     dim3 b(32, 8, 1);
+    if (kp.solver == ZQS_SOLVER_COARSE_OPEN) {
+        // no fine pressure or right-hand side: both read back as zero
+        ZQS_CUDA_TRY(cudaMemsetAsync(g.p - L.plane, 0, (size_t)L.elems * sizeof(float), s));
+        ZQS_CUDA_TRY(cudaMemsetAsync(g.div - L.plane, 0, (size_t)L.elems * sizeof(float), s));
+        int rc = launch_project_coarse(g, kp, K, s, lc);
+        if (p_final) *p_final = g.p;
+        return rc;
+    }
     dim3 gc((L.W + 31) / 32, (L.H + 7) / 8, L.D);
     const bool closed = kp.solver == ZQS_SOLVER_CLOSED;
     k_divergence<<<gc, b, 0, s>>>(L, g.u, g.v, g.w, g.flags, g.div, g.p, g.red, closed ? 1 : 0);

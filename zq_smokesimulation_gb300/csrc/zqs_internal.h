@@ -69,6 +69,8 @@ struct SourceList {
 };
 
 // Pointers of one grid's device state.
+struct CoarseState;  // zqs_coarse.h
+
 struct DevGrid {
     Layout L;
     float *u, *v, *w;          // current velocity
@@ -82,6 +84,7 @@ struct DevGrid {
     float4 *qu, *qv, *qw;      // quad copies of the velocity for the MAC sampler (tri0_quad)
     double* red;               // FP64 reduction scratch (the closed-solver mean sits in the last 2)
     long long red_len;
+    CoarseState* coarse = nullptr;  // ZQS_SOLVER_COARSE_OPEN state (owned by the grid handle)
 };
 
 // ---- error reporting -------------------------------------------------------
