@@ -54,6 +54,9 @@ def parse():
     ap.add_argument("--adjoint", default="64,128", help="control-problem sizes timed for the reverse mode ('' or none = skip)")
     ap.add_argument("--adjoint-steps", type=int, default=64)
     ap.add_argument("--checkpoint-every", type=int, default=8)
+    ap.add_argument("--coarse", default="coarse256",
+                    help="coarse-grid projection configuration measured beside the plain step ('' or none = skip)")
+    ap.add_argument("--coarse-steps", type=int, default=5)
     return ap.parse_args()
 
 
@@ -251,6 +254,47 @@ def measure_batch(args, stream, rel_check: bool = True):
             "step_alg_gbs": step_alg / (ms_b / steps * 1e-3) / 1e9}
 
 
+def measure_coarse(args, stream):
+    """The reference's fine256 configuration: COARSE_OPEN_POISSON_SOR with
+    subSize 8 (coarse face-ratio SOR, K iterations on the 32^3 grid, then the
+    block sub-projection), regular-grid advection, the centred sphere obstacle.
+    Full steps through the same C ABI, device-resident, graph-replayed."""
+    import torch
+
+    from zq_smokesimulation_gb300 import capi
+    from zq_smokesimulation_gb300 import workloads as wl
+
+    w = wl.make(args.coarse)
+    sp = stream.cuda_stream
+    g = capi.Grid(w.W, w.H, w.D)
+    g.set_params(w.params)
+    g.load_state(w.occ, w.u, w.v, w.w, w.T, w.rho)
+    g.step(max(3, args.warmup), sp)
+    steps = max(1, args.coarse_steps)
+
+    def timed(fn, reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(stream)
+        for _ in range(reps):
+            fn()
+        b.record(stream)
+        b.synchronize()
+        return a.elapsed_time(b) / reps
+
+    ms = timed(lambda: g.step(1, sp), steps)
+    launches = g.launch_count()
+    g.project(sp)
+    ms_proj = timed(lambda: g.project(sp), 3)
+    mx = g.stats().max_abs_div
+    g.close()
+    return {"workload": args.coarse, "grid": [w.W, w.H, w.D], "sub_size": int(w.params.sub_size),
+            "coarse_grid": [w.W // w.params.sub_size] * 3, "sor_iters": int(w.params.sor_iters),
+            "advection": "inReg_outReg + Reg scalar", "steps": steps, "ms_per_step": ms,
+            "value": w.cells / (ms * 1e-3) / 1e9, "unit": UNIT, "gpu_launches_per_step": launches,
+            "projection_ms": ms_proj, "max_abs_div_after_projection": mx}
+
+
 def measure_adjoint(args, stream, N: int):
     """The force-field control problem at N^3: forward (nsteps steps with the
     control force, checkpoints every k) and backward (recomputation + adjoint
@@ -438,6 +482,9 @@ def run_ours(args):
     batch = None
     if args.batch not in ("", "none") and world == 1:
         batch = measure_batch(args, stream)
+    coarse = None
+    if args.coarse not in ("", "none") and world == 1:
+        coarse = measure_coarse(args, stream)
     adjoint = None
     if args.adjoint not in ("", "none") and world == 1:
         adjoint = {f"control{n}": measure_adjoint(args, stream, int(n)) for n in args.adjoint.split(",") if n}
@@ -471,7 +518,7 @@ def run_ours(args):
                          "step_alg_gbs": step_alg / (ms / args.steps * 1e-3) / 1e9,
                          "step_frac": step_alg / (ms / args.steps * 1e-3) / 1e9 / peak},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches_per_step * args.steps, "clocks": clocks,
-            "batch": batch, "adjoint": adjoint,
+            "batch": batch, "adjoint": adjoint, "coarse": coarse,
         }
         print(json.dumps(line), flush=True)
     g.close()

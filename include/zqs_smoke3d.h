@@ -11,9 +11,10 @@
  * ZQ_SmokeSimulation3D keeps the state on the GPU between frames and copies it
  * back only when the host arrays are asked for (GetFineGrid, exports).
  *
- * Differences, kept as parameters or documented: the projection is always the
- * fine-grid red-black SOR (the coarse, octree and flux solvers of the reference
- * map to the SOR of the same open/closed kind, with a notice); moving objects,
+ * Differences, kept as parameters or documented: the projection is the
+ * fine-grid red-black SOR (TOTAL_*_POISSON_SOR) or the coarse-grid projection
+ * (COARSE_*_POISSON_SOR); the octree, flux and PCG solvers of the reference
+ * map to the fine-grid SOR of the same open/closed kind, with a notice; moving objects,
  * guiding control and the wavelet / compressed export formats are not
  * available (Init or the export returns false). */
 #ifndef ZQS_SMOKE3D_H
@@ -219,6 +220,10 @@ ZQS_CXX_API bool ZQ_Attenuation3D(ZQ_SmokeGrid3D* fineGrid, const ZQ_SmokeSimula
 ZQS_CXX_API bool ZQ_AdvectVelocity3D(ZQ_SmokeGrid3D* fineGrid, const ZQ_SmokeSimulationPara3D& para);
 ZQS_CXX_API bool ZQ_SolveOpenPressure3DSOR(ZQ_SmokeGrid3D* fineGrid, const ZQ_SmokeSimulationPara3D& para);
 ZQS_CXX_API bool ZQ_SolveClosedPressure3DSOR(ZQ_SmokeGrid3D* fineGrid, const ZQ_SmokeSimulationPara3D& para);
+/* The projection the configuration selects (ZQ_TotalProjection3D, Utils3D:3688-3794):
+ * the coarse-grid solver for COARSE_{OPEN,CLOSED}_POISSON_SOR, else the
+ * fine-grid SOR of the same open/closed kind. */
+ZQS_CXX_API bool ZQ_TotalProjection3D(ZQ_SmokeGrid3D* fineGrid, const ZQ_SmokeSimulationPara3D& para);
 ZQS_CXX_API bool ZQ_AdvectScalar3D(ZQ_SmokeGrid3D* fineGrid, const ZQ_SmokeSimulationPara3D& para);
 ZQS_CXX_API bool ZQ_ReinjectTemperatureDensity3D(ZQ_SmokeGrid3D* fineGrid, const ZQ_SmokeSimulationPara3D& para);
 /* One frame through the free functions above (force, attenuation, velocity

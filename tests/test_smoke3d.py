@@ -15,6 +15,7 @@ from pathlib import Path
 import numpy as np
 import pytest
 
+from conftest import rel_l2
 from zq_smokesimulation_gb300 import capi
 from zq_smokesimulation_gb300 import workloads as wl
 
@@ -56,7 +57,7 @@ noiseAmp 0.05
 seed 3
 advVelType inMAC_outMAC
 advScaType MAC
-globalGridSolver COARSE_CLOSED_POISSON_SOR
+globalGridSolver TOTAL_CLOSED_POISSON_SOR
 """
 
 
@@ -128,7 +129,8 @@ def test_reference_config_quirks(driver, tmp_path):
     ok = "resolution 16 16 16\nsubSize 2\nsource 0.5 0.1 0.5 0.1 0.05 0.1 0.8 20\nstep 30\nvelAttenCoeff 10\n"
     out = run_driver(driver, "parse", ok, tmp_path / "q")
     p, occ, _ = load_setup(out, 16, 16, 16)
-    assert p.substeps == 20 and p.sor_iters == 100 and p.solver == capi.SOLVER_OPEN
+    # the reference's default solver is COARSE_OPEN_POISSON_SOR (coarse grid, subSize blocks)
+    assert p.substeps == 20 and p.sor_iters == 100 and p.solver == capi.SOLVER_COARSE_OPEN and p.sub_size == 2
     assert p.vel_atten == np.float32(math.exp(np.float32(-0.01) * np.float32(10.0)))
     assert (p.adv_vel_mode, p.adv_sca_mode) == (capi.ADV_VEL_INREG_OUTREG, capi.ADV_SCA_REG)
     assert not occ.any()  # open solver, no internal object
@@ -155,3 +157,21 @@ def test_resident_and_stage_paths_match_oracle(driver, tmp_path, oracle32):
     for k in ("u", "v", "w", "T", "rho"):
         np.testing.assert_array_equal(fin[k], ref[k])
     assert float(ref["rho"].sum()) > 0.0
+
+
+@pytest.mark.gpu
+def test_coarse_solver_config_matches_oracle(driver, tmp_path, oracle32):
+    """COARSE_CLOSED_POISSON_SOR runs the coarse-grid projection (the open coarse
+    solver, as the reference does); blocks with obstacles are least-squares
+    solves, so the comparison carries a floating-point tolerance."""
+    W, H, D = 24, 20, 16
+    cfg = CONFIG.replace("globalGridSolver TOTAL_CLOSED_POISSON_SOR", "globalGridSolver COARSE_CLOSED_POISSON_SOR")
+    run_out = run_driver(driver, "run", cfg, tmp_path / "run")
+    p, occ, st = load_setup(run_out, W, H, D)
+    assert p.solver == capi.SOLVER_COARSE_OPEN and p.sub_size == 4
+    ref = {k: np.ascontiguousarray(v) for k, v in st.items()}
+    rc, _ = oracle32.step(W, H, D, ref, occ, p, 3)
+    assert rc == 0
+    fin = load_guide(run_out / "final.guidedat", W, H, D)
+    for k in ("u", "v", "w", "T", "rho"):
+        assert rel_l2(fin[k], ref[k]) <= 1e-5, k

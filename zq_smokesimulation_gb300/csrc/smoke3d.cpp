@@ -280,6 +280,11 @@ bool ZQ_SmokeSimulationPara3D::ToParams(zqs_params* p) const {
     p->temp_atten = tempAttenFactor >= 0.0f ? tempAttenFactor : std::exp(-stepTime * tempAttenCoeff);
     p->dens_atten = densityAttenFactor >= 0.0f ? densityAttenFactor : std::exp(-stepTime * densityAttenCoeff);
     p->solver = (is_closed(globalGridSolver) && !wallsExceptTop) ? ZQS_SOLVER_CLOSED : ZQS_SOLVER_OPEN;
+    // both coarse Poisson SOR settings run the open coarse solver, as the
+    // reference's ZQ_TotalProjection3D does (Utils3D:3732-3746)
+    if (globalGridSolver == COARSE_OPEN_POISSON_SOR || globalGridSolver == COARSE_CLOSED_POISSON_SOR)
+        p->solver = ZQS_SOLVER_COARSE_OPEN;
+    p->sub_size = subSize;
     p->sor_iters = maxIter;
     p->omega = omega;
     // the Para enum order differs from the CUDA header's (mapping of ZQ_SmokeSimulationUtils3D.cpp:2124-2148)
@@ -719,6 +724,11 @@ bool ZQ_SolveClosedPressure3DSOR(ZQ_SmokeGrid3D* g, const ZQ_SmokeSimulationPara
     return d ? finish(g, zqs_stage_project(d, nullptr), "ZQ_SolveClosedPressure3DSOR") : false;
 }
 
+bool ZQ_TotalProjection3D(ZQ_SmokeGrid3D* g, const ZQ_SmokeSimulationPara3D& para) {
+    zqs_grid* d = g ? prepare(g, para) : nullptr;
+    return d ? finish(g, zqs_stage_project(d, nullptr), "ZQ_TotalProjection3D") : false;
+}
+
 bool ZQ_AdvectScalar3D(ZQ_SmokeGrid3D* g, const ZQ_SmokeSimulationPara3D& para) {
     zqs_params p;
     if (!para.ToParams(&p)) return false;
@@ -733,8 +743,7 @@ bool ZQ_ReinjectTemperatureDensity3D(ZQ_SmokeGrid3D* g, const ZQ_SmokeSimulation
 
 bool ZQ_UpdateOneFrame3D(ZQ_SmokeGrid3D* g, const ZQ_SmokeSimulationPara3D& para) {
     if (!ZQ_AddForce3D(g, para) || !ZQ_Attenuation3D(g, para) || !ZQ_AdvectVelocity3D(g, para)) return false;
-    const bool closed = is_closed(para.globalGridSolver) && !para.wallsExceptTop;
-    if (!(closed ? ZQ_SolveClosedPressure3DSOR(g, para) : ZQ_SolveOpenPressure3DSOR(g, para))) return false;
+    if (!ZQ_TotalProjection3D(g, para)) return false;
     return ZQ_AdvectScalar3D(g, para) && ZQ_ReinjectTemperatureDensity3D(g, para);
 }
 
@@ -755,7 +764,8 @@ bool ZQ_SmokeSimulation3D::Init(const char* file) {
         return false;
     }
     const GlobalSolverType3D s = para.globalGridSolver;
-    if (s != TOTAL_OPEN_POISSON_SOR && s != TOTAL_CLOSED_POISSON_SOR)
+    if (s != TOTAL_OPEN_POISSON_SOR && s != TOTAL_CLOSED_POISSON_SOR && s != COARSE_OPEN_POISSON_SOR &&
+        s != COARSE_CLOSED_POISSON_SOR)
         printf("note: globalGridSolver %d runs as the fine-grid %s red-black SOR\n", (int)s,
                is_closed(s) && !para.wallsExceptTop ? "closed" : "open");
     delete fineGrid;

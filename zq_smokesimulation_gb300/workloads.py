@@ -193,6 +193,22 @@ def initial_velocity(occ: np.ndarray, seed: int, amp: float = 1e-3):
     return u, v, w
 
 
+def plain_sources(N: int, seed: int) -> list:
+    """Four seeded sphere sources near the floor of an N^3 domain."""
+    rs = uniform(seed + 1000, 4, 8.0, 16.0)
+    src = []
+    for q in range(4):
+        r = float(rs[q])
+        u3 = uniform01(seed + 2000 + q, 5)
+        cx = float(np.float32(r + 1) + np.float32(N - 2 * r - 2) * u3[0])
+        cz = float(np.float32(r + 1) + np.float32(N - 2 * r - 2) * u3[1])
+        cy = float(np.float32(1.0) + np.float32(0.1 * N - 1.0) * u3[2])
+        den = float(np.float32(0.5) + np.float32(0.5) * u3[3])
+        tem = float(np.float32(0.5) + np.float32(0.5) * u3[4])
+        src.append(sphere(cx, cy, cz, r, den, tem))
+    return src
+
+
 def make(name: str, *, K: int | None = None, substeps: int = 20, steps: int | None = None, seed: int = 0,
          vel_mode=capi.ADV_VEL_INMAC_OUTMAC, sca_mode=capi.ADV_SCA_MAC, omega: float = 1.9) -> Workload:
     if name in ("plain64", "plain128_obs"):
@@ -208,23 +224,28 @@ def make(name: str, *, K: int | None = None, substeps: int = 20, steps: int | No
     elif name.startswith("plain") and name[5:].isdigit():
         N = int(name[5:])
         occ = walls_open_top(N, N, N)
-        rs = uniform(seed + 1000, 4, 8.0, 16.0)
-        src = []
-        for q in range(4):
-            r = float(rs[q])
-            u3 = uniform01(seed + 2000 + q, 5)
-            cx = float(np.float32(r + 1) + np.float32(N - 2 * r - 2) * u3[0])
-            cz = float(np.float32(r + 1) + np.float32(N - 2 * r - 2) * u3[1])
-            cy = float(np.float32(1.0) + np.float32(0.1 * N - 1.0) * u3[2])
-            den = float(np.float32(0.5) + np.float32(0.5) * u3[3])
-            tem = float(np.float32(0.5) + np.float32(0.5) * u3[4])
-            src.append(sphere(cx, cy, cz, r, den, tem))
+        src = plain_sources(N, seed)
         Kd, steps_d = 600, 200
+    elif name.startswith("coarse") and name[6:].isdigit():
+        # the reference's fine256 configuration (expsimu3D/fine256.txt): open
+        # domain, the centred sphere obstacle of intObj sphere (Utils3D:1587-1599,
+        # r^2 < N^2/400), COARSE_OPEN_POISSON_SOR with subSize 8, maxIter 600,
+        # regular-grid advection (inReg_outReg, Reg); sources as plainN
+        N = int(name[6:])
+        occ = np.zeros((N, N, N), np.uint8)
+        c = np.arange(N) + 0.5 - N / 2
+        occ[(c[:, None, None] ** 2 + c[None, :, None] ** 2 + c[None, None, :] ** 2) < N * N / 400.0] = 1
+        src = plain_sources(N, seed)
+        Kd, steps_d = 600, 200
+        vel_mode, sca_mode = capi.ADV_VEL_INREG_OUTREG, capi.ADV_SCA_REG
     else:
         raise KeyError(f"unknown workload {name!r}")
     N = occ.shape[0]
     p = smoke_params(N, K if K is not None else Kd, substeps=substeps, omega=omega, vel_mode=vel_mode,
                      sca_mode=sca_mode)
+    if name.startswith("coarse"):
+        p.solver = capi.SOLVER_COARSE_OPEN
+        p.sub_size = 8
     p.set_sources(src)
     u, v, w = initial_velocity(occ, seed)
     T = np.zeros((N, N, N), np.float32)
