@@ -887,7 +887,9 @@ void project(const Dims& d, R* u, R* v, R* w, const uint8_t* occ, const zqs_para
  *   5. with s > 1, an exact projection inside every s^3 block
  *      (ZQ_SubProjection3D, Utils3D:3298-3685): blocks without an occupied fine
  *      cell apply the dense matrix of ZQ_InitSubMatPoisson3D (Utils3D:1151-
- *      1391) to the block's faces; the others solve their closed Poisson
+ *      1391) to the block's faces (products accumulated with fused
+ *      multiply-adds in column order, as a GPU matrix product compiled with
+ *      contraction accumulates); the others solve their closed Poisson
  *      problem (ratio 1 between free cells, first free cell pinned) in the
  *      least-squares sense (ZQ_SolveSubGrid3D, Utils3D:1393-1521), here by CG
  *      on the normal equations in double, and correct the interior faces. */
@@ -1374,7 +1376,7 @@ void sub_projection(const Dims& f, int s, const uint8_t* occ, const std::vector<
                     for (size_t r = 0; r < rows.size(); r++) {
                         R acc = R(0);
                         const float* mr = &M[r * bf.nf];
-                        for (int q = 0; q < bf.nf; q++) acc = acc + (R)mr[q] * in[q];
+                        for (int q = 0; q < bf.nf; q++) acc = std::fma((R)mr[q], in[q], acc);
                         out[rows[r]] = acc;
                     }
                 } else {

@@ -18,6 +18,7 @@
 // project_coarse); the least-squares CG reduces in a fixed tree order and so
 // agrees with the oracle's sequential CG to rounding, not bit for bit.
 #include <algorithm>
+#include <climits>
 #include <map>
 #include <mutex>
 
@@ -336,41 +337,68 @@ __global__ void k_subproj_gather(Layout L, Layout Lc, int s, int nf, long long t
     X[e] = __ldg((comp == 0 ? u : (comp == 1 ? v : w)) + c);
 }
 
-constexpr int kFastRows = 256;   // rows per CTA (one per thread)
+constexpr int kFastRows = 256;   // rows per CTA
 constexpr int kFastBlocks = 16;  // blocks per CTA
+constexpr int kFastThreads = 256;
 
-// Obstacle-free blocks: interior row r of block b = sum_q M[r][q] X[b][q] in q
-// order (separately rounded products and sums, from 0), written to the fine face.
-__global__ void __launch_bounds__(kFastRows) k_subproj_fast(Layout L, Layout Lc, int s, int nf, int rows,
-                                                            int nblocks, const float* __restrict__ MT,
-                                                            const float* __restrict__ X,
-                                                            const uint8_t* __restrict__ bobs, float* __restrict__ u,
-                                                            float* __restrict__ v, float* __restrict__ w) {
+// Obstacle-free blocks: interior row r of block b = sum_q M[r][q] X[b][q],
+// accumulated in q order with fused multiply-adds from 0, written to the fine
+// face.  Thread t computes rows tr + 64 m (m < 4) of blocks 4 tb + n (n < 4),
+// tr = t % 64, tb = t / 64: per q four coalesced loads of the transposed
+// matrix and four broadcast shared loads feed sixteen FMAs.
+__global__ void __launch_bounds__(kFastThreads) k_subproj_fast(Layout L, Layout Lc, int s, int nf, int rows,
+                                                               int nblocks, const float* __restrict__ MT,
+                                                               const float* __restrict__ X,
+                                                               const uint8_t* __restrict__ bobs,
+                                                               float* __restrict__ u, float* __restrict__ v,
+                                                               float* __restrict__ w) {
     extern __shared__ float xs[];  // [kFastBlocks][nf]
     const int b0 = blockIdx.y * kFastBlocks;
     const int nb = min(kFastBlocks, nblocks - b0);
     for (int e = threadIdx.x; e < nb * nf; e += blockDim.x) xs[e] = __ldg(X + (size_t)b0 * nf + e);
+    for (int e = nb * nf + threadIdx.x; e < kFastBlocks * nf; e += blockDim.x) xs[e] = 0.0f;
     __syncthreads();
-    const int r = blockIdx.x * kFastRows + threadIdx.x;
-    if (r >= rows) return;
-    float acc[kFastBlocks];
+    const int tr = threadIdx.x & 63, tb = threadIdx.x >> 6;
+    int r[4];
+    bool rok[4];
 #pragma unroll
-    for (int b = 0; b < kFastBlocks; b++) acc[b] = 0.0f;
-    for (int q = 0; q < nf; q++) {
-        const float m = __ldg(MT + (size_t)q * rows + r);
-#pragma unroll
-        for (int b = 0; b < kFastBlocks; b++) acc[b] = __fadd_rn(acc[b], __fmul_rn(m, xs[b * nf + q]));
+    for (int m = 0; m < 4; m++) {
+        r[m] = blockIdx.x * kFastRows + tr + 64 * m;
+        rok[m] = r[m] < rows;
     }
-    const int f = interior_face(s, r);
+    float acc[4][4];
 #pragma unroll
-    for (int b = 0; b < kFastBlocks; b++) {
-        if (b >= nb) break;
-        const int gb = b0 + b;
-        if (bobs[gb]) continue;
-        const int bi = gb % Lc.W, bj = (gb / Lc.W) % Lc.H, bk = gb / (Lc.W * Lc.H);
-        int comp;
-        const int c = block_face(L, s, f, bi, bj, bk, comp);
-        comp_ptr(comp, u, v, w)[c] = acc[b];
+    for (int m = 0; m < 4; m++)
+#pragma unroll
+        for (int n = 0; n < 4; n++) acc[m][n] = 0.0f;
+    const float* xb = xs + (tb * 4) * nf;
+#pragma unroll 8
+    for (int q = 0; q < nf; q++) {
+        float mv[4], xv[4];
+#pragma unroll
+        for (int m = 0; m < 4; m++) mv[m] = rok[m] ? __ldg(MT + (size_t)q * rows + r[m]) : 0.0f;
+#pragma unroll
+        for (int n = 0; n < 4; n++) xv[n] = xb[n * nf + q];
+#pragma unroll
+        for (int m = 0; m < 4; m++)
+#pragma unroll
+            for (int n = 0; n < 4; n++) acc[m][n] = __fmaf_rn(mv[m], xv[n], acc[m][n]);
+    }
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+        if (!rok[m]) continue;
+        const int f = interior_face(s, r[m]);
+#pragma unroll
+        for (int n = 0; n < 4; n++) {
+            const int b = tb * 4 + n;
+            if (b >= nb) continue;
+            const int gb = b0 + b;
+            if (bobs[gb]) continue;
+            const int bi = gb % Lc.W, bj = (gb / Lc.W) % Lc.H, bk = gb / (Lc.W * Lc.H);
+            int comp;
+            const int c = block_face(L, s, f, bi, bj, bk, comp);
+            comp_ptr(comp, u, v, w)[c] = acc[m][n];
+        }
     }
 }
 
@@ -379,19 +407,57 @@ __global__ void __launch_bounds__(kFastRows) k_subproj_fast(Layout L, Layout Lc,
 // neighbours); CG in double on the normal equations, one thread per cell.
 constexpr int kMaxBlockCells = 1024;
 
+// Sum over the CTA in a fixed order (warp trees, then the warp sums in warp
+// order by the first warp); blockDim.x is a multiple of 32, at most 1024.
 __device__ double block_sum(double x, double* red) {
-    const int t = threadIdx.x;
-    red[t] = x;
+    const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) red[wid] = x;
     __syncthreads();
-    for (int o = blockDim.x / 2; o > 0; o >>= 1) {  // blockDim.x is a power of two
-        if (t < o) red[t] += red[t + o];
-        __syncthreads();
+    if (wid == 0) {
+        const int nw = blockDim.x >> 5;
+        double y = lane < nw ? red[lane] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) y += __shfl_down_sync(0xffffffffu, y, o);
+        if (lane == 0) red[32] = y;
     }
-    const double r = red[0];
+    __syncthreads();
+    const double r = red[32];
     __syncthreads();
     return r;
 }
 
+__device__ int block_min(int x, int* redi) {
+    const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x = min(x, __shfl_down_sync(0xffffffffu, x, o));
+    if (lane == 0) redi[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = blockDim.x >> 5;
+        int y = lane < nw ? redi[lane] : INT_MAX;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) y = min(y, __shfl_down_sync(0xffffffffu, y, o));
+        if (lane == 0) redi[32] = y;
+    }
+    __syncthreads();
+    const int r = redi[32];
+    __syncthreads();
+    return r;
+}
+
+// Blocks with an occupied fine cell (ZQ_SolveSubGrid3D, Utils3D:1393-1521):
+// the least-squares pressure of the block's closed Poisson problem.  The
+// least-squares solutions of A p = b (A the Laplacian of the free cells, weight
+// 1 between free neighbours) are the solutions of A p = b' with b' = b minus
+// its mean over each connected free region, unique up to a constant per
+// region, which the face corrections do not see.  So: label the regions (min
+// cell index, propagated), remove each region's mean (regions in increasing
+// root order, fixed-order sums), then CG on -A p = -b' in double from 0 to a
+// relative residual of 1e-12 (the reference's PCG tolerance), one thread per
+// cell.  Pressures rounded to float; interior faces between free cells get
+// -(p_b - p_a).
 __global__ void k_subproj_obstacle(Layout L, Layout Lc, int s, int nf, const uint8_t* __restrict__ flags,
                                    const float* __restrict__ X, const uint8_t* __restrict__ bobs,
                                    float* __restrict__ u, float* __restrict__ v, float* __restrict__ w) {
@@ -399,92 +465,115 @@ __global__ void k_subproj_obstacle(Layout L, Layout Lc, int s, int nf, const uin
     if (!bobs[b]) return;
     extern __shared__ double sm[];
     const int nthr = blockDim.x;
-    double* xv = sm;             // [nthr] solution
-    double* rv = xv + nthr;      // residual
-    double* pd = rv + nthr;      // direction
-    double* tv = pd + nthr;      // A p
-    double* red = tv + nthr;     // reduction scratch
-    __shared__ int first_s;
+    double* pd = sm;                                      // [nthr] direction
+    double* tv = pd + nthr;                               // [nthr] scratch; pressures as float at the end
+    int* lab = reinterpret_cast<int*>(tv + nthr);         // [nthr] region labels
+    __shared__ double red[33];
+    __shared__ int redi[33];
     const int n = s * s * s;
     const int c = threadIdx.x;
     const int bi = b % Lc.W, bj = (b / Lc.W) % Lc.H, bk = b / (Lc.W * Lc.H);
     const int ci = c % s, cj = (c / s) % s, ck = c / (s * s);
     const bool in = c < n;
     const bool occ = in ? fine_occ(L, flags, bi * s + ci, bj * s + cj, bk * s + ck) : true;
-    if (c == 0) first_s = n;
+    const bool fr = in && !occ;
+    // free in-block neighbours in the order z-, z+, y-, y+, x-, x+ (bit q), their count
+    const int dk[6] = {-1, 1, 0, 0, 0, 0}, dj[6] = {0, 0, -1, 1, 0, 0}, di[6] = {0, 0, 0, 0, -1, 1};
+    const int off[6] = {-s * s, s * s, -s, s, -1, 1};
+    unsigned nbm = 0;
+    int cnt = 0;
+    if (fr) {
+#pragma unroll
+        for (int q = 0; q < 6; q++) {
+            const int a = ci + di[q], bb = cj + dj[q], e = ck + dk[q];
+            if (a < 0 || a >= s || bb < 0 || bb >= s || e < 0 || e >= s) continue;
+            if (fine_occ(L, flags, bi * s + a, bj * s + bb, bk * s + e)) continue;
+            nbm |= 1u << q;
+            cnt++;
+        }
+    }
+    // regions: every free cell takes the smallest index reachable (at most n rounds)
+    lab[c] = fr ? c : INT_MAX;
     __syncthreads();
-    if (in && !occ) atomicMin(&first_s, c);
-    __syncthreads();
-    const int first = first_s;
+    for (int round = 0; round < n; round++) {
+        int m = lab[c];
+        if (fr)
+#pragma unroll
+            for (int q = 0; q < 6; q++)
+                if (nbm & (1u << q)) m = min(m, lab[c + off[q]]);
+        __syncthreads();
+        const bool ch = fr && m < lab[c];
+        if (ch) lab[c] = m;
+        if (!__syncthreads_or(ch)) break;
+    }
     const float* xb = X + (size_t)b * nf;
     const int nu = s * s * (s + 1);
     auto fu = [&](int i, int j, int k) { return (k * s + j) * (s + 1) + i; };
     auto fv = [&](int i, int j, int k) { return nu + (k * (s + 1) + j) * s + i; };
     auto fw = [&](int i, int j, int k) { return 2 * nu + (k * s + j) * s + i; };
-    // right-hand side: the float divergence of the free cell
+    // right-hand side: the float divergence of the free cell, minus its region's mean
     double bval = 0.0;
-    if (in && !occ) {
+    if (fr) {
         const float dvg = ((((__ldg(xb + fu(ci + 1, cj, ck)) - __ldg(xb + fu(ci, cj, ck))) + __ldg(xb + fv(ci, cj + 1, ck))) -
                             __ldg(xb + fv(ci, cj, ck))) + __ldg(xb + fw(ci, cj, ck + 1))) - __ldg(xb + fw(ci, cj, ck));
         bval = (double)dvg;
     }
-    const bool pinned = !in || occ || c == first;
-    // y = A x for this thread's cell (neighbours in the order z-, z+, y-, y+, x-, x+)
-    auto applyA = [&](const double* x) -> double {
-        if (!in || occ) return 0.0;
-        double acc = 0.0;
-        int cnt = 0;
-        const int dk[6] = {-1, 1, 0, 0, 0, 0}, dj[6] = {0, 0, -1, 1, 0, 0}, di[6] = {0, 0, 0, 0, -1, 1};
-        for (int q = 0; q < 6; q++) {
-            const int a = ci + di[q], bb = cj + dj[q], e = ck + dk[q];
-            if (a < 0 || a >= s || bb < 0 || bb >= s || e < 0 || e >= s) continue;
-            const int nbc = (e * s + bb) * s + a;
-            if (fine_occ(L, flags, bi * s + a, bj * s + bb, bk * s + e)) continue;
-            acc += x[nbc];
-            cnt++;
+    double bp = bval;
+    bool done = !fr;
+    for (;;) {
+        const int root = block_min(done ? INT_MAX : lab[c], redi);
+        if (root == INT_MAX) break;
+        const bool mine = fr && lab[c] == root;
+        const double sum = block_sum(mine ? bval : 0.0, red);
+        const double num = block_sum(mine ? 1.0 : 0.0, red);
+        if (mine) {
+            bp = bval - sum / num;
+            done = true;
         }
-        return acc - (double)cnt * x[c];
+    }
+    // CG on -A x = -b'
+    auto applyM = [&](const double* x, double xc) -> double {
+        if (!fr) return 0.0;
+        double acc = 0.0;
+#pragma unroll
+        for (int q = 0; q < 6; q++)
+            if (nbm & (1u << q)) acc += x[c + off[q]];
+        return (double)cnt * xc - acc;
     };
-    // r0 = A b (masked), p0 = r0, x0 = 0
-    tv[c] = bval;
-    xv[c] = 0.0;
+    double xv = 0.0;
+    double rv = -bp;
+    pd[c] = rv;
     __syncthreads();
-    double r = pinned ? 0.0 : applyA(tv);
-    rv[c] = r;
-    pd[c] = r;
-    __syncthreads();
-    double rr = block_sum(r * r, red);
+    double rr = block_sum(rv * rv, red);
     const double rr0 = rr;
     const int maxit = 2 * (n + nf + 1);
     for (int it = 0; it < maxit && rr > 1e-24 * rr0 && rr > 0.0; it++) {
-        tv[c] = applyA(pd);
-        __syncthreads();
-        const double q = pinned ? 0.0 : applyA(tv);
-        const double pq = block_sum(pd[c] * q, red);
-        if (!(pq > 0.0)) break;
-        const double alpha = rr / pq;
-        xv[c] += alpha * pd[c];
-        const double rn_c = rv[c] - alpha * q;
-        rv[c] = rn_c;
-        const double rn = block_sum(rn_c * rn_c, red);
+        const double pc = pd[c];
+        const double t = applyM(pd, pc);
+        const double pt = block_sum(pc * t, red);
+        if (!(pt > 0.0)) break;
+        const double alpha = rr / pt;
+        xv += alpha * pc;
+        rv = rv - alpha * t;
+        const double rn = block_sum(rv * rv, red);
         const double beta = rn / rr;
         rr = rn;
-        pd[c] = rn_c + beta * pd[c];
+        pd[c] = rv + beta * pc;
         __syncthreads();
     }
     // pressures to float, then the interior faces between free cells
-    float* pf = reinterpret_cast<float*>(red);  // reuse: [nthr] floats
-    pf[c] = (float)xv[c];
+    float* pf = reinterpret_cast<float*>(tv);
+    pf[c] = (float)xv;
     __syncthreads();
-    if (!in || occ) return;
+    if (!fr) return;
     auto put = [&](int q, int comp, int lo) {
         const float d = -(pf[c] - pf[lo]);
         const int fc = lidx(L, bi * s + ci, bj * s + cj, bk * s + ck);
         comp_ptr(comp, u, v, w)[fc] = __ldg(xb + q) + d;
     };
-    if (ci > 0 && !fine_occ(L, flags, bi * s + ci - 1, bj * s + cj, bk * s + ck)) put(fu(ci, cj, ck), 0, c - 1);
-    if (cj > 0 && !fine_occ(L, flags, bi * s + ci, bj * s + cj - 1, bk * s + ck)) put(fv(ci, cj, ck), 1, c - s);
-    if (ck > 0 && !fine_occ(L, flags, bi * s + ci, bj * s + cj, bk * s + ck - 1)) put(fw(ci, cj, ck), 2, c - s * s);
+    if (nbm & (1u << 4)) put(fu(ci, cj, ck), 0, c - 1);
+    if (nbm & (1u << 2)) put(fv(ci, cj, ck), 1, c - s);
+    if (nbm & (1u << 0)) put(fw(ci, cj, ck), 2, c - s * s);
 }
 
 // The sub-projection matrix per block edge, transposed on the device, shared by
@@ -646,11 +735,11 @@ int launch_project_coarse(DevGrid& g, const KParams& kp, int K, cudaStream_t st,
                                                                             cs->X);
         const dim3 gf((cs->rows + kFastRows - 1) / kFastRows, (cs->nblocks + kFastBlocks - 1) / kFastBlocks, 1);
         const size_t smf = (size_t)kFastBlocks * cs->nf * sizeof(float);
-        k_subproj_fast<<<gf, kFastRows, smf, st>>>(L, Lc, s, cs->nf, cs->rows, cs->nblocks, cs->MT, cs->X, cs->bobs,
-                                                   g.u, g.v, g.w);
+        k_subproj_fast<<<gf, kFastThreads, smf, st>>>(L, Lc, s, cs->nf, cs->rows, cs->nblocks, cs->MT, cs->X,
+                                                      cs->bobs, g.u, g.v, g.w);
         int nthr = 32;
         while (nthr < s * s * s) nthr <<= 1;
-        const size_t smo = (size_t)5 * nthr * sizeof(double);
+        const size_t smo = (size_t)2 * nthr * sizeof(double) + (size_t)nthr * sizeof(int);
         k_subproj_obstacle<<<cs->nblocks, nthr, smo, st>>>(L, Lc, s, cs->nf, g.flags, cs->X, cs->bobs, g.u, g.v,
                                                            g.w);
         lc.n += 3;
