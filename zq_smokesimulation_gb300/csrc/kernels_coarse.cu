@@ -17,6 +17,8 @@
 // Every expression follows the oracle's order (oracle/zqs_oracle.cpp,
 // project_coarse); the least-squares CG reduces in a fixed tree order and so
 // agrees with the oracle's sequential CG to rounding, not bit for bit.
+#include <cooperative_groups.h>
+
 #include <algorithm>
 #include <climits>
 #include <map>
@@ -199,6 +201,101 @@ __global__ void k_coarse_sor(Layout Lc, const float* __restrict__ ru, const floa
     const float sum = ((xm + xp) + (ym + yp)) + (zm + zp);
     const float wc = omega / diag[c];
     p[c] = __fmaf_rn(wc, sum - div[c], om1 * p[c]);
+}
+
+// All K iterations of the coarse SOR in one launch of one thread-block
+// cluster of kClusterCtas CTAs (small coarse grids): CTA r of the cluster
+// keeps planes [r P, (r+1) P) of p in its shared memory and reads the z
+// neighbours across the slab boundary from the adjacent CTA's shared memory
+// (distributed shared memory); a hardware cluster barrier separates the
+// half-sweeps.  Each thread holds up to kClusterCpt cells with their six
+// weights, neighbour mask, 1/diag weight and divergence in registers.  Same
+// arithmetic as k_coarse_sor (a colour reads only the other colour, so the
+// order of updates inside a half-sweep does not matter): identical results.
+constexpr int kClusterCtas = 8;
+constexpr int kClusterThreads = 1024;
+constexpr int kClusterCpt = 4;
+
+__global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterThreads)
+    k_coarse_sor_cluster(Layout Lc, int P, const float* __restrict__ ru, const float* __restrict__ rv,
+                         const float* __restrict__ rw, const uint8_t* __restrict__ occ,
+                         const float* __restrict__ diag, const float* __restrict__ div, float* __restrict__ pout,
+                         int K, float omega, float om1) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    extern __shared__ float ps[];  // [P][cH][cW] this CTA's planes
+    const int rank = (int)cluster.block_rank();
+    const int W = Lc.W, H = Lc.H, D = Lc.D;
+    const int z0 = rank * P;
+    const int nloc = max(0, min(P, D - z0)) * H * W;
+    for (int e = threadIdx.x; e < P * H * W; e += blockDim.x) ps[e] = 0.0f;
+    float* below = rank > 0 ? cluster.map_shared_rank(ps, rank - 1) : nullptr;   // planes z0-P .. z0-1
+    float* above = rank < kClusterCtas - 1 ? cluster.map_shared_rank(ps, rank + 1) : nullptr;
+    float w6[kClusterCpt][6], wc[kClusterCpt], dv[kClusterCpt];
+    unsigned mk[kClusterCpt];
+    int le[kClusterCpt], col[kClusterCpt];
+#pragma unroll
+    for (int m = 0; m < kClusterCpt; m++) {
+        const int e = threadIdx.x + m * kClusterThreads;
+        le[m] = e;
+        mk[m] = 0;
+        col[m] = -1;
+        wc[m] = 0.0f;
+        dv[m] = 0.0f;
+#pragma unroll
+        for (int q = 0; q < 6; q++) w6[m][q] = 0.0f;
+        if (e >= nloc) continue;
+        const int i = e % W, j = (e / W) % H, k = z0 + e / (W * H);
+        const int c = lidx(Lc, i, j, k);
+        if (occ[c] || diag[c] == 0.0f) continue;
+        const int px = Lc.px, pl = (int)Lc.plane;
+        col[m] = (i + j + k) & 1;
+        // neighbours x-, x+, y-, y+, z-, z+ (bit q) that are in the domain and free
+        if (i > 0 && !occ[c - 1]) mk[m] |= 1u, w6[m][0] = ru[c];
+        if (i < W - 1 && !occ[c + 1]) mk[m] |= 2u, w6[m][1] = ru[c + 1];
+        if (j > 0 && !occ[c - px]) mk[m] |= 4u, w6[m][2] = rv[c];
+        if (j < H - 1 && !occ[c + px]) mk[m] |= 8u, w6[m][3] = rv[c + px];
+        if (k > 0 && !occ[c - pl]) mk[m] |= 16u, w6[m][4] = rw[c];
+        if (k < D - 1 && !occ[c + pl]) mk[m] |= 32u, w6[m][5] = rw[c + pl];
+        wc[m] = omega / diag[c];
+        dv[m] = div[c];
+    }
+    cluster.sync();
+    const int plane = H * W;
+    for (int it = 0; it < K; it++) {
+        for (int colour = 0; colour < 2; colour++) {
+#pragma unroll
+            for (int m = 0; m < kClusterCpt; m++) {
+                if (col[m] != colour) continue;
+                const int e = le[m];
+                const float* pe = ps + e;
+                const int zl = e / plane;
+                const float xm = (mk[m] & 1u) ? w6[m][0] * pe[-1] : 0.0f;
+                const float xp = (mk[m] & 2u) ? w6[m][1] * pe[1] : 0.0f;
+                const float ym = (mk[m] & 4u) ? w6[m][2] * pe[-W] : 0.0f;
+                const float yp = (mk[m] & 8u) ? w6[m][3] * pe[W] : 0.0f;
+                float zm = 0.0f, zp = 0.0f;
+                if (mk[m] & 16u) {
+                    const float pn = zl > 0 ? pe[-plane] : below[e + (P - 1) * plane];
+                    zm = w6[m][4] * pn;
+                }
+                if (mk[m] & 32u) {
+                    const float pn = zl < P - 1 ? pe[plane] : above[e - (P - 1) * plane];
+                    zp = w6[m][5] * pn;
+                }
+                const float sum = ((xm + xp) + (ym + yp)) + (zm + zp);
+                ps[e] = __fmaf_rn(wc[m], sum - dv[m], om1 * ps[e]);
+            }
+            cluster.sync();
+        }
+    }
+#pragma unroll
+    for (int m = 0; m < kClusterCpt; m++) {
+        const int e = le[m];
+        if (e >= nloc) continue;
+        const int i = e % W, j = (e / W) % H, k = z0 + e / (W * H);
+        pout[lidx(Lc, i, j, k)] = ps[e];
+    }
 }
 
 // delta = (u - g) - u with g = p_R - p_L (p = 0 outside the domain) on faces
@@ -718,12 +815,22 @@ int launch_project_coarse(DevGrid& g, const KParams& kp, int K, cudaStream_t st,
     k_fine2coarse<<<gcf, b, 0, st>>>(L, Lc, s, g.u, g.v, g.w, cs->cu, cs->cv, cs->cw);
     k_coarse_div<<<gcc, b, 0, st>>>(Lc, cs->cu, cs->cv, cs->cw, cs->occ, cs->div, cs->p);
     lc.n += 5;
-    for (int it = 0; it < K; it++)
-        for (int colour = 0; colour < 2; colour++) {
-            k_coarse_sor<<<gcc, b, 0, st>>>(Lc, cs->ru, cs->rv, cs->rw, cs->occ, cs->diag, cs->div, cs->p, colour,
-                                            kp.omega, kp.om1);
-            lc.n++;
-        }
+    // small coarse grids: every iteration in one cluster launch; else one launch per colour
+    const int P = (Lc.D + kClusterCtas - 1) / kClusterCtas;
+    if (K > 0 && P * Lc.H * Lc.W <= kClusterThreads * kClusterCpt) {
+        const size_t smc = (size_t)P * Lc.H * Lc.W * sizeof(float);
+        k_coarse_sor_cluster<<<kClusterCtas, kClusterThreads, smc, st>>>(Lc, P, cs->ru, cs->rv, cs->rw, cs->occ,
+                                                                       cs->diag, cs->div, cs->p, K, kp.omega,
+                                                                       kp.om1);
+        lc.n++;
+    } else {
+        for (int it = 0; it < K; it++)
+            for (int colour = 0; colour < 2; colour++) {
+                k_coarse_sor<<<gcc, b, 0, st>>>(Lc, cs->ru, cs->rv, cs->rw, cs->occ, cs->diag, cs->div, cs->p,
+                                                colour, kp.omega, kp.om1);
+                lc.n++;
+            }
+    }
     k_coarse_delta<<<gcf, b, 0, st>>>(Lc, cs->ru, cs->rv, cs->rw, cs->cu, cs->cv, cs->cw, cs->p, cs->du, cs->dv,
                                       cs->dw);
     k_coarse2fine<<<gff, b, 0, st>>>(L, Lc, s, g.flags, cs->du, cs->dv, cs->dw, g.u, g.v, g.w);
