@@ -434,74 +434,103 @@ __global__ void k_subproj_gather(Layout L, Layout Lc, int s, int nf, long long t
     X[e] = __ldg((comp == 0 ? u : (comp == 1 ? v : w)) + c);
 }
 
-constexpr int kFastRows = 256;   // rows per CTA
-constexpr int kFastBlocks = 16;  // blocks per CTA
-constexpr int kFastThreads = 256;
+// Obstacle-free blocks as one matrix product Y = M X (rows x nblocks, inner
+// dimension nf), written to the blocks' interior fine faces.  Tiled SGEMM:
+// a CTA owns a 128-row x 128-block tile; 16-deep slices of M (from its
+// transpose MT[q][r]) and X (X[b][q]) are staged through shared memory, double
+// buffered; thread (tx, ty) accumulates rows 8 ty + i and blocks 8 tx + j
+// (i, j < 8; two 16-byte shared loads each per step) with fused multiply-adds
+// in q order from 0, so every output is the sequential sum of the oracle
+// (padding beyond nf adds exact zeros).
+constexpr int kGemmTile = 128;
+constexpr int kGemmK = 16;
+constexpr int kGemmThreads = 256;
 
-// Obstacle-free blocks: interior row r of block b = sum_q M[r][q] X[b][q],
-// accumulated in q order with fused multiply-adds from 0, written to the fine
-// face.  Thread t computes rows tr + 64 m (m < 4) of blocks 4 tb + n (n < 4),
-// tr = t % 64, tb = t / 64: per q four coalesced loads of the transposed
-// matrix and four broadcast shared loads feed sixteen FMAs.
-__global__ void __launch_bounds__(kFastThreads) k_subproj_fast(Layout L, Layout Lc, int s, int nf, int rows,
+__global__ void __launch_bounds__(kGemmThreads, 2) k_subproj_fast(Layout L, Layout Lc, int s, int nf, int rows,
                                                                int nblocks, const float* __restrict__ MT,
                                                                const float* __restrict__ X,
                                                                const uint8_t* __restrict__ bobs,
                                                                float* __restrict__ u, float* __restrict__ v,
                                                                float* __restrict__ w) {
-    extern __shared__ float xs[];  // [kFastBlocks][nf]
-    const int b0 = blockIdx.y * kFastBlocks;
-    const int nb = min(kFastBlocks, nblocks - b0);
-    for (int e = threadIdx.x; e < nb * nf; e += blockDim.x) xs[e] = __ldg(X + (size_t)b0 * nf + e);
-    for (int e = nb * nf + threadIdx.x; e < kFastBlocks * nf; e += blockDim.x) xs[e] = 0.0f;
+    __shared__ __align__(16) float As[2][kGemmK][kGemmTile];
+    // B rows padded by 4 floats: the transposing stores (16 q of one block per
+    // 16 threads) then spread over 8 banks instead of one
+    __shared__ __align__(16) float Bs[2][kGemmK][kGemmTile + 4];
+    const int t = threadIdx.x;
+    const int tx = t & 15, ty = t >> 4;
+    const int r0 = blockIdx.x * kGemmTile, b0 = blockIdx.y * kGemmTile;
+    // one slice: 2048 elements of each of A (q-major, 128 rows per q) and B
+    // (block-major, 16 q per block); eight of each per thread
+    float ra[8], rb[8];
+    auto load = [&](int q0) {
+#pragma unroll
+        for (int e = 0; e < 8; e++) {
+            const int idx = t + e * kGemmThreads;  // 0 .. 2047
+            const int kk = idx >> 7, c = idx & 127;
+            const int q = q0 + kk, r = r0 + c;
+            ra[e] = (q < nf && r < rows) ? __ldg(MT + (size_t)q * rows + r) : 0.0f;
+            // B: 128 blocks x 16 q, q fastest within a block
+            const int bb = idx >> 4, k2 = idx & 15;
+            const int qb = q0 + k2, b = b0 + bb;
+            rb[e] = (qb < nf && b < nblocks) ? __ldg(X + (size_t)b * nf + qb) : 0.0f;
+        }
+    };
+    auto store = [&](int buf) {
+#pragma unroll
+        for (int e = 0; e < 8; e++) {
+            const int idx = t + e * kGemmThreads;
+            As[buf][idx >> 7][idx & 127] = ra[e];
+            Bs[buf][idx & 15][idx >> 4] = rb[e];
+        }
+    };
+    float acc[8][8];
+#pragma unroll
+    for (int i = 0; i < 8; i++)
+#pragma unroll
+        for (int j = 0; j < 8; j++) acc[i][j] = 0.0f;
+    const int nk = (nf + kGemmK - 1) / kGemmK;
+    load(0);
+    store(0);
     __syncthreads();
-    const int tr = threadIdx.x & 63, tb = threadIdx.x >> 6;
-    int r[4];
-    bool rok[4];
+    for (int kt = 0; kt < nk; kt++) {
+        const int buf = kt & 1;
+        if (kt + 1 < nk) load((kt + 1) * kGemmK);
 #pragma unroll
-    for (int m = 0; m < 4; m++) {
-        r[m] = blockIdx.x * kFastRows + tr + 64 * m;
-        rok[m] = r[m] < rows;
-    }
-    float acc[4][4];
+        for (int kk = 0; kk < kGemmK; kk++) {
+            float a[8], bv[8];
+            const float4 a0 = *reinterpret_cast<const float4*>(&As[buf][kk][8 * ty]);
+            const float4 a1 = *reinterpret_cast<const float4*>(&As[buf][kk][8 * ty + 4]);
+            const float4 c0 = *reinterpret_cast<const float4*>(&Bs[buf][kk][8 * tx]);
+            const float4 c1 = *reinterpret_cast<const float4*>(&Bs[buf][kk][8 * tx + 4]);
+            a[0] = a0.x, a[1] = a0.y, a[2] = a0.z, a[3] = a0.w, a[4] = a1.x, a[5] = a1.y, a[6] = a1.z, a[7] = a1.w;
+            bv[0] = c0.x, bv[1] = c0.y, bv[2] = c0.z, bv[3] = c0.w, bv[4] = c1.x, bv[5] = c1.y, bv[6] = c1.z,
+            bv[7] = c1.w;
 #pragma unroll
-    for (int m = 0; m < 4; m++)
+            for (int i = 0; i < 8; i++)
 #pragma unroll
-        for (int n = 0; n < 4; n++) acc[m][n] = 0.0f;
-    const float* xb = xs + (tb * 4) * nf;
-#pragma unroll 8
-    for (int q = 0; q < nf; q++) {
-        float mv[4], xv[4];
-#pragma unroll
-        for (int m = 0; m < 4; m++) mv[m] = rok[m] ? __ldg(MT + (size_t)q * rows + r[m]) : 0.0f;
-#pragma unroll
-        for (int n = 0; n < 4; n++) xv[n] = xb[n * nf + q];
-#pragma unroll
-        for (int m = 0; m < 4; m++)
-#pragma unroll
-            for (int n = 0; n < 4; n++) acc[m][n] = __fmaf_rn(mv[m], xv[n], acc[m][n]);
+                for (int j = 0; j < 8; j++) acc[i][j] = __fmaf_rn(a[i], bv[j], acc[i][j]);
+        }
+        if (kt + 1 < nk) store(buf ^ 1);
+        __syncthreads();
     }
 #pragma unroll
-    for (int m = 0; m < 4; m++) {
-        if (!rok[m]) continue;
-        const int f = interior_face(s, r[m]);
+    for (int i = 0; i < 8; i++) {
+        const int r = r0 + 8 * ty + i;
+        if (r >= rows) continue;
+        const int f = interior_face(s, r);
 #pragma unroll
-        for (int n = 0; n < 4; n++) {
-            const int b = tb * 4 + n;
-            if (b >= nb) continue;
-            const int gb = b0 + b;
-            if (bobs[gb]) continue;
+        for (int j = 0; j < 8; j++) {
+            const int gb = b0 + 8 * tx + j;
+            if (gb >= nblocks || bobs[gb]) continue;
             const int bi = gb % Lc.W, bj = (gb / Lc.W) % Lc.H, bk = gb / (Lc.W * Lc.H);
             int comp;
             const int c = block_face(L, s, f, bi, bj, bk, comp);
-            comp_ptr(comp, u, v, w)[c] = acc[m][n];
+            comp_ptr(comp, u, v, w)[c] = acc[i][j];
         }
     }
 }
 
-// Blocks with an occupied fine cell: min |A p - div| with the first free cell
-// pinned, A the Laplacian of the block's free cells (weight 1 between free
-// neighbours); CG in double on the normal equations, one thread per cell.
+// Blocks with obstacles: one thread per block cell, at most this many.
 constexpr int kMaxBlockCells = 1024;
 
 // Sum over the CTA in a fixed order (warp trees, then the warp sums in warp
@@ -727,9 +756,6 @@ int coarse_prepare(CoarseState*& cs, const Layout& L, int s) {
         return ZQS_EINVAL;
     }
     if (cs && cs->s == s && cs->Lc.W == L.W / s && cs->Lc.H == L.H / s && cs->Lc.D == L.D / s) return ZQS_OK;
-    // the fast kernel's dynamic shared memory exceeds the 48 KB default for s > 4
-    ZQS_CUDA_TRY(cudaFuncSetAttribute(k_subproj_fast, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      kFastBlocks * 3 * 10 * 10 * 11 * (int)sizeof(float)));
     coarse_free(cs);
     CoarseState* c = new CoarseState();
     c->s = s;
@@ -840,10 +866,9 @@ int launch_project_coarse(DevGrid& g, const KParams& kp, int K, cudaStream_t st,
         const long long total = (long long)cs->nblocks * cs->nf;
         k_subproj_gather<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(L, Lc, s, cs->nf, total, g.u, g.v, g.w,
                                                                             cs->X);
-        const dim3 gf((cs->rows + kFastRows - 1) / kFastRows, (cs->nblocks + kFastBlocks - 1) / kFastBlocks, 1);
-        const size_t smf = (size_t)kFastBlocks * cs->nf * sizeof(float);
-        k_subproj_fast<<<gf, kFastThreads, smf, st>>>(L, Lc, s, cs->nf, cs->rows, cs->nblocks, cs->MT, cs->X,
-                                                      cs->bobs, g.u, g.v, g.w);
+        const dim3 gf((cs->rows + kGemmTile - 1) / kGemmTile, (cs->nblocks + kGemmTile - 1) / kGemmTile, 1);
+        k_subproj_fast<<<gf, kGemmThreads, 0, st>>>(L, Lc, s, cs->nf, cs->rows, cs->nblocks, cs->MT, cs->X,
+                                                    cs->bobs, g.u, g.v, g.w);
         int nthr = 32;
         while (nthr < s * s * s) nthr <<= 1;
         const size_t smo = (size_t)2 * nthr * sizeof(double) + (size_t)nthr * sizeof(int);
