@@ -252,6 +252,22 @@ ZQS_API int zqs_batch_set_sor_variant(zqs_batch* b, int index, int zchunk);
 ZQS_API int64_t zqs_batch_launch_count(const zqs_batch* b);
 ZQS_API int zqs_batch_synchronize(zqs_batch* b, void* stream);
 
+/* ---- moving voxel objects ---------------------------------------------------
+ * ZQ_ApplyMovingObject3D (ZQ_SmokeSimulationUtils3D.cpp:1933-2046): the grid's
+ * occupancy becomes the objects' voxels (every other cell free; all six
+ * domain walls occupied when closed_walls is 1, all but the y = H-1 layer
+ * when it is 2, the open-top walls of wallsExceptTop), and for each object in
+ * order every in-domain voxel's six faces take the object's velocity, vel
+ * (cells per step, as in the reference's object files) times h/dt rounded
+ * toward zero to an integer as the reference's int arithmetic does.  mask is
+ * host memory, size[0]*size[1]*size[2] bytes with x fastest; a voxel lands
+ * at pos - center + (x, y, z). */
+typedef struct zqs_object {
+    const uint8_t* mask;
+    int32_t size[3], center[3], pos[3], vel[3];
+} zqs_object;
+ZQS_API int zqs_grid_stamp_objects(zqs_grid* g, const zqs_object* objects, int n, int closed_walls, void* stream);
+
 /* ---- external force and reverse mode ----------------------------------------
  * No counterpart in the reference.  An external per-cell force F is added to
  * the cell force of every step after the buoyancy terms (force stage, before

@@ -230,6 +230,43 @@ ZQS_CXX_API bool ZQ_ReinjectTemperatureDensity3D(ZQ_SmokeGrid3D* fineGrid, const
  * advection, projection, scalar advection, reinjection). */
 ZQS_CXX_API bool ZQ_UpdateOneFrame3D(ZQ_SmokeGrid3D* fineGrid, const ZQ_SmokeSimulationPara3D& para);
 
+/* A moving voxel object (ZQ_SmokeMovingObject3D.h:6-35): a solid mask of
+ * sizex*sizey*sizez voxels (x fastest) placed at pos - c, moved by vels[curstep]
+ * cells per step. */
+class ZQS_CXX_API ZQ_SmokeMovingObject3D {
+public:
+    class Velocity {
+    public:
+        int x, y, z;
+        Velocity(int u = 0, int v = 0, int w = 0) : x(u), y(v), z(w) {}
+    };
+    ZQ_SmokeMovingObject3D();
+    ~ZQ_SmokeMovingObject3D();
+    int cx, cy, cz;        // rotation centre
+    int posx, posy, posz;  // position in the grid
+    int sizex, sizey, sizez;
+    int curstep;
+    std::vector<Velocity> vels;
+    bool* occupy;
+    void GetCenter(int& cx, int& cy, int& cz) const;
+    void GetPos(int& posx, int& posy, int& posz) const;
+    void GetSize(int& sizex, int& sizey, int& sizez) const;
+    /* vels[curstep], 0 past the end */
+    void GetCurVel(int& u, int& v, int& w) const;
+    const bool*& GetOccupyPtr() const;
+    /* pos += vels[curstep] (when in range), curstep++ */
+    void UpdateOneStep();
+};
+/* The reference's object file (ZQ_SmokeMovingObject3D.cpp:101-123): count, then
+ * per object sizes, centre, position, step count, the step velocities and the
+ * voxel mask, whitespace-separated integers. */
+ZQS_CXX_API bool LoadMovingObjects3D(const char* file, std::vector<ZQ_SmokeMovingObject3D*>& mvobjs);
+/* ZQ_ApplyMovingObject3D (Utils3D:1933-2046): the occupancy becomes the objects'
+ * voxels (all six walls too for the closed solvers) and the voxels' faces take
+ * the objects' velocities; on the GPU, host arrays in and out. */
+ZQS_CXX_API bool ZQ_ApplyMovingObject3D(ZQ_SmokeGrid3D* fineGrid, const std::vector<ZQ_SmokeMovingObject3D*>& mvobjs,
+                                        const ZQ_SmokeSimulationPara3D& para);
+
 class ZQS_CXX_API ZQ_SmokeSimulation3D {
 public:
     ZQ_SmokeSimulation3D();
@@ -251,6 +288,8 @@ public:
 private:
     ZQ_SmokeSimulationPara3D para;
     ZQ_SmokeGrid3D* fineGrid;
+    std::vector<ZQ_SmokeMovingObject3D*> mvobjs;
+    int frame;  // frames run; the objects are re-applied from the second on (ZQ_SmokeSimulation3D.cpp:161-173)
 };
 
 #endif /* ZQS_SMOKE3D_H */

@@ -98,6 +98,15 @@ class Oracle:
         return self._f("project_coarse")(W, H, D, _p(st["u"]), _p(st["v"]), _p(st["w"]), _p(occ),
                                          C.byref(params))
 
+    def stamp_objects(self, W, H, D, st, occ, objs, closed, params):
+        """In place on occ (uint8, (D, H, W)) and st's u, v, w."""
+        from zq_smokesimulation_gb300 import capi
+        arr, keep = capi.make_objects(objs)
+        assert occ.dtype == np.uint8 and occ.flags["C_CONTIGUOUS"]
+        self._f("stamp_objects")(W, H, D, _p(occ), _p(st["u"]), _p(st["v"]), _p(st["w"]),
+                                 C.cast(arr, C.c_void_p), len(objs), int(closed), C.byref(params))
+        del keep
+
     def submatrix(self, s):
         """The sub-projection matrix of block edge s as (3 s^2 (s-1), 3 s^2 (s+1)) float32."""
         rows, cols = 3 * s * s * (s - 1), 3 * s * s * (s + 1)

@@ -1408,6 +1408,49 @@ int project_coarse(const Dims& d, R* u, R* v, R* w, const uint8_t* occ, const zq
     return ZQS_OK;
 }
 
+/* ZQ_ApplyMovingObject3D (Utils3D:1933-2046): the occupancy becomes the
+ * objects' voxels (plus the six domain walls for the closed solvers, :1994-
+ * 2044); each in-domain voxel of each object, in order, is occupied and its
+ * six faces take the object's velocity, an int scaled by h/dt (float
+ * division, widened) and truncated to int (:1958-1962). */
+template <class R>
+void stamp_objects(const Dims& d, uint8_t* occ, R* u, R* v, R* w, const zqs_object* objs, int n, int closed,
+                   const zqs_params& P) {
+    const int W = d.W, H = d.H, D = d.D;
+    // closed: 0 no walls, 1 the six walls of the closed solvers, 2 all but y = H-1
+    for (int k = 0; k < D; k++)
+        for (int j = 0; j < H; j++)
+            for (int i = 0; i < W; i++)
+                occ[d.cell(i, j, k)] = (closed && (i == 0 || i == W - 1 || j == 0 || (j == H - 1 && closed == 1) ||
+                                                   k == 0 || k == D - 1))
+                                           ? 1
+                                           : 0;
+    const double scale = (double)(P.voxel_size / P.step_time);
+    for (int q = 0; q < n; q++) {
+        const zqs_object& o = objs[q];
+        int cu = o.vel[0], cv = o.vel[1], cw = o.vel[2];
+        cu = (int)(cu * scale);
+        cv = (int)(cv * scale);
+        cw = (int)(cw * scale);
+        for (int sk = 0; sk < o.size[2]; sk++)
+            for (int sj = 0; sj < o.size[1]; sj++)
+                for (int si = 0; si < o.size[0]; si++) {
+                    if (!o.mask[((size_t)sk * o.size[1] + sj) * o.size[0] + si]) continue;
+                    const int ix = si + o.pos[0] - o.center[0];
+                    const int iy = sj + o.pos[1] - o.center[1];
+                    const int iz = sk + o.pos[2] - o.center[2];
+                    if (ix < 0 || ix >= W || iy < 0 || iy >= H || iz < 0 || iz >= D) continue;
+                    occ[d.cell(ix, iy, iz)] = 1;
+                    u[d.uix(ix, iy, iz)] = (R)cu;
+                    u[d.uix(ix + 1, iy, iz)] = (R)cu;
+                    v[d.vix(ix, iy, iz)] = (R)cv;
+                    v[d.vix(ix, iy + 1, iz)] = (R)cv;
+                    w[d.wix(ix, iy, iz)] = (R)cw;
+                    w[d.wix(ix, iy, iz + 1)] = (R)cw;
+                }
+    }
+}
+
 /* One timestep in the order of ZQ_SmokeSimulation3D::UpdateOneFrame
  * (ZQ_SmokeSimulation3D.cpp:156-243): force, attenuation, velocity advection
  * (always with the open write-back, Utils3D:2163), projection, scalar
@@ -2106,6 +2149,10 @@ ZQO_API int zqo_submatrix(int s, float* out, int cap) {
     ZQO_API int zqo_project_coarse_##SFX(int W, int H, int D, R* u, R* v, R* w, const uint8_t* occ,     \
                                          const zqs_params* P) {                                         \
         return zqo::project_coarse<R>(zqo::Dims{W, H, D}, u, v, w, occ, *P);                            \
+    }                                                                                                   \
+    ZQO_API void zqo_stamp_objects_##SFX(int W, int H, int D, uint8_t* occ, R* u, R* v, R* w,            \
+                                         const zqs_object* objs, int n, int closed, const zqs_params* P) { \
+        zqo::stamp_objects<R>(zqo::Dims{W, H, D}, occ, u, v, w, objs, n, closed, *P);              \
     }                                                                                                   \
     ZQO_API void zqo_reinject_##SFX(int W, int H, int D, R* T, R* rho, const zqs_params* P) {           \
         zqo::reinject<R>(zqo::Dims{W, H, D}, T, rho, *P);                                               \

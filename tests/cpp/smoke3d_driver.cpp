@@ -3,11 +3,16 @@
 //   smoke3d_driver parse  <config> <outdir>   parameters and initial state only (no GPU)
 //   smoke3d_driver run    <config> <outdir>   ZQ_SmokeSimulation3D::Init + Run (resident)
 //   smoke3d_driver stages <config> <outdir>   ZQ_InitFineGrid3D + ZQ_UpdateOneFrame3D per frame
+//                                             (+ ZQ_ApplyMovingObject3D as the class does)
+//   smoke3d_driver objects <file> <outdir>    LoadMovingObjects3D, then objects.txt: per object
+//                                             size, centre, step count, mask sum and the
+//                                             positions and current velocities over 4 steps (no GPU)
 // Outputs in <outdir>: params.bin (zqs_params bytes), occupancy.bin (W*H*D bytes),
 // init.guidedat (u, v, w, density, temperature) and frame files.
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "zqs_smoke3d.h"
 
@@ -50,16 +55,48 @@ int main(int argc, char** argv) {
         ZQ_SmokeGrid3D* after = sim.GetFineGrid();
         return after->ExportGuide((out + "/final.guidedat").c_str()) ? 0 : 6;
     }
+    if (mode == "objects") {
+        std::vector<ZQ_SmokeMovingObject3D*> objs;
+        if (!LoadMovingObjects3D(cfg.c_str(), objs)) return 3;
+        FILE* f = fopen((out + "/objects.txt").c_str(), "w");
+        if (!f) return 4;
+        fprintf(f, "%d\n", (int)objs.size());
+        for (ZQ_SmokeMovingObject3D* o : objs) {
+            int sum = 0;
+            for (int b = 0; b < o->sizex * o->sizey * o->sizez; b++) sum += o->GetOccupyPtr()[b] ? 1 : 0;
+            fprintf(f, "%d %d %d %d %d %d %d %d", o->sizex, o->sizey, o->sizez, o->cx, o->cy, o->cz,
+                    (int)o->vels.size(), sum);
+            for (int t = 0; t < 4; t++) {
+                int x, y, z, u, v, w;
+                o->GetPos(x, y, z);
+                o->GetCurVel(u, v, w);
+                fprintf(f, " %d %d %d %d %d %d", x, y, z, u, v, w);
+                o->UpdateOneStep();
+            }
+            fprintf(f, "\n");
+            delete o;
+        }
+        fclose(f);
+        return 0;
+    }
     if (mode == "stages") {
         ZQ_SmokeSimulationPara3D para;
         if (!para.LoadFromFile(cfg.c_str(), false)) return 3;
         ZQ_SmokeGrid3D g(para.width, para.height, para.depth);
         if (!ZQ_InitFineGrid3D(&g, para)) return 4;
+        std::vector<ZQ_SmokeMovingObject3D*> objs;
+        if (para.useMovingObject) {
+            if (!LoadMovingObjects3D(para.movingObjectFile, objs)) return 10;
+            if (!ZQ_ApplyMovingObject3D(&g, objs, para)) return 11;
+        }
         for (int i = 0; i < para.frameCount; i++) {
+            if (para.useMovingObject && i > 0 && !ZQ_ApplyMovingObject3D(&g, objs, para)) return 11;
             if (!ZQ_UpdateOneFrame3D(&g, para)) return 5;
+            for (ZQ_SmokeMovingObject3D* o : objs) o->UpdateOneStep();
             const std::string name = out + "/stage_frame" + std::to_string(i) + ".di3";
             if (!g.ExportDensity(name.c_str())) return 6;
         }
+        for (ZQ_SmokeMovingObject3D* o : objs) delete o;
         // Clone, and a guide round trip through ImportGuide
         ZQ_SmokeGrid3D* c = g.Clone();
         const std::string gd = out + "/stage_final.guidedat";

@@ -175,3 +175,93 @@ def test_coarse_solver_config_matches_oracle(driver, tmp_path, oracle32):
     fin = load_guide(run_out / "final.guidedat", W, H, D)
     for k in ("u", "v", "w", "T", "rho"):
         assert rel_l2(fin[k], ref[k]) <= 1e-5, k
+
+
+# moving objects (ZQ_SmokeMovingObject3D.cpp:101-123 file format)
+OBJECTS = [
+    {"mask": (np.arange(3 * 4 * 5).reshape(3, 4, 5) % 3 != 0), "center": (2, 1, 1), "pos": (6, 5, 5),
+     "vels": [(1, 0, 0), (1, 1, 0), (0, 1, -1)]},
+    {"mask": np.ones((2, 2, 2), bool), "center": (0, 0, 0), "pos": (15, 12, 9), "vels": [(0, -2, 1)]},
+]
+
+
+def write_objects(path, objs):
+    lines = [str(len(objs))]
+    for o in objs:
+        sz, sy, sx = o["mask"].shape
+        lines += [f"{sx} {sy} {sz}", "{} {} {}".format(*o["center"]), "{} {} {}".format(*o["pos"]),
+                  str(len(o["vels"]))]
+        lines += ["{} {} {}".format(*v) for v in o["vels"]]
+        lines.append(" ".join(str(int(b)) for b in o["mask"].ravel()))
+    path.write_text("\n".join(lines) + "\n")
+
+
+def object_track(o, t):
+    """(pos, vel) after t calls of UpdateOneStep (ZQ_SmokeMovingObject3D.cpp:83-98)."""
+    pos = list(o["pos"])
+    for s in range(t):
+        if s < len(o["vels"]):
+            pos = [a + b for a, b in zip(pos, o["vels"][s])]
+    vel = o["vels"][t] if t < len(o["vels"]) else (0, 0, 0)
+    return tuple(pos), tuple(vel)
+
+
+def test_load_moving_objects(driver, tmp_path):
+    f = tmp_path / "objs.txt"
+    write_objects(f, OBJECTS)
+    r = subprocess.run([str(driver), "objects", str(f), str(tmp_path)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    rows = (tmp_path / "objects.txt").read_text().split("\n")
+    assert int(rows[0]) == 2
+    for o, row in zip(OBJECTS, rows[1:]):
+        vals = [int(x) for x in row.split()]
+        sz, sy, sx = o["mask"].shape
+        assert vals[:8] == [sx, sy, sz, *o["center"], len(o["vels"]), int(o["mask"].sum())]
+        for t in range(4):
+            pos, vel = object_track(o, t)
+            assert tuple(vals[8 + 6 * t: 11 + 6 * t]) == pos and tuple(vals[11 + 6 * t: 14 + 6 * t]) == vel
+    # a truncated file fails
+    f.write_text("1\n2 2 2\n0 0 0\n1 1 1\n1\n0 0 0\n1 1 1\n")
+    assert subprocess.run([str(driver), "objects", str(f), str(tmp_path)], capture_output=True).returncode == 3
+
+
+@pytest.mark.gpu
+def test_moving_objects_match_oracle(driver, tmp_path, oracle32):
+    """useMovingObject: the objects are stamped at Init, again before every
+    frame from the second on, and advanced after each frame; the resident class
+    path and the free-function path (ZQ_ApplyMovingObject3D) both equal the
+    oracle's stamp + step sequence bit for bit."""
+    W, H, D = 24, 20, 16
+    objf = tmp_path / "objs.txt"
+    write_objects(objf, OBJECTS)
+    cfg = CONFIG.replace("stepTime 0.05", "stepTime 0.02") + f"useMovingObject true\nmovingObjectFile {objf}\n"
+    pre = run_driver(driver, "parse", cfg, tmp_path / "pre")
+    run_out = run_driver(driver, "run", cfg, tmp_path / "run")
+    stage_out = run_driver(driver, "stages", cfg, tmp_path / "stages")
+    p, occ0, st0 = load_setup(pre, W, H, D)
+    ref = {k: np.ascontiguousarray(v).copy() for k, v in st0.items()}
+    occ = np.ascontiguousarray(occ0).copy()
+
+    def stamp(t):
+        objs = []
+        for o in OBJECTS:
+            pos, vel = object_track(o, t)
+            objs.append({"mask": o["mask"], "center": o["center"], "pos": pos, "vel": vel})
+        oracle32.stamp_objects(W, H, D, ref, occ, objs, 2, p)   # wallsExceptTop: all walls but y = H-1
+
+    stamp(0)
+    _, occ_init, st_init = load_setup(run_out, W, H, D)
+    np.testing.assert_array_equal(occ_init, occ)
+    for k in ("u", "v", "w"):
+        np.testing.assert_array_equal(st_init[k], ref[k])
+    assert int(2 * np.float64(np.float32(1.0 / 24) / np.float32(0.02))) != 0   # the stamped velocities are not zero
+    for i in range(3):
+        if i > 0:
+            stamp(i)
+        rc, _ = oracle32.step(W, H, D, ref, occ, p, 1)
+        assert rc == 0
+        np.testing.assert_array_equal(load_di3(run_out / f"frame{i}.di3"), ref["rho"])
+        np.testing.assert_array_equal(load_di3(stage_out / f"stage_frame{i}.di3"), ref["rho"])
+    fin = load_guide(run_out / "final.guidedat", W, H, D)
+    for k in ("u", "v", "w", "T", "rho"):
+        np.testing.assert_array_equal(fin[k], ref[k])

@@ -58,6 +58,29 @@ class Params(C.Structure):
             self.sources[i] = s
 
 
+class Object(C.Structure):
+    """zqs_object: a voxel mask (host, x fastest) with its size, rotation centre,
+    position and velocity in cells per step."""
+    _fields_ = [("mask", C.c_void_p), ("size", C.c_int32 * 3), ("center", C.c_int32 * 3), ("pos", C.c_int32 * 3),
+                ("vel", C.c_int32 * 3)]
+
+
+def make_objects(objs):
+    """zqs_object array from dicts {mask (sz, sy, sx) bool/uint8, center, pos, vel}; returns (array, keepalive)."""
+    arr = (Object * max(1, len(objs)))()
+    keep = []
+    for q, o in enumerate(objs):
+        m = np.ascontiguousarray(o["mask"], dtype=np.uint8)
+        keep.append(m)
+        arr[q].mask = m.ctypes.data
+        sz, sy, sx = m.shape
+        arr[q].size[:] = (sx, sy, sz)
+        arr[q].center[:] = tuple(int(x) for x in o.get("center", (0, 0, 0)))
+        arr[q].pos[:] = tuple(int(x) for x in o["pos"])
+        arr[q].vel[:] = tuple(int(x) for x in o.get("vel", (0, 0, 0)))
+    return arr, keep
+
+
 class Stats(C.Structure):
     _fields_ = [("max_abs_div", C.c_double), ("residual_l2", C.c_double), ("div_mean_removed", C.c_double),
                 ("free_cells", C.c_int64)]
@@ -91,7 +114,7 @@ CAPI_SYMBOLS = [
     "zqs_sor_variant_info", "zqs_grid_set_sor_variant", "zqs_grid_synchronize", "zqs_grid_launch_count",
     "zqs_batch_create", "zqs_batch_destroy", "zqs_batch_step", "zqs_batch_use_graph", "zqs_batch_set_sor_variant",
     "zqs_batch_launch_count", "zqs_batch_synchronize",
-    "zqs_grid_set_force", "zqs_adjoint_create", "zqs_adjoint_destroy", "zqs_adjoint_forward",
+    "zqs_grid_set_force", "zqs_grid_stamp_objects", "zqs_adjoint_create", "zqs_adjoint_destroy", "zqs_adjoint_forward",
     "zqs_adjoint_backward", "zqs_adjoint_download", "zqs_adjoint_get_info",
 ]
 LEGACY_C_SYMBOLS = ["ZQ_Cuda_Prepare_Advection", "Advect_Velocity", "Advect_Scalar", "AddForce3D",
@@ -161,6 +184,7 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.zqs_batch_launch_count.restype = C.c_int64
     lib.zqs_batch_synchronize.argtypes = [vp, vp]
     lib.zqs_grid_set_force.argtypes = [vp, vp, i, vp]
+    lib.zqs_grid_stamp_objects.argtypes = [vp, vp, i, i, vp]
     lib.zqs_adjoint_create.argtypes = [C.POINTER(vp), vp, i, i]
     lib.zqs_adjoint_destroy.argtypes = [vp]
     lib.zqs_adjoint_forward.argtypes = [vp, vp, i, vp]
@@ -373,6 +397,14 @@ class Grid:
             raise ValueError("force must hold 3*W*H*D values")
         check(self.lib.zqs_grid_set_force(self.h, C.c_void_p(ptr(a)), 0, None), "zqs_grid_set_force")
         self.sync()
+
+    def stamp_objects(self, objs, closed_walls: int = 0, stream=None):
+        """Moving voxel objects (zqs_grid_stamp_objects); objs as for make_objects;
+        closed_walls 0 none, 1 (or True) all six walls, 2 all but the y = H-1 layer."""
+        arr, keep = make_objects(objs)
+        check(self.lib.zqs_grid_stamp_objects(self.h, C.cast(arr, C.c_void_p), len(objs), int(closed_walls),
+                                              C.c_void_p(stream or 0)), "zqs_grid_stamp_objects")
+        del keep
 
     def set_force_device(self, dev_ptr: int, stream: int | None = None):
         check(self.lib.zqs_grid_set_force(self.h, C.c_void_p(dev_ptr), 1, C.c_void_p(stream or 0)),

@@ -316,6 +316,7 @@ ZQS_API int zqs_grid_destroy(zqs_grid* g) {
     cudaFree(g->occ_dense);
     cudaFree(g->base);
     coarse_free(g->g.coarse);
+    if (g->obj_mask) cudaFree(g->obj_mask);
     if (g->fext_base) cudaFree(g->fext_base);
     delete g;
     return ZQS_OK;

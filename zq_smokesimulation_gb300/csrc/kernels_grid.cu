@@ -13,7 +13,11 @@ namespace {
 // in-domain neighbours count 1, outside the domain counts 1 for the open
 // solver (ZQ_SmokeSimulationUtils3D.cpp:570, count = 6 - #in-domain) and 0 for
 // the closed one.
-__global__ void k_build_flags(Layout L, const uint8_t* __restrict__ occ, uint8_t* __restrict__ flags, int open) {
+// The SOR sweeps sum all six neighbours and the divergence writes only free
+// cells, so pressure and right-hand side must hold 0 in every occupied cell;
+// occupancy that changes (moving objects, a new upload) clears them there.
+__global__ void k_build_flags(Layout L, const uint8_t* __restrict__ occ, uint8_t* __restrict__ flags, int open,
+                              float* __restrict__ p, float* __restrict__ p2, float* __restrict__ div) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y * blockDim.y + threadIdx.y;
     int k = blockIdx.z;
@@ -21,6 +25,12 @@ __global__ void k_build_flags(Layout L, const uint8_t* __restrict__ occ, uint8_t
     const int W = L.W, H = L.H, D = L.D;
     auto occupied = [&](int a, int b, int c) -> bool { return occ[((size_t)c * H + b) * W + a] != 0; };
     uint8_t f = 0;
+    if (i < W && j < H && k < D && occupied(i, j, k)) {
+        const int c = lidx(L, i, j, k);
+        p[c] = 0.0f;
+        p2[c] = 0.0f;
+        div[c] = 0.0f;
+    }
     if (i < W && j < H && k < D && !occupied(i, j, k)) {
         f |= F_FREE;
         int nin = 0, nfree = 0;
@@ -152,7 +162,7 @@ int launch_dense_reg4_to_mac(int W, int H, int D, const float4* vel4, float* u, 
 int launch_build_flags(const DevGrid& g, const uint8_t* occ_dense, int solver, cudaStream_t s, LaunchCounter& lc) {
     const Layout& L = g.L;
     dim3 b(32, 8, 1), gr((L.px + 31) / 32, (L.py + 7) / 8, L.pz);
-    k_build_flags<<<gr, b, 0, s>>>(L, occ_dense, g.flags, solver != ZQS_SOLVER_CLOSED ? 1 : 0);
+    k_build_flags<<<gr, b, 0, s>>>(L, occ_dense, g.flags, solver != ZQS_SOLVER_CLOSED ? 1 : 0, g.p, g.p2, g.div);
     lc.n++;
     ZQS_LAUNCH_CHECK("k_build_flags");
     return ZQS_OK;

@@ -509,7 +509,8 @@ bool ZQ_SmokeGrid3D::Upload() {
 
 bool ZQ_SmokeGrid3D::Download() {
     if (!dev) return false;
-    if (zqs_grid_download(dev, ZQS_FIELD_U, u, 0, nullptr) || zqs_grid_download(dev, ZQS_FIELD_V, v, 0, nullptr) ||
+    if (zqs_grid_download(dev, ZQS_FIELD_OCCUPANCY, occ_store.data(), 0, nullptr) ||
+        zqs_grid_download(dev, ZQS_FIELD_U, u, 0, nullptr) || zqs_grid_download(dev, ZQS_FIELD_V, v, 0, nullptr) ||
         zqs_grid_download(dev, ZQS_FIELD_W, w, 0, nullptr) ||
         zqs_grid_download(dev, ZQS_FIELD_TEMPERATURE, temperature, 0, nullptr) ||
         zqs_grid_download(dev, ZQS_FIELD_DENSITY, density, 0, nullptr) ||
@@ -747,16 +748,117 @@ bool ZQ_UpdateOneFrame3D(ZQ_SmokeGrid3D* g, const ZQ_SmokeSimulationPara3D& para
     return ZQ_AdvectScalar3D(g, para) && ZQ_ReinjectTemperatureDensity3D(g, para);
 }
 
+// ----------------------------------------------------------------- moving objects
+
+ZQ_SmokeMovingObject3D::ZQ_SmokeMovingObject3D()
+    : cx(0), cy(0), cz(0), posx(0), posy(0), posz(0), sizex(0), sizey(0), sizez(0), curstep(0), occupy(nullptr) {}
+
+ZQ_SmokeMovingObject3D::~ZQ_SmokeMovingObject3D() { delete[] occupy; }
+
+void ZQ_SmokeMovingObject3D::GetCenter(int& x, int& y, int& z) const { x = cx, y = cy, z = cz; }
+void ZQ_SmokeMovingObject3D::GetPos(int& x, int& y, int& z) const { x = posx, y = posy, z = posz; }
+void ZQ_SmokeMovingObject3D::GetSize(int& x, int& y, int& z) const { x = sizex, y = sizey, z = sizez; }
+
+void ZQ_SmokeMovingObject3D::GetCurVel(int& u, int& v, int& w) const {
+    const bool in = curstep >= 0 && (size_t)curstep < vels.size();
+    u = in ? vels[curstep].x : 0;
+    v = in ? vels[curstep].y : 0;
+    w = in ? vels[curstep].z : 0;
+}
+
+const bool*& ZQ_SmokeMovingObject3D::GetOccupyPtr() const { return (const bool*&)occupy; }
+
+void ZQ_SmokeMovingObject3D::UpdateOneStep() {
+    if (curstep >= 0 && (size_t)curstep < vels.size()) {
+        posx += vels[curstep].x;
+        posy += vels[curstep].y;
+        posz += vels[curstep].z;
+    }
+    curstep++;
+}
+
+bool LoadMovingObjects3D(const char* file, std::vector<ZQ_SmokeMovingObject3D*>& mvobjs) {
+    FILE* in = file ? fopen(file, "r") : nullptr;
+    if (!in) return false;
+    auto next = [&](int& x) { return fscanf(in, "%d", &x) == 1; };
+    int count = 0;
+    bool ok = next(count) && count >= 0;
+    for (int q = 0; ok && q < count; q++) {
+        auto* o = new ZQ_SmokeMovingObject3D();
+        int nsteps = 0;
+        ok = next(o->sizex) && next(o->sizey) && next(o->sizez) && next(o->cx) && next(o->cy) && next(o->cz) &&
+             next(o->posx) && next(o->posy) && next(o->posz) && next(nsteps) && o->sizex >= 0 && o->sizey >= 0 &&
+             o->sizez >= 0 && nsteps >= 0;
+        for (int t = 0; ok && t < nsteps; t++) {
+            int a, b, c;
+            ok = next(a) && next(b) && next(c);
+            if (ok) o->vels.emplace_back(a, b, c);
+        }
+        const size_t n = ok ? (size_t)o->sizex * o->sizey * o->sizez : 0;
+        if (ok) o->occupy = new bool[n > 0 ? n : 1];
+        for (size_t b = 0; ok && b < n; b++) {
+            int x = 0;
+            ok = next(x);
+            o->occupy[b] = x != 0;
+        }
+        if (ok) mvobjs.push_back(o);
+        else delete o;
+    }
+    fclose(in);
+    return ok;
+}
+
+namespace {
+
+// The objects' current positions and velocities stamped into the device grid.
+bool stamp_objects(zqs_grid* d, const std::vector<ZQ_SmokeMovingObject3D*>& mvobjs,
+                   const ZQ_SmokeSimulationPara3D& para) {
+    static_assert(sizeof(bool) == 1, "object masks are passed as bytes");
+    std::vector<zqs_object> objs;
+    for (const ZQ_SmokeMovingObject3D* m : mvobjs) {
+        if (!m || !m->occupy) continue;
+        zqs_object o;
+        o.mask = reinterpret_cast<const uint8_t*>(m->occupy);
+        m->GetSize(o.size[0], o.size[1], o.size[2]);
+        m->GetCenter(o.center[0], o.center[1], o.center[2]);
+        m->GetPos(o.pos[0], o.pos[1], o.pos[2]);
+        m->GetCurVel(o.vel[0], o.vel[1], o.vel[2]);
+        objs.push_back(o);
+    }
+    // the reference rebuilds the six walls for its closed solvers; the open-top
+    // walls of wallsExceptTop are kept the same way
+    const int walls = para.wallsExceptTop ? 2 : is_closed(para.globalGridSolver) ? 1 : 0;
+    if (zqs_grid_stamp_objects(d, objs.data(), (int)objs.size(), walls, nullptr) != ZQS_OK)
+        return fail("ZQ_ApplyMovingObject3D");
+    return zqs_grid_synchronize(d, nullptr) == ZQS_OK || fail("ZQ_ApplyMovingObject3D");
+}
+
+}  // namespace
+
+bool ZQ_ApplyMovingObject3D(ZQ_SmokeGrid3D* g, const std::vector<ZQ_SmokeMovingObject3D*>& mvobjs,
+                            const ZQ_SmokeSimulationPara3D& para) {
+    zqs_grid* d = g ? prepare(g, para) : nullptr;
+    if (!d || !stamp_objects(d, mvobjs, para)) return false;
+    g->MarkHostStale();
+    return g->Download() || fail("ZQ_ApplyMovingObject3D");
+}
+
 // ----------------------------------------------------------------- simulation
 
-ZQ_SmokeSimulation3D::ZQ_SmokeSimulation3D() : fineGrid(nullptr) {}
+ZQ_SmokeSimulation3D::ZQ_SmokeSimulation3D() : fineGrid(nullptr), frame(0) {}
 
-ZQ_SmokeSimulation3D::~ZQ_SmokeSimulation3D() { delete fineGrid; }
+ZQ_SmokeSimulation3D::~ZQ_SmokeSimulation3D() {
+    delete fineGrid;
+    for (ZQ_SmokeMovingObject3D* o : mvobjs) delete o;
+}
 
 bool ZQ_SmokeSimulation3D::Init(const char* file) {
     if (!para.LoadFromFile(file, true)) return false;
-    if (para.useMovingObject) {
-        printf("moving objects are not available in this library\n");
+    for (ZQ_SmokeMovingObject3D* o : mvobjs) delete o;
+    mvobjs.clear();
+    frame = 0;
+    if (para.useMovingObject && !LoadMovingObjects3D(para.movingObjectFile, mvobjs)) {
+        printf("cannot read the moving objects of %s\n", para.movingObjectFile);
         return false;
     }
     if (para.exportType != ZQ_SmokeSimulationPara3D::EXPORT_DI3) {
@@ -773,14 +875,29 @@ bool ZQ_SmokeSimulation3D::Init(const char* file) {
     if (!ZQ_InitFineGrid3D(fineGrid, para)) return false;
     zqs_params p;
     if (!para.ToParams(&p)) return false;
-    return prepare(fineGrid, para) != nullptr || fail("Init");
+    zqs_grid* d = prepare(fineGrid, para);
+    if (!d) return fail("Init");
+    // the objects at their start positions (_initRegular, ZQ_SmokeSimulation3D.cpp:293-310)
+    if (para.useMovingObject) {
+        if (!stamp_objects(d, mvobjs, para)) return false;
+        fineGrid->MarkHostStale();
+    }
+    return true;
 }
 
 bool ZQ_SmokeSimulation3D::UpdateOneFrame(const void* guideGrid) {
     if (!fineGrid || guideGrid) return false;
     zqs_grid* d = fineGrid->DeviceGrid();
-    if (!d || zqs_grid_step(d, 1, nullptr) != ZQS_OK) return fail("UpdateOneFrame");
+    if (!d) return fail("UpdateOneFrame");
+    // re-applied from the second frame on, advanced after the step
+    // (ZQ_SmokeSimulation3D.cpp:161-173, 232-241)
+    frame++;
+    if (para.useMovingObject && frame > 1 && !stamp_objects(d, mvobjs, para)) return false;
+    if (zqs_grid_step(d, 1, nullptr) != ZQS_OK) return fail("UpdateOneFrame");
     fineGrid->MarkHostStale();
+    if (para.useMovingObject)
+        for (ZQ_SmokeMovingObject3D* o : mvobjs)
+            if (o) o->UpdateOneStep();
     return true;
 }
 
