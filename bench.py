@@ -57,6 +57,9 @@ def parse():
     ap.add_argument("--coarse", default="coarse256",
                     help="coarse-grid projection configuration measured beside the plain step ('' or none = skip)")
     ap.add_argument("--coarse-steps", type=int, default=5)
+    ap.add_argument("--render", default="256:1024x768x300",
+                    help="headless ray march N:WxHxSTEPS of an N^3 density in the viewer's default view "
+                         "('' or none = skip)")
     return ap.parse_args()
 
 
@@ -295,6 +298,64 @@ def measure_coarse(args, stream):
             "projection_ms": ms_proj, "max_abs_div_after_projection": mx}
 
 
+def measure_render(args, stream):
+    """The viewer's volume shader as k_raymarch: an N^3 density (seeded uniform
+    values; the cost does not depend on them) in the default view, one launch
+    per frame, timed with CUDA events; the FP32 oracle on the host cores renders
+    the same view at a quarter of the resolution in each direction for the CPU
+    rate.  Samples = hit rays x steps; each sample reads 8 texels."""
+    import time
+
+    import numpy as np
+    import torch
+
+    from zq_smokesimulation_gb300 import capi
+
+    n_s, rest = args.render.split(":")
+    N = int(n_s)
+    iw, ih, steps = (int(x) for x in rest.split("x"))
+    gen = torch.Generator(device="cuda").manual_seed(11)
+    vol = torch.rand((N, N, N), generator=gen, device="cuda", dtype=torch.float32)
+    cam = capi.default_camera(iw, ih, N, N, N)
+    cam.steps = steps
+    img = torch.empty((ih, iw, 4), dtype=torch.float32, device="cuda")
+    sp = stream.cuda_stream
+    for _ in range(3):
+        capi.render_density(vol.data_ptr(), N, N, N, cam, img.data_ptr(), sp)
+    reps = 10
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record(stream)
+    for _ in range(reps):
+        capi.render_density(vol.data_ptr(), N, N, N, cam, img.data_ptr(), sp)
+    b.record(stream)
+    b.synchronize()
+    ms = a.elapsed_time(b) / reps
+    # rays that met the box: alpha < 1 (the density is positive almost everywhere)
+    hits = int((img[..., 3] < 1).sum().item())
+    samples = hits * steps
+    out = {"volume": [N, N, N], "image": [iw, ih], "steps": steps, "ms_per_frame": ms, "rays_hit": hits,
+           "gsamples_per_s": samples / (ms * 1e-3) / 1e9,
+           "texel_reads_gbs": samples * 8 * 4 / (ms * 1e-3) / 1e9,
+           "hbm_alg_bytes": N ** 3 * 4 + iw * ih * 16,
+           "note": "L1/L2-gather bound: the volume (%.0f MB) stays in the 129 MB L2" % (N ** 3 * 4 / 1e6)}
+    if not args.no_cpu_baseline:
+        from oracle.binding import Oracle, num_threads
+
+        o = Oracle(np.float32)
+        small = capi.default_camera(iw // 4, ih // 4, N, N, N)
+        small.steps = steps
+        small.focal = cam.focal / 4
+        host = vol.cpu().numpy()
+        t0 = time.perf_counter()
+        ref = o.render(host, small)
+        dt = time.perf_counter() - t0
+        cs = int((ref[..., 3] < 1).sum()) * steps
+        out["cpu_baseline"] = {"gsamples_per_s": cs / dt / 1e9, "cores": num_threads(), "kind": "port",
+                               "sample": f"{iw // 4}x{ih // 4} image of the same view, {steps} steps, FP32 oracle"}
+    return out
+
+
 def measure_adjoint(args, stream, N: int):
     """The force-field control problem at N^3: forward (nsteps steps with the
     control force, checkpoints every k) and backward (recomputation + adjoint
@@ -485,6 +546,9 @@ def run_ours(args):
     coarse = None
     if args.coarse not in ("", "none") and world == 1:
         coarse = measure_coarse(args, stream)
+    render = None
+    if args.render not in ("", "none") and world == 1:
+        render = measure_render(args, stream)
     adjoint = None
     if args.adjoint not in ("", "none") and world == 1:
         adjoint = {f"control{n}": measure_adjoint(args, stream, int(n)) for n in args.adjoint.split(",") if n}
@@ -518,7 +582,7 @@ def run_ours(args):
                          "step_alg_gbs": step_alg / (ms / args.steps * 1e-3) / 1e9,
                          "step_frac": step_alg / (ms / args.steps * 1e-3) / 1e9 / peak},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches_per_step * args.steps, "clocks": clocks,
-            "batch": batch, "adjoint": adjoint, "coarse": coarse,
+            "batch": batch, "adjoint": adjoint, "coarse": coarse, "render": render,
         }
         print(json.dumps(line), flush=True)
     g.close()

@@ -268,6 +268,40 @@ typedef struct zqs_object {
 } zqs_object;
 ZQS_API int zqs_grid_stamp_objects(zqs_grid* g, const zqs_object* objects, int n, int closed_walls, void* stream);
 
+/* ---- headless ray march of the density ---------------------------------------
+ * The viewer's volume shader (SampleSmokeGUI/raycastingshader.h:10-70, its
+ * uniforms set in ZQ_SmokeGUI.cpp:711-752) as a CUDA kernel writing an RGBA
+ * float image to device memory; no graphics API.  Pixel (px, py), py counted
+ * from the bottom row as gl_FragCoord is, casts a ray through
+ * (px + 0.5 - (width-1)/2, py + 0.5 - (height-1)/2, -focal) turned by
+ * inv_view (row-major); a ray that meets the box takes `steps` samples from
+ * its entry point and writes (v, v, v, exp(-v)), v = density_scale times the
+ * sum of steplen * density, steplen = (tfar - tnear) / steps / box_size[0];
+ * other pixels get (0, 0, 0, 1).  The density is sampled as the viewer's
+ * GL_LINEAR / GL_CLAMP texture: coordinates clamped to [0, 1] over the box,
+ * texel centres at (i + 0.5) / n, zero outside the volume, exact trilinear
+ * weights (not the hardware filter's 8-bit ones).  rgba holds
+ * width * height * 4 floats in device memory, row py at py * width * 4. */
+typedef struct zqs_camera {
+    int32_t width, height;        /* image size in pixels */
+    float focal;                  /* distance of the image plane in pixels */
+    float inv_view[9];            /* eye-space -> world directions, row-major */
+    float eye[3];                 /* ray origin */
+    float box_min[3], box_max[3], box_size[3];
+    int32_t steps;                /* samples per ray, 0..65536 */
+    float density_scale;
+} zqs_camera;
+/* The viewer's start-up view of a W x H x D volume: fovy 40 (focal =
+ * height / 2 / atan(fovy / 360 * pi), the viewer's formula), eye (0, 0, 2)
+ * looking at the origin with y up, a box of height 1 with the volume's aspect
+ * centred at the origin, 300 steps, density scale 1. */
+ZQS_API void zqs_camera_default(zqs_camera* cam, int image_width, int image_height, int W, int H, int D);
+/* density: device memory, W*H*D floats, x fastest. */
+ZQS_API int zqs_render_density(const float* density, int W, int H, int D, const zqs_camera* cam, float* rgba,
+                               void* stream);
+/* The grid's current density. */
+ZQS_API int zqs_grid_render(zqs_grid* g, const zqs_camera* cam, float* rgba, void* stream);
+
 /* ---- external force and reverse mode ----------------------------------------
  * No counterpart in the reference.  An external per-cell force F is added to
  * the cell force of every step after the buoyancy terms (force stage, before

@@ -107,6 +107,13 @@ class Oracle:
                                  C.cast(arr, C.c_void_p), len(objs), int(closed), C.byref(params))
         del keep
 
+    def render(self, vol, cam):
+        """Ray march a dense (D, H, W) density; returns (height, width, 4), bottom row first."""
+        v = self.arr(vol)
+        out = np.zeros((cam.height, cam.width, 4), self.dtype)
+        self._f("render")(_p(v), v.shape[2], v.shape[1], v.shape[0], C.byref(cam), _p(out))
+        return out
+
     def submatrix(self, s):
         """The sub-projection matrix of block edge s as (3 s^2 (s-1), 3 s^2 (s+1)) float32."""
         rows, cols = 3 * s * s * (s - 1), 3 * s * s * (s + 1)

@@ -2096,6 +2096,85 @@ int control_loss(const Dims& d, const R* u, const R* v, const R* w, const R* T, 
     return ZQS_OK;
 }
 
+/* Headless ray march of a dense density volume: the viewer's fragment shader
+ * (SampleSmokeGUI/raycastingshader.h:10-70) per pixel, py from the bottom
+ * row, (0, 0, 0, 1) where the ray misses the box.  The 3D texture is read as
+ * GL_LINEAR with GL_CLAMP: coordinates clamped to [0, 1], texel centres at
+ * (i + 0.5) / n, zero outside, exact trilinear weights a + t (b - a) in x,
+ * then y, then z.  Every expression keeps the shader's order of operations. */
+template <class R>
+void render(const R* vol, int W, int H, int D, const zqs_camera& c, R* out) {
+    auto at = [&](int i, int j, int k) -> R {
+        if (i < 0 || i >= W || j < 0 || j >= H || k < 0 || k >= D) return R(0);
+        return vol[((size_t)k * H + j) * W + i];
+    };
+    auto lerp = [](R a, R b, R t) { return a + t * (b - a); };
+    auto sample = [&](R s, R t, R r) -> R {
+        s = std::fmin(std::fmax(s, R(0)), R(1));  // fmax/fmin: a NaN coordinate clamps to 0
+        t = std::fmin(std::fmax(t, R(0)), R(1));
+        r = std::fmin(std::fmax(r, R(0)), R(1));
+        const R fx = s * (R)W - R(0.5), fy = t * (R)H - R(0.5), fz = r * (R)D - R(0.5);
+        const R x0 = std::floor(fx), y0 = std::floor(fy), z0 = std::floor(fz);
+        const R ax = fx - x0, ay = fy - y0, az = fz - z0;
+        const int i = (int)x0, j = (int)y0, k = (int)z0;
+        const R e00 = lerp(at(i, j, k), at(i + 1, j, k), ax), e10 = lerp(at(i, j + 1, k), at(i + 1, j + 1, k), ax);
+        const R e01 = lerp(at(i, j, k + 1), at(i + 1, j, k + 1), ax);
+        const R e11 = lerp(at(i, j + 1, k + 1), at(i + 1, j + 1, k + 1), ax);
+        return lerp(lerp(e00, e10, ay), lerp(e01, e11, ay), az);
+    };
+    const R hw = ((R)c.width - R(1)) / R(2), hh = ((R)c.height - R(1)) / R(2);
+    R m[9], eye[3], bmin[3], bmax[3], bsize[3];
+    for (int q = 0; q < 9; q++) m[q] = (R)c.inv_view[q];
+    for (int q = 0; q < 3; q++) {
+        eye[q] = (R)c.eye[q];
+        bmin[q] = (R)c.box_min[q];
+        bmax[q] = (R)c.box_max[q];
+        bsize[q] = (R)c.box_size[q];
+    }
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int py = 0; py < c.height; py++)
+        for (int px = 0; px < c.width; px++) {
+            R dx = ((R)px + R(0.5)) - hw, dy = ((R)py + R(0.5)) - hh, dz = -(R)c.focal;
+            R len = std::sqrt((dx * dx + dy * dy) + dz * dz);
+            dx = dx / len, dy = dy / len, dz = dz / len;
+            R rx = (m[0] * dx + m[1] * dy) + m[2] * dz;
+            R ry = (m[3] * dx + m[4] * dy) + m[5] * dz;
+            R rz = (m[6] * dx + m[7] * dy) + m[8] * dz;
+            len = std::sqrt((rx * rx + ry * ry) + rz * rz);
+            rx = rx / len, ry = ry / len, rz = rz / len;
+            const R ix = R(1) / rx, iy = R(1) / ry, iz = R(1) / rz;
+            const R bx0 = ix * (bmin[0] - eye[0]), bx1 = ix * (bmax[0] - eye[0]);
+            const R by0 = iy * (bmin[1] - eye[1]), by1 = iy * (bmax[1] - eye[1]);
+            const R bz0 = iz * (bmin[2] - eye[2]), bz1 = iz * (bmax[2] - eye[2]);
+            using std::fmax;
+            using std::fmin;
+            const R tminx = fmin(bx1, bx0), tminy = fmin(by1, by0), tminz = fmin(bz1, bz0);
+            const R tmaxx = fmax(bx1, bx0), tmaxy = fmax(by1, by0), tmaxz = fmax(bz1, bz0);
+            const R tnear = fmax(fmax(tminx, tminy), fmax(tminx, tminz));
+            const R tfar = fmin(fmin(tmaxx, tmaxy), fmin(tmaxx, tmaxz));
+            R* o = out + ((size_t)py * c.width + px) * 4;
+            if (!(tfar > tnear)) {
+                o[0] = o[1] = o[2] = R(0);
+                o[3] = R(1);
+                continue;
+            }
+            R sx = ((eye[0] + rx * tnear) - bmin[0]) / bsize[0];
+            R sy = ((eye[1] + ry * tnear) - bmin[1]) / bsize[1];
+            R sz = ((eye[2] + rz * tnear) - bmin[2]) / bsize[2];
+            R steplen = (tfar - tnear) / (R)c.steps;
+            const R qx = (steplen * rx) / bsize[0], qy = (steplen * ry) / bsize[1], qz = (steplen * rz) / bsize[2];
+            steplen = steplen / bsize[0];
+            R acc = R(0);
+            for (int n = 0; n < c.steps; n++) {
+                acc = acc + steplen * sample(sx, sy, sz);
+                sx = sx + qx, sy = sy + qy, sz = sz + qz;
+            }
+            const R v = acc * (R)c.density_scale;
+            o[0] = o[1] = o[2] = v;
+            o[3] = std::exp(-v);
+        }
+}
+
 }  // namespace zqo
 
 /* ---------------------------------------------------------------------- */
@@ -2153,6 +2232,9 @@ ZQO_API int zqo_submatrix(int s, float* out, int cap) {
     ZQO_API void zqo_stamp_objects_##SFX(int W, int H, int D, uint8_t* occ, R* u, R* v, R* w,            \
                                          const zqs_object* objs, int n, int closed, const zqs_params* P) { \
         zqo::stamp_objects<R>(zqo::Dims{W, H, D}, occ, u, v, w, objs, n, closed, *P);              \
+    }                                                                                                   \
+    ZQO_API void zqo_render_##SFX(const R* vol, int W, int H, int D, const zqs_camera* cam, R* rgba) {    \
+        zqo::render<R>(vol, W, H, D, *cam, rgba);                                                       \
     }                                                                                                   \
     ZQO_API void zqo_reinject_##SFX(int W, int H, int D, R* T, R* rho, const zqs_params* P) {           \
         zqo::reinject<R>(zqo::Dims{W, H, D}, T, rho, *P);                                               \

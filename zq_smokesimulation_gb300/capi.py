@@ -81,6 +81,40 @@ def make_objects(objs):
     return arr, keep
 
 
+class Camera(C.Structure):
+    """zqs_camera: the ray-march view (image size, focal length in pixels,
+    row-major inverse view rotation, eye, box, samples per ray, density scale)."""
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("focal", C.c_float), ("inv_view", C.c_float * 9),
+                ("eye", C.c_float * 3), ("box_min", C.c_float * 3), ("box_max", C.c_float * 3),
+                ("box_size", C.c_float * 3), ("steps", C.c_int32), ("density_scale", C.c_float)]
+
+
+def default_camera(image_width: int, image_height: int, W: int, H: int, D: int) -> Camera:
+    """The viewer's start-up view of a W x H x D volume (zqs_camera_default)."""
+    c = Camera()
+    load().zqs_camera_default(C.byref(c), image_width, image_height, W, H, D)
+    return c
+
+
+def render_density(density_ptr: int, W: int, H: int, D: int, cam: Camera, rgba_ptr: int, stream: int | None = None):
+    """Ray march a dense device density (W*H*D floats, x fastest) into a device
+    RGBA image (cam.width * cam.height * 4 floats, bottom row first)."""
+    lib = load()
+    check(lib.zqs_render_density(C.c_void_p(density_ptr), W, H, D, C.byref(cam), C.c_void_p(rgba_ptr),
+                                 C.c_void_p(stream or 0)), "zqs_render_density")
+
+
+def save_ppm(path, rgba: np.ndarray, background=(0.0, 0.0, 0.0)):
+    """Write an RGBA image from the ray march (rows bottom first) as a binary PPM:
+    colour + transmittance * background, clamped to [0, 1], top row first."""
+    img = np.asarray(rgba, np.float32)
+    rgb = img[..., :3] + img[..., 3:4] * np.asarray(background, np.float32)
+    rgb = (np.clip(rgb, 0.0, 1.0)[::-1] * 255.0 + 0.5).astype(np.uint8)
+    with open(path, "wb") as f:
+        f.write(b"P6\n%d %d\n255\n" % (rgb.shape[1], rgb.shape[0]))
+        f.write(rgb.tobytes())
+
+
 class Stats(C.Structure):
     _fields_ = [("max_abs_div", C.c_double), ("residual_l2", C.c_double), ("div_mean_removed", C.c_double),
                 ("free_cells", C.c_int64)]
@@ -114,7 +148,8 @@ CAPI_SYMBOLS = [
     "zqs_sor_variant_info", "zqs_grid_set_sor_variant", "zqs_grid_synchronize", "zqs_grid_launch_count",
     "zqs_batch_create", "zqs_batch_destroy", "zqs_batch_step", "zqs_batch_use_graph", "zqs_batch_set_sor_variant",
     "zqs_batch_launch_count", "zqs_batch_synchronize",
-    "zqs_grid_set_force", "zqs_grid_stamp_objects", "zqs_adjoint_create", "zqs_adjoint_destroy", "zqs_adjoint_forward",
+    "zqs_grid_set_force", "zqs_grid_stamp_objects", "zqs_camera_default", "zqs_render_density", "zqs_grid_render",
+    "zqs_adjoint_create", "zqs_adjoint_destroy", "zqs_adjoint_forward",
     "zqs_adjoint_backward", "zqs_adjoint_download", "zqs_adjoint_get_info",
 ]
 LEGACY_C_SYMBOLS = ["ZQ_Cuda_Prepare_Advection", "Advect_Velocity", "Advect_Scalar", "AddForce3D",
@@ -185,6 +220,10 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.zqs_batch_synchronize.argtypes = [vp, vp]
     lib.zqs_grid_set_force.argtypes = [vp, vp, i, vp]
     lib.zqs_grid_stamp_objects.argtypes = [vp, vp, i, i, vp]
+    lib.zqs_camera_default.argtypes = [C.POINTER(Camera), i, i, i, i, i]
+    lib.zqs_camera_default.restype = None
+    lib.zqs_render_density.argtypes = [vp, i, i, i, C.POINTER(Camera), vp, vp]
+    lib.zqs_grid_render.argtypes = [vp, C.POINTER(Camera), vp, vp]
     lib.zqs_adjoint_create.argtypes = [C.POINTER(vp), vp, i, i]
     lib.zqs_adjoint_destroy.argtypes = [vp]
     lib.zqs_adjoint_forward.argtypes = [vp, vp, i, vp]
@@ -405,6 +444,11 @@ class Grid:
         check(self.lib.zqs_grid_stamp_objects(self.h, C.cast(arr, C.c_void_p), len(objs), int(closed_walls),
                                               C.c_void_p(stream or 0)), "zqs_grid_stamp_objects")
         del keep
+
+    def render(self, cam: Camera, rgba_ptr: int, stream: int | None = None):
+        """Ray march the current density into a device RGBA image (zqs_grid_render)."""
+        check(self.lib.zqs_grid_render(self.h, C.byref(cam), C.c_void_p(rgba_ptr), C.c_void_p(stream or 0)),
+              "zqs_grid_render")
 
     def set_force_device(self, dev_ptr: int, stream: int | None = None):
         check(self.lib.zqs_grid_set_force(self.h, C.c_void_p(dev_ptr), 1, C.c_void_p(stream or 0)),
