@@ -252,6 +252,14 @@ ZQS_API int zqs_batch_set_sor_variant(zqs_batch* b, int index, int zchunk);
 ZQS_API int64_t zqs_batch_launch_count(const zqs_batch* b);
 ZQS_API int zqs_batch_synchronize(zqs_batch* b, void* stream);
 
+/* Coarse solver, obstacle-free blocks (the dense block product of
+ * SubProjection3DCuda): 1 (default) = tcgen05 tensor cores in TF32 with the
+ * 3xTF32 split (relative error ~1e-6 against FP32), 0 = FP32 SIMT with
+ * fused multiply-adds in face order (bit-identical to the oracle).  A
+ * tensor-core wait that times out is reported by zqs_grid_synchronize
+ * (ZQS_ETIMEOUT). */
+ZQS_API int zqs_grid_set_coarse_gemm(zqs_grid* g, int mode);
+
 /* ---- moving voxel objects ---------------------------------------------------
  * ZQ_ApplyMovingObject3D (ZQ_SmokeSimulationUtils3D.cpp:1933-2046): the grid's
  * occupancy becomes the objects' voxels (every other cell free; all six

@@ -148,7 +148,7 @@ CAPI_SYMBOLS = [
     "zqs_sor_variant_info", "zqs_grid_set_sor_variant", "zqs_grid_synchronize", "zqs_grid_launch_count",
     "zqs_batch_create", "zqs_batch_destroy", "zqs_batch_step", "zqs_batch_use_graph", "zqs_batch_set_sor_variant",
     "zqs_batch_launch_count", "zqs_batch_synchronize",
-    "zqs_grid_set_force", "zqs_grid_stamp_objects", "zqs_camera_default", "zqs_render_density", "zqs_grid_render",
+    "zqs_grid_set_force", "zqs_grid_stamp_objects", "zqs_grid_set_coarse_gemm", "zqs_camera_default", "zqs_render_density", "zqs_grid_render",
     "zqs_adjoint_create", "zqs_adjoint_destroy", "zqs_adjoint_forward",
     "zqs_adjoint_backward", "zqs_adjoint_download", "zqs_adjoint_get_info",
 ]
@@ -220,6 +220,7 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.zqs_batch_synchronize.argtypes = [vp, vp]
     lib.zqs_grid_set_force.argtypes = [vp, vp, i, vp]
     lib.zqs_grid_stamp_objects.argtypes = [vp, vp, i, i, vp]
+    lib.zqs_grid_set_coarse_gemm.argtypes = [vp, i]
     lib.zqs_camera_default.argtypes = [C.POINTER(Camera), i, i, i, i, i]
     lib.zqs_camera_default.restype = None
     lib.zqs_render_density.argtypes = [vp, i, i, i, C.POINTER(Camera), vp, vp]
@@ -444,6 +445,10 @@ class Grid:
         check(self.lib.zqs_grid_stamp_objects(self.h, C.cast(arr, C.c_void_p), len(objs), int(closed_walls),
                                               C.c_void_p(stream or 0)), "zqs_grid_stamp_objects")
         del keep
+
+    def set_coarse_gemm(self, mode: int):
+        """Coarse solver's obstacle-free blocks: 1 tensor cores (3xTF32), 0 FP32 SIMT (exact)."""
+        check(self.lib.zqs_grid_set_coarse_gemm(self.h, int(mode)), "zqs_grid_set_coarse_gemm")
 
     def render(self, cam: Camera, rgba_ptr: int, stream: int | None = None):
         """Ray march the current density into a device RGBA image (zqs_grid_render)."""

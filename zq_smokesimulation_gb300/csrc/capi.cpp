@@ -347,7 +347,7 @@ ZQS_API int zqs_grid_set_params(zqs_grid* g, const zqs_params* p) {
     int rc = validate_params(*p);
     if (rc) return rc;
     if (p->solver == ZQS_SOLVER_COARSE_OPEN) {
-        rc = coarse_prepare(g->g.coarse, g->g.L, p->sub_size);
+        rc = coarse_prepare(g->g.coarse, g->g.L, p->sub_size, g->coarse_tc);
         if (rc) return rc;
     } else {
         coarse_free(g->g.coarse);
@@ -624,6 +624,21 @@ ZQS_API int zqs_grid_set_sor_variant(zqs_grid* g, int index, int zchunk) {
 ZQS_API int zqs_grid_synchronize(zqs_grid* g, void* stream) {
     if (!g) return set_error("NULL grid"), ZQS_EINVAL;
     ZQS_CUDA_TRY(cudaStreamSynchronize(g->pick(stream)));
+    return coarse_check(g->g.coarse, g->pick(stream));
+}
+
+ZQS_API int zqs_grid_set_coarse_gemm(zqs_grid* g, int mode) {
+    if (!g || mode < 0 || mode > 1) {
+        set_error("zqs_grid_set_coarse_gemm: mode must be 0 (FP32 SIMT) or 1 (tensor cores, 3xTF32)");
+        return ZQS_EINVAL;
+    }
+    g->coarse_tc = mode;
+    if (g->g.coarse) {
+        ZQS_CUDA_TRY(cudaStreamSynchronize(g->own));
+        int rc = coarse_prepare(g->g.coarse, g->g.L, g->g.coarse->s, mode);
+        if (rc) return rc;
+    }
+    g->drop_graphs();
     return ZQS_OK;
 }
 

@@ -373,50 +373,11 @@ __global__ void k_coarse2fine(Layout L, Layout Lc, int s, const uint8_t* __restr
     }
 }
 
-// Block face q (u: k, j, i <= s; v: k, j <= s, i; w: k <= s, j, i) of block
-// (bi, bj, bk) -> the fine face's padded index and component.
 __device__ __forceinline__ int block_face(const Layout& L, int s, int q, int bi, int bj, int bk, int& comp) {
-    const int nu = s * s * (s + 1);
-    int i, j, k;
-    if (q < nu) {
-        comp = 0;
-        i = q % (s + 1);
-        j = (q / (s + 1)) % s;
-        k = q / (s * (s + 1));
-    } else if (q < 2 * nu) {
-        comp = 1;
-        const int x = q - nu;
-        i = x % s;
-        j = (x / s) % (s + 1);
-        k = x / (s * (s + 1));
-    } else {
-        comp = 2;
-        const int x = q - 2 * nu;
-        i = x % s;
-        j = (x / s) % s;
-        k = x / (s * s);
-    }
-    return lidx(L, bi * s + i, bj * s + j, bk * s + k);
+    return subproj_block_face(L, s, q, bi, bj, bk, comp);
 }
 
-// Interior row r (u: k, j, i = 1..s-1; v: k, j = 1..s-1, i; w: k = 1..s-1, j, i)
-// -> block face index.
-__device__ __forceinline__ int interior_face(int s, int r) {
-    const int nu = s * s * (s + 1);
-    const int ni = s * s * (s - 1);
-    if (r < ni) {
-        const int i = 1 + r % (s - 1), j = (r / (s - 1)) % s, k = r / ((s - 1) * s);
-        return (k * s + j) * (s + 1) + i;
-    }
-    if (r < 2 * ni) {
-        const int x = r - ni;
-        const int i = x % s, j = 1 + (x / s) % (s - 1), k = x / (s * (s - 1));
-        return nu + (k * (s + 1) + j) * s + i;
-    }
-    const int x = r - 2 * ni;
-    const int i = x % s, j = (x / s) % s, k = 1 + x / (s * s);
-    return 2 * nu + (k * s + j) * s + i;
-}
+__device__ __forceinline__ int interior_face(int s, int r) { return subproj_interior_face(s, r); }
 
 __device__ __forceinline__ float* comp_ptr(int comp, float* u, float* v, float* w) {
     return comp == 0 ? u : (comp == 1 ? v : w);
@@ -746,7 +707,33 @@ Layout coarse_layout(int W, int H, int D) {
 
 }  // namespace
 
-int coarse_prepare(CoarseState*& cs, const Layout& L, int s) {
+namespace {
+
+// The tensor-core operands and the timeout flag of a state with s > 1.
+int coarse_alloc_tc(CoarseState* c) {
+    if (c->s < 2 || c->Xsplit) return ZQS_OK;
+    ZQS_CUDA_TRY(cudaMalloc(&c->Xsplit, subproj_tc_split_bytes(c->nblocks, c->nf)));
+    if (!c->err) {
+        ZQS_CUDA_TRY(cudaMalloc(&c->err, sizeof(int)));
+        ZQS_CUDA_TRY(cudaMemset(c->err, 0, sizeof(int)));
+    }
+    return ZQS_OK;
+}
+
+}  // namespace
+
+int coarse_check(CoarseState* cs, cudaStream_t st) {
+    if (!cs || !cs->err) return ZQS_OK;
+    ZQS_CUDA_TRY(cudaStreamSynchronize(st));
+    int flag = 0;
+    ZQS_CUDA_TRY(cudaMemcpy(&flag, cs->err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (!flag) return ZQS_OK;
+    ZQS_CUDA_TRY(cudaMemset(cs->err, 0, sizeof(int)));
+    set_error("coarse projection: a tensor-core pipeline wait timed out; those blocks were not projected");
+    return ZQS_ETIMEOUT;
+}
+
+int coarse_prepare(CoarseState*& cs, const Layout& L, int s, int tc) {
     if (s < 1 || L.W % s || L.H % s || L.D % s) {
         set_error("sub_size must be >= 1 and divide the grid's width, height and depth");
         return ZQS_EINVAL;
@@ -755,7 +742,10 @@ int coarse_prepare(CoarseState*& cs, const Layout& L, int s) {
         set_error("sub_size must be at most 10 (one thread per block cell)");
         return ZQS_EINVAL;
     }
-    if (cs && cs->s == s && cs->Lc.W == L.W / s && cs->Lc.H == L.H / s && cs->Lc.D == L.D / s) return ZQS_OK;
+    if (cs && cs->s == s && cs->Lc.W == L.W / s && cs->Lc.H == L.H / s && cs->Lc.D == L.D / s) {
+        cs->tc = tc ? 1 : 0;
+        return cs->tc ? coarse_alloc_tc(cs) : ZQS_OK;
+    }
     coarse_free(cs);
     CoarseState* c = new CoarseState();
     c->s = s;
@@ -803,11 +793,12 @@ int coarse_prepare(CoarseState*& cs, const Layout& L, int s) {
     c->bobs = (uint8_t*)b;
     b += bb;
     c->X = s > 1 ? (float*)b : nullptr;
+    c->tc = tc ? 1 : 0;
     if (s > 1) {
         int rc = get_mt(s, &c->MT);
+        if (!rc && c->tc) rc = coarse_alloc_tc(c);
         if (rc) {
-            cudaFree(c->base);
-            delete c;
+            coarse_free(c);
             return rc;
         }
     }
@@ -818,6 +809,8 @@ int coarse_prepare(CoarseState*& cs, const Layout& L, int s) {
 void coarse_free(CoarseState*& cs) {
     if (!cs) return;
     cudaFree(cs->base);
+    if (cs->Xsplit) cudaFree(cs->Xsplit);
+    if (cs->err) cudaFree(cs->err);
     delete cs;
     cs = nullptr;
 }
@@ -866,9 +859,16 @@ int launch_project_coarse(DevGrid& g, const KParams& kp, int K, cudaStream_t st,
         const long long total = (long long)cs->nblocks * cs->nf;
         k_subproj_gather<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(L, Lc, s, cs->nf, total, g.u, g.v, g.w,
                                                                             cs->X);
-        const dim3 gf((cs->rows + kGemmTile - 1) / kGemmTile, (cs->nblocks + kGemmTile - 1) / kGemmTile, 1);
-        k_subproj_fast<<<gf, kGemmThreads, 0, st>>>(L, Lc, s, cs->nf, cs->rows, cs->nblocks, cs->MT, cs->X,
-                                                    cs->bobs, g.u, g.v, g.w);
+        if (cs->tc && cs->Xsplit) {
+            int rc = launch_subproj_tc(L, Lc, s, cs->nf, cs->rows, cs->nblocks, cs->X, cs->Xsplit, cs->bobs, g.u,
+                                       g.v, g.w, cs->err, st, lc);
+            if (rc) return rc;
+            lc.n--;  // counted below with the other two
+        } else {
+            const dim3 gf((cs->rows + kGemmTile - 1) / kGemmTile, (cs->nblocks + kGemmTile - 1) / kGemmTile, 1);
+            k_subproj_fast<<<gf, kGemmThreads, 0, st>>>(L, Lc, s, cs->nf, cs->rows, cs->nblocks, cs->MT, cs->X,
+                                                        cs->bobs, g.u, g.v, g.w);
+        }
         int nthr = 32;
         while (nthr < s * s * s) nthr <<= 1;
         const size_t smo = (size_t)2 * nthr * sizeof(double) + (size_t)nthr * sizeof(int);

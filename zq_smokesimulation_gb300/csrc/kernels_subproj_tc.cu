@@ -1,0 +1,361 @@
+// Block sub-projection of obstacle-free blocks on the 5th-generation tensor
+// cores: Y = X M^T (X: blocks x faces, M: interior rows x faces, the dense
+// matrix of ZQ_InitSubMatPoisson3D, Utils3D:1151-1391) with tcgen05.mma in TF32
+// and the 3xTF32 split for FP32 accuracy:
+//   xh = x rounded to TF32 (10 mantissa bits, nearest even), xl = x - xh
+//   (exact) rounded to TF32, so the hardware's TF32 reads change neither;
+//   x m ~ xh mh + xh ml + xl mh   (the xl ml term, <= 2^-22 |x m|, is dropped).
+// One CTA of 128 threads owns a tile of 128 blocks x BN rows; the sums live in
+// tensor memory (128 lanes x BN fp32 columns) as two accumulators, the main
+// products xh mh in one and the small corrections xh ml + xl mh in the other,
+// added in FP32 at the end: the tensor cores' accumulation rounding then acts
+// on one third of the accumulation steps of the large sum.  K advances in chunks
+// of 32 faces (128 bytes per row: one 128-byte-swizzle atom row); each chunk's
+// four operand tiles (xh, xl, mh, ml) are copied to shared memory with
+// cp.async into the 128-byte-swizzled K-major layout, two stages deep; one
+// elected thread issues the 12 MMAs of a chunk (3 products x 4 K-steps of 8)
+// and commits them to the stage's mbarrier, which frees the stage for the copy
+// two chunks later.  The epilogue reads the accumulator with tcgen05.ld (one
+// TMEM lane per thread = one block) and writes each interior face.
+//
+// Every wait is bounded: on timeout the CTA records an error flag, stops
+// issuing work, waits (bounded) for the MMAs it issued, frees its tensor
+// memory and returns; the host reports the flag.
+#include <cstdint>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <vector>
+
+#include "zqs_coarse.h"
+
+namespace zqs {
+
+namespace {
+
+constexpr int kTcM = 128;         // blocks per tile (MMA M)
+constexpr int kTcK = 32;          // faces per K chunk (128 bytes of fp32)
+constexpr int kTcThreads = 128;   // one TMEM lane per thread
+constexpr int kTcStages = 2;
+constexpr int kTcMaxN = 256;      // rows per tile at most (MMA N)
+constexpr uint32_t kTcTmemCols = 512;   // two accumulators of up to 256 columns
+constexpr uint32_t kTcCorr = 256;       // column of the correction accumulator
+constexpr int kTileA = kTcM * kTcK * 4;      // 16 KB
+constexpr int kTileB = kTcMaxN * kTcK * 4;   // 32 KB
+constexpr int kStageBytes = 2 * kTileA + 2 * kTileB;
+constexpr size_t kTcSmem = (size_t)kTcStages * kStageBytes + 1024 + 64;
+constexpr long long kWaitLimit = 1LL << 24;  // try_wait polls before a wait gives up
+
+// FP32 -> TF32 (1 + 8 + 10 bits) by round to nearest even, as an FP32 bit pattern.
+__host__ __device__ __forceinline__ uint32_t tf32_rne_bits(uint32_t b) {
+    return (b + 0x0FFFu + ((b >> 13) & 1u)) & 0xFFFFE000u;
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait for the completion of the phase with this parity.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    for (long long n = 0; n < kWaitLimit; n++)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major operand, 128-byte swizzle, rows 128
+// bytes apart, 8-row groups 1024 bytes apart.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+    uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)1 << 16;             // leading byte offset (unused by this layout)
+    d |= (uint64_t)(1024 >> 4) << 32;   // stride byte offset
+    d |= (uint64_t)1 << 46;             // descriptor version
+    d |= (uint64_t)2 << 61;             // 128-byte swizzle
+    return d;
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+        "l"(da), "l"(db), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                 : "memory");
+}
+
+// 16 consecutive fp32 columns of this warp's 32 TMEM lanes (one per thread).
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+        "%14, %15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+}
+
+// Copy one operand tile (nrow rows of 32 floats from row-major src with
+// leading dimension ld) into the swizzled layout at dst.
+__device__ __forceinline__ void load_tile(uint32_t dst, const float* __restrict__ src, long long ld, int nrow) {
+    for (int e = threadIdx.x; e < nrow * 8; e += kTcThreads) {
+        const int r = e >> 3, c = e & 7;
+        cp_async16(dst + r * 128 + ((c ^ (r & 7)) << 4), src + (long long)r * ld + c * 4);
+    }
+}
+
+__global__ void __launch_bounds__(kTcThreads, 1)
+    k_subproj_tc(Layout L, Layout Lc, int s, int rows, int nblocks, int kpad, int bn,
+                 const float* __restrict__ Xh, const float* __restrict__ Xl, const float* __restrict__ Mh,
+                 const float* __restrict__ Ml, const uint8_t* __restrict__ bobs, float* __restrict__ u,
+                 float* __restrict__ v, float* __restrict__ w, int* __restrict__ err) {
+    extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
+    // 1024-byte alignment for the swizzle atoms
+    const uint32_t raw = smem_u32(tc_smem_raw);
+    const uint32_t base = (raw + 1023u) & ~1023u;
+    unsigned char* gbase = tc_smem_raw + (base - raw);
+    const uint32_t bars = base + kTcStages * kStageBytes;      // kTcStages mbarriers
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(gbase + kTcStages * kStageBytes + 32);
+    __shared__ int s_fail;
+
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int n0 = blockIdx.x * bn;        // first row of the tile
+    const int b0 = blockIdx.y * kTcM;      // first block of the tile
+    const int nk = kpad / kTcK;
+
+    if (tid == 0) {
+        s_fail = 0;
+        for (int q = 0; q < kTcStages; q++) mbar_init(bars + 8 * q, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(kTcTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    // kind::tf32: D f32 (bits 4-5 = 1), A and B tf32 (bits 7-9, 10-12 = 2), both
+    // K-major, N >> 3 at bit 17, M >> 4 at bit 24
+    const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(bn >> 3) << 17) | ((uint32_t)(kTcM >> 4) << 24);
+
+    const float* xh = Xh + (long long)b0 * kpad;
+    const float* xl = Xl + (long long)b0 * kpad;
+    const float* mh = Mh + (long long)n0 * kpad;
+    const float* ml = Ml + (long long)n0 * kpad;
+    auto stage_addr = [&](int st) { return base + st * kStageBytes; };
+    auto issue_load = [&](int kc, int st) {
+        const uint32_t sa = stage_addr(st);
+        const int k0 = kc * kTcK;
+        load_tile(sa, xh + k0, kpad, kTcM);
+        load_tile(sa + kTileA, xl + k0, kpad, kTcM);
+        load_tile(sa + 2 * kTileA, mh + k0, kpad, bn);
+        load_tile(sa + 2 * kTileA + kTileB, ml + k0, kpad, bn);
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+
+    int issued = 0;  // chunks whose MMAs were issued (thread 0)
+    issue_load(0, 0);
+    for (int kc = 0; kc < nk; kc++) {
+        const int st = kc % kTcStages;
+        bool my_fail = false;
+        if (kc + 1 < nk) {
+            const int st1 = (kc + 1) % kTcStages;
+            // the stage was last read by the MMAs of chunk kc + 1 - kTcStages,
+            // the (chunk / kTcStages)-th completion of its barrier
+            if (kc + 1 >= kTcStages)
+                my_fail = !mbar_wait(bars + 8 * st1, (uint32_t)(((kc + 1 - kTcStages) / kTcStages) & 1));
+            if (!my_fail) issue_load(kc + 1, st1);
+            asm volatile("cp.async.wait_group 1;" ::: "memory");
+        } else {
+            asm volatile("cp.async.wait_group 0;" ::: "memory");
+        }
+        if (my_fail) s_fail = 1;
+        // the copies of chunk kc, written through the generic proxy, become
+        // visible to the tensor cores (async proxy)
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (s_fail) break;  // uniform: read by every thread after the barrier
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t sa = stage_addr(st);
+            const uint32_t ah = sa, al = sa + kTileA, bh = sa + 2 * kTileA, bl = sa + 2 * kTileA + kTileB;
+#pragma unroll
+            for (int k = 0; k < kTcK / 8; k++) {
+                const uint32_t off = k * 32;  // 8 tf32 = 32 bytes along K
+                const uint32_t acc = (kc > 0 || k > 0) ? 1u : 0u;
+                mma_tf32(tmem, sw128_desc(ah + off), sw128_desc(bh + off), idesc, acc);
+                mma_tf32(tmem + kTcCorr, sw128_desc(ah + off), sw128_desc(bl + off), idesc, acc);
+                mma_tf32(tmem + kTcCorr, sw128_desc(al + off), sw128_desc(bh + off), idesc, 1u);
+            }
+            mma_commit(bars + 8 * st);
+            issued = kc + 1;
+        }
+    }
+    __syncthreads();
+    // every issued MMA done: a commit tracks all earlier MMAs of the thread
+    if (tid == 0 && issued > 0) {
+        const int last = issued - 1;
+        if (!mbar_wait(bars + 8 * (last % kTcStages), (uint32_t)((last / kTcStages) & 1))) s_fail = 1;
+    }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const bool ok = !s_fail;
+    if (ok) {
+        const int gb = b0 + tid;  // this thread's block (TMEM lane tid)
+        const bool live = gb < nblocks && !bobs[gb];
+        const int bi = gb % Lc.W, bj = (gb / Lc.W) % Lc.H, bk = gb / (Lc.W * Lc.H);
+        const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+        for (int c0 = 0; c0 < bn; c0 += 16) {
+            uint32_t r[16], rc[16];
+            tmem_ld16(lane_base + (uint32_t)c0, r);
+            tmem_ld16(lane_base + kTcCorr + (uint32_t)c0, rc);
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (live) {
+#pragma unroll
+                for (int q = 0; q < 16; q++) {
+                    const int row = n0 + c0 + q;
+                    if (row < rows) {
+                        const int f = subproj_interior_face(s, row);
+                        int comp;
+                        const int c = subproj_block_face(L, s, f, bi, bj, bk, comp);
+                        (comp == 0 ? u : (comp == 1 ? v : w))[c] = __uint_as_float(r[q]) + __uint_as_float(rc[q]);
+                    }
+                }
+            }
+        }
+    } else if (tid == 0) {
+        atomicExch(err, 1);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcTmemCols)
+                     : "memory");
+    }
+}
+
+// xh / xl split of the gathered faces, row-padded to kpad and block-padded to
+// a multiple of 128 with zeros.
+__global__ void k_split_tf32(const float* __restrict__ X, int nf, int nblocks, int kpad, long long total,
+                             float* __restrict__ Xh, float* __restrict__ Xl) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= total) return;
+    const int b = (int)(e / kpad), q = (int)(e - (long long)b * kpad);
+    const float x = (b < nblocks && q < nf) ? __ldg(X + (long long)b * nf + q) : 0.0f;
+    const float hi = __uint_as_float(tf32_rne_bits(__float_as_uint(x)));
+    Xh[e] = hi;
+    Xl[e] = __uint_as_float(tf32_rne_bits(__float_as_uint(x - hi)));
+}
+
+struct MSplit {
+    float* h = nullptr;
+    float* l = nullptr;
+    int kpad = 0, bn = 0, ntiles = 0;
+};
+std::mutex g_ms_mu;
+std::map<int, MSplit> g_ms;
+
+int get_msplit(int s, MSplit& out) {
+    std::lock_guard<std::mutex> lk(g_ms_mu);
+    auto it = g_ms.find(s);
+    if (it != g_ms.end()) {
+        out = it->second;
+        return ZQS_OK;
+    }
+    const std::vector<float> M = coarse_submatrix(s);
+    const int nf = 3 * s * s * (s + 1), rows = 3 * s * s * (s - 1);
+    MSplit m;
+    m.kpad = (nf + kTcK - 1) / kTcK * kTcK;
+    m.ntiles = (rows + kTcMaxN - 1) / kTcMaxN;
+    m.bn = ((rows + m.ntiles - 1) / m.ntiles + 15) / 16 * 16;
+    const size_t n = (size_t)m.ntiles * m.bn * m.kpad;
+    std::vector<float> h(n, 0.0f), l(n, 0.0f);
+    for (int r = 0; r < rows; r++)
+        for (int q = 0; q < nf; q++) {
+            const float x = M[(size_t)r * nf + q];
+            uint32_t bits;
+            std::memcpy(&bits, &x, 4);
+            bits = tf32_rne_bits(bits);
+            float hi, lo;
+            std::memcpy(&hi, &bits, 4);
+            const float rest = x - hi;
+            std::memcpy(&bits, &rest, 4);
+            bits = tf32_rne_bits(bits);
+            std::memcpy(&lo, &bits, 4);
+            h[(size_t)r * m.kpad + q] = hi;
+            l[(size_t)r * m.kpad + q] = lo;
+        }
+    ZQS_CUDA_TRY(cudaMalloc(&m.h, n * sizeof(float)));
+    cudaError_t e = cudaMalloc(&m.l, n * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemcpy(m.h, h.data(), n * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(m.l, l.data(), n * sizeof(float), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(m.h);
+        cudaFree(m.l);
+        return cuda_fail(e, "tensor-core sub-projection matrix upload");
+    }
+    g_ms[s] = m;
+    out = m;
+    return ZQS_OK;
+}
+
+}  // namespace
+
+size_t subproj_tc_split_bytes(int nblocks, int nf) {
+    const long long kpad = (nf + kTcK - 1) / kTcK * kTcK;
+    const long long bpad = (nblocks + kTcM - 1) / kTcM * kTcM;
+    return (size_t)(2 * bpad * kpad) * sizeof(float);
+}
+
+int launch_subproj_tc(const Layout& L, const Layout& Lc, int s, int nf, int rows, int nblocks, const float* X,
+                      float* Xsplit, const uint8_t* bobs, float* u, float* v, float* w, int* err, cudaStream_t st,
+                      LaunchCounter& lc) {
+    MSplit m;
+    int rc = get_msplit(s, m);
+    if (rc) return rc;
+    static bool attr_set = false;
+    if (!attr_set) {
+        ZQS_CUDA_TRY(cudaFuncSetAttribute(k_subproj_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem));
+        attr_set = true;
+    }
+    const long long bpad = (nblocks + kTcM - 1) / kTcM * kTcM;
+    const long long total = bpad * m.kpad;
+    float* Xh = Xsplit;
+    float* Xl = Xsplit + total;
+    k_split_tf32<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(X, nf, nblocks, m.kpad, total, Xh, Xl);
+    const dim3 grid(m.ntiles, (unsigned)(bpad / kTcM), 1);
+    k_subproj_tc<<<grid, kTcThreads, kTcSmem, st>>>(L, Lc, s, rows, nblocks, m.kpad, m.bn, Xh, Xl, m.h, m.l, bobs, u,
+                                                    v, w, err);
+    lc.n += 2;
+    ZQS_LAUNCH_CHECK("k_subproj_tc");
+    return ZQS_OK;
+}
+
+}  // namespace zqs

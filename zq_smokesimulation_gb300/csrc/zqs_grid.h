@@ -29,6 +29,7 @@ struct zqs_grid {
     long long gen = 0;  // bumped whenever parameters, occupancy or the SOR setup change
     float* fext_base = nullptr;  // external per-cell force, 3 padded cell fields (allocated on first use)
     bool fext_on = false;
+    int coarse_tc = 1;            // coarse solver's obstacle-free blocks: 1 tensor cores, 0 FP32 SIMT
     uint8_t* obj_mask = nullptr;  // device copy of a moving object's voxel mask (grown on demand)
     size_t obj_mask_cap = 0;
 
