@@ -131,6 +131,28 @@ def test_coarse_steps_match_oracle(zqs_lib, oracle32):
     g.close()
 
 
+def test_coarse_step_graph_first_use(zqs_lib, oracle32):
+    """A block edge no other test uses (s = 6): its tensor-core matrix is
+    prepared with the parameters, so the first step can be captured into a CUDA
+    graph (no allocation inside the capture)."""
+    W, H, D = 12, 12, 12
+    w0 = wl.small_case(W, H, D, K=10, vel_amp=0.3)
+    w0.params.solver = capi.SOLVER_COARSE_OPEN
+    w0.params.sub_size = 6
+    g = capi.Grid(W, H, D)
+    g.set_params(w0.params)
+    g.load_state(w0.occ, w0.u, w0.v, w0.w, w0.T, w0.rho)
+    g.step(2)
+    g.sync()
+    out = g.state()
+    st = oracle32.state(w0)
+    rc, _ = oracle32.step(W, H, D, st, w0.occ, w0.params, 2)
+    assert rc == 0
+    for k in ("u", "v", "w", "T", "rho"):
+        assert rel_l2(out[k], st[k]) <= 1e-5, k
+    g.close()
+
+
 def test_coarse_parameter_checks(zqs_lib):
     g = capi.Grid(12, 12, 12)
     p = wl.smoke_params(12, 5, solver=capi.SOLVER_COARSE_OPEN)

@@ -712,6 +712,8 @@ namespace {
 // The tensor-core operands and the timeout flag of a state with s > 1.
 int coarse_alloc_tc(CoarseState* c) {
     if (c->s < 2 || c->Xsplit) return ZQS_OK;
+    int rc = subproj_tc_prepare(c->s);
+    if (rc) return rc;
     ZQS_CUDA_TRY(cudaMalloc(&c->Xsplit, subproj_tc_split_bytes(c->nblocks, c->nf)));
     if (!c->err) {
         ZQS_CUDA_TRY(cudaMalloc(&c->err, sizeof(int)));

@@ -10,17 +10,19 @@
 // products xh mh in one and the small corrections xh ml + xl mh in the other,
 // added in FP32 at the end: the tensor cores' accumulation rounding then acts
 // on one third of the accumulation steps of the large sum.  K advances in chunks
-// of 32 faces (128 bytes per row: one 128-byte-swizzle atom row); each chunk's
-// four operand tiles (xh, xl, mh, ml) are copied to shared memory with
-// cp.async into the 128-byte-swizzled K-major layout, two stages deep; one
-// elected thread issues the 12 MMAs of a chunk (3 products x 4 K-steps of 8)
-// and commits them to the stage's mbarrier, which frees the stage for the copy
-// two chunks later.  The epilogue reads the accumulator with tcgen05.ld (one
+// of 16 faces (64-byte rows); each chunk's four operand tiles (xh, xl, mh, ml)
+// are copied to shared memory with cp.async into the 64-byte-swizzled K-major
+// layout, as many stages as shared memory holds (5 at BN = 224), the copies
+// running two chunks behind the stage ring so that one elected thread can
+// queue the 6 MMAs of a chunk (3 products x 2 K-steps of 8) while the previous
+// chunk's MMAs still run; each chunk's MMAs commit to its stage's mbarrier,
+// which frees the stage for the copy of a later chunk.  The epilogue reads the accumulator with tcgen05.ld (one
 // TMEM lane per thread = one block) and writes each interior face.
 //
 // Every wait is bounded: on timeout the CTA records an error flag, stops
 // issuing work, waits (bounded) for the MMAs it issued, frees its tensor
 // memory and returns; the host reports the flag.
+#include <algorithm>
 #include <cstdint>
 #include <cstring>
 #include <map>
@@ -34,16 +36,17 @@ namespace zqs {
 namespace {
 
 constexpr int kTcM = 128;         // blocks per tile (MMA M)
-constexpr int kTcK = 32;          // faces per K chunk (128 bytes of fp32)
+constexpr int kTcK = 16;          // faces per K chunk (64 bytes of fp32)
+constexpr int kTcPad = 32;        // faces are padded to a multiple of this
 constexpr int kTcThreads = 128;   // one TMEM lane per thread
-constexpr int kTcStages = 2;
+constexpr int kTcMaxStages = 8;
+constexpr int kTcAhead = 2;       // stages between the chunk being copied and the chunk consumed
 constexpr int kTcMaxN = 256;      // rows per tile at most (MMA N)
 constexpr uint32_t kTcTmemCols = 512;   // two accumulators of up to 256 columns
 constexpr uint32_t kTcCorr = 256;       // column of the correction accumulator
-constexpr int kTileA = kTcM * kTcK * 4;      // 16 KB
-constexpr int kTileB = kTcMaxN * kTcK * 4;   // 32 KB
-constexpr int kStageBytes = 2 * kTileA + 2 * kTileB;
-constexpr size_t kTcSmem = (size_t)kTcStages * kStageBytes + 1024 + 64;
+constexpr int kTileA = kTcM * kTcK * 4;      // 8 KB
+constexpr int kSmemBudget = 224 * 1024;       // dynamic: 227 KB less the kernel's static shared memory
+constexpr int kSmemExtra = 1024 + 128;       // alignment slack, barriers, TMEM address
 constexpr long long kWaitLimit = 1LL << 24;  // try_wait polls before a wait gives up
 
 // FP32 -> TF32 (1 + 8 + 10 bits) by round to nearest even, as an FP32 bit pattern.
@@ -80,14 +83,27 @@ __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
 }
 
-// Shared-memory matrix descriptor: K-major operand, 128-byte swizzle, rows 128
-// bytes apart, 8-row groups 1024 bytes apart.
-__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+// Wait until at most n of this thread's cp.async groups are pending.
+__device__ __forceinline__ void cp_async_wait_pending(int n) {
+    switch (n) {
+        case 0: asm volatile("cp.async.wait_group 0;" ::: "memory"); break;
+        case 1: asm volatile("cp.async.wait_group 1;" ::: "memory"); break;
+        case 2: asm volatile("cp.async.wait_group 2;" ::: "memory"); break;
+        case 3: asm volatile("cp.async.wait_group 3;" ::: "memory"); break;
+        case 4: asm volatile("cp.async.wait_group 4;" ::: "memory"); break;
+        default: asm volatile("cp.async.wait_group 5;" ::: "memory"); break;
+    }
+}
+
+// Shared-memory matrix descriptor: K-major operand, 64-byte swizzle (16-byte
+// chunk c of row r stored at chunk c ^ ((r >> 1) & 3)), rows 64 bytes apart,
+// 8-row groups 512 bytes apart.
+__device__ __forceinline__ uint64_t sw64_desc(uint32_t saddr) {
     uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
     d |= (uint64_t)1 << 16;             // leading byte offset (unused by this layout)
-    d |= (uint64_t)(1024 >> 4) << 32;   // stride byte offset
+    d |= (uint64_t)(512 >> 4) << 32;    // stride byte offset
     d |= (uint64_t)1 << 46;             // descriptor version
-    d |= (uint64_t)2 << 61;             // 128-byte swizzle
+    d |= (uint64_t)4 << 61;             // 64-byte swizzle
     return d;
 }
 
@@ -115,12 +131,12 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
         : "r"(taddr));
 }
 
-// Copy one operand tile (nrow rows of 32 floats from row-major src with
-// leading dimension ld) into the swizzled layout at dst.
+// Copy one operand tile (nrow rows of 16 floats from row-major src with
+// leading dimension ld) into the 64-byte-swizzled layout at dst.
 __device__ __forceinline__ void load_tile(uint32_t dst, const float* __restrict__ src, long long ld, int nrow) {
-    for (int e = threadIdx.x; e < nrow * 8; e += kTcThreads) {
-        const int r = e >> 3, c = e & 7;
-        cp_async16(dst + r * 128 + ((c ^ (r & 7)) << 4), src + (long long)r * ld + c * 4);
+    for (int e = threadIdx.x; e < nrow * 4; e += kTcThreads) {
+        const int r = e >> 2, c = e & 3;
+        cp_async16(dst + r * 64 + ((c ^ ((r >> 1) & 3)) << 4), src + (long long)r * ld + c * 4);
     }
 }
 
@@ -128,24 +144,38 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     k_subproj_tc(Layout L, Layout Lc, int s, int rows, int nblocks, int kpad, int bn,
                  const float* __restrict__ Xh, const float* __restrict__ Xl, const float* __restrict__ Mh,
                  const float* __restrict__ Ml, const uint8_t* __restrict__ bobs, float* __restrict__ u,
-                 float* __restrict__ v, float* __restrict__ w, int* __restrict__ err) {
+                 float* __restrict__ v, float* __restrict__ w, int nstages, int* __restrict__ err) {
     extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
     // 1024-byte alignment for the swizzle atoms
     const uint32_t raw = smem_u32(tc_smem_raw);
     const uint32_t base = (raw + 1023u) & ~1023u;
     unsigned char* gbase = tc_smem_raw + (base - raw);
-    const uint32_t bars = base + kTcStages * kStageBytes;      // kTcStages mbarriers
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(gbase + kTcStages * kStageBytes + 32);
+    const int tile_b = bn * kTcK * 4;                     // a multiple of 1024 (bn % 16 == 0)
+    const int stage_bytes = 2 * kTileA + 2 * tile_b;
+    const uint32_t bars = base + nstages * stage_bytes;   // nstages mbarriers
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(gbase + nstages * stage_bytes + 8 * kTcMaxStages);
     __shared__ int s_fail;
+    // per row of the tile: the face's offset from its block's corner cell in
+    // the padded layout (i + j px + k plane) and its component, -1 past the rows
+    __shared__ int s_off[kTcMaxN];
+    __shared__ int s_comp[kTcMaxN];
 
     const int tid = threadIdx.x, warp = tid >> 5;
     const int n0 = blockIdx.x * bn;        // first row of the tile
     const int b0 = blockIdx.y * kTcM;      // first block of the tile
     const int nk = kpad / kTcK;
 
+    for (int q = tid; q < bn; q += kTcThreads) {
+        const int row = n0 + q;
+        int comp = -1, off = 0;
+        if (row < rows) off = subproj_block_face(L, s, subproj_interior_face(s, row), 0, 0, 0, comp) - lidx(L, 0, 0, 0);
+        s_off[q] = off;
+        s_comp[q] = comp;
+    }
+
     if (tid == 0) {
         s_fail = 0;
-        for (int q = 0; q < kTcStages; q++) mbar_init(bars + 8 * q, 1);
+        for (int q = 0; q < nstages; q++) mbar_init(bars + 8 * q, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
@@ -167,33 +197,35 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     const float* xl = Xl + (long long)b0 * kpad;
     const float* mh = Mh + (long long)n0 * kpad;
     const float* ml = Ml + (long long)n0 * kpad;
-    auto stage_addr = [&](int st) { return base + st * kStageBytes; };
-    auto issue_load = [&](int kc, int st) {
-        const uint32_t sa = stage_addr(st);
-        const int k0 = kc * kTcK;
-        load_tile(sa, xh + k0, kpad, kTcM);
-        load_tile(sa + kTileA, xl + k0, kpad, kTcM);
-        load_tile(sa + 2 * kTileA, mh + k0, kpad, bn);
-        load_tile(sa + 2 * kTileA + kTileB, ml + k0, kpad, bn);
+    auto stage_addr = [&](int st) { return base + st * stage_bytes; };
+    // one commit group per chunk index (empty past the last chunk), so that
+    // "at most PD groups pending" always means "chunk kc has landed"
+    auto issue_load = [&](int kc) {
+        if (kc < nk) {
+            const uint32_t sa = stage_addr(kc % nstages);
+            const int k0 = kc * kTcK;
+            load_tile(sa, xh + k0, kpad, kTcM);
+            load_tile(sa + kTileA, xl + k0, kpad, kTcM);
+            load_tile(sa + 2 * kTileA, mh + k0, kpad, bn);
+            load_tile(sa + 2 * kTileA + tile_b, ml + k0, kpad, bn);
+        }
         asm volatile("cp.async.commit_group;" ::: "memory");
     };
+    const int PD = nstages - kTcAhead;  // chunks copied ahead of the one consumed
 
     int issued = 0;  // chunks whose MMAs were issued (thread 0)
-    issue_load(0, 0);
+    for (int j = 0; j < PD; j++) issue_load(j);
     for (int kc = 0; kc < nk; kc++) {
-        const int st = kc % kTcStages;
+        const int st = kc % nstages;
         bool my_fail = false;
-        if (kc + 1 < nk) {
-            const int st1 = (kc + 1) % kTcStages;
-            // the stage was last read by the MMAs of chunk kc + 1 - kTcStages,
-            // the (chunk / kTcStages)-th completion of its barrier
-            if (kc + 1 >= kTcStages)
-                my_fail = !mbar_wait(bars + 8 * st1, (uint32_t)(((kc + 1 - kTcStages) / kTcStages) & 1));
-            if (!my_fail) issue_load(kc + 1, st1);
-            asm volatile("cp.async.wait_group 1;" ::: "memory");
-        } else {
-            asm volatile("cp.async.wait_group 0;" ::: "memory");
-        }
+        // chunk j goes into the stage chunk j - nstages used: its MMAs (issued
+        // kTcAhead chunks ago, at kc - kTcAhead) must have completed; the MMAs
+        // of chunk kc - 1 may still run
+        const int j = kc + PD;
+        if (j < nk && j >= nstages)
+            my_fail = !mbar_wait(bars + 8 * (j % nstages), (uint32_t)(((j - nstages) / nstages) & 1));
+        if (!my_fail) issue_load(j);
+        cp_async_wait_pending(PD);
         if (my_fail) s_fail = 1;
         // the copies of chunk kc, written through the generic proxy, become
         // visible to the tensor cores (async proxy)
@@ -203,14 +235,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         if (tid == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const uint32_t sa = stage_addr(st);
-            const uint32_t ah = sa, al = sa + kTileA, bh = sa + 2 * kTileA, bl = sa + 2 * kTileA + kTileB;
+            const uint32_t ah = sa, al = sa + kTileA, bh = sa + 2 * kTileA, bl = sa + 2 * kTileA + tile_b;
 #pragma unroll
             for (int k = 0; k < kTcK / 8; k++) {
                 const uint32_t off = k * 32;  // 8 tf32 = 32 bytes along K
                 const uint32_t acc = (kc > 0 || k > 0) ? 1u : 0u;
-                mma_tf32(tmem, sw128_desc(ah + off), sw128_desc(bh + off), idesc, acc);
-                mma_tf32(tmem + kTcCorr, sw128_desc(ah + off), sw128_desc(bl + off), idesc, acc);
-                mma_tf32(tmem + kTcCorr, sw128_desc(al + off), sw128_desc(bh + off), idesc, 1u);
+                mma_tf32(tmem, sw64_desc(ah + off), sw64_desc(bh + off), idesc, acc);
+                mma_tf32(tmem + kTcCorr, sw64_desc(ah + off), sw64_desc(bl + off), idesc, acc);
+                mma_tf32(tmem + kTcCorr, sw64_desc(al + off), sw64_desc(bh + off), idesc, 1u);
             }
             mma_commit(bars + 8 * st);
             issued = kc + 1;
@@ -220,7 +252,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     // every issued MMA done: a commit tracks all earlier MMAs of the thread
     if (tid == 0 && issued > 0) {
         const int last = issued - 1;
-        if (!mbar_wait(bars + 8 * (last % kTcStages), (uint32_t)((last / kTcStages) & 1))) s_fail = 1;
+        if (!mbar_wait(bars + 8 * (last % nstages), (uint32_t)((last / nstages) & 1))) s_fail = 1;
     }
     asm volatile("cp.async.wait_group 0;" ::: "memory");
     __syncthreads();
@@ -230,6 +262,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         const int gb = b0 + tid;  // this thread's block (TMEM lane tid)
         const bool live = gb < nblocks && !bobs[gb];
         const int bi = gb % Lc.W, bj = (gb / Lc.W) % Lc.H, bk = gb / (Lc.W * Lc.H);
+        const int corner = lidx(L, bi * s, bj * s, bk * s);
         const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
         for (int c0 = 0; c0 < bn; c0 += 16) {
             uint32_t r[16], rc[16];
@@ -239,13 +272,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             if (live) {
 #pragma unroll
                 for (int q = 0; q < 16; q++) {
-                    const int row = n0 + c0 + q;
-                    if (row < rows) {
-                        const int f = subproj_interior_face(s, row);
-                        int comp;
-                        const int c = subproj_block_face(L, s, f, bi, bj, bk, comp);
-                        (comp == 0 ? u : (comp == 1 ? v : w))[c] = __uint_as_float(r[q]) + __uint_as_float(rc[q]);
-                    }
+                    const int comp = s_comp[c0 + q];
+                    if (comp >= 0)
+                        (comp == 0 ? u : (comp == 1 ? v : w))[corner + s_off[c0 + q]] =
+                            __uint_as_float(r[q]) + __uint_as_float(rc[q]);
                 }
             }
         }
@@ -292,7 +322,7 @@ int get_msplit(int s, MSplit& out) {
     const std::vector<float> M = coarse_submatrix(s);
     const int nf = 3 * s * s * (s + 1), rows = 3 * s * s * (s - 1);
     MSplit m;
-    m.kpad = (nf + kTcK - 1) / kTcK * kTcK;
+    m.kpad = (nf + kTcPad - 1) / kTcPad * kTcPad;
     m.ntiles = (rows + kTcMaxN - 1) / kTcMaxN;
     m.bn = ((rows + m.ntiles - 1) / m.ntiles + 15) / 16 * 16;
     const size_t n = (size_t)m.ntiles * m.bn * m.kpad;
@@ -328,8 +358,20 @@ int get_msplit(int s, MSplit& out) {
 
 }  // namespace
 
+int subproj_tc_prepare(int s) {
+    MSplit m;
+    int rc = get_msplit(s, m);
+    if (rc) return rc;
+    static bool attr_set = false;
+    if (!attr_set) {
+        ZQS_CUDA_TRY(cudaFuncSetAttribute(k_subproj_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBudget));
+        attr_set = true;
+    }
+    return ZQS_OK;
+}
+
 size_t subproj_tc_split_bytes(int nblocks, int nf) {
-    const long long kpad = (nf + kTcK - 1) / kTcK * kTcK;
+    const long long kpad = (nf + kTcPad - 1) / kTcPad * kTcPad;
     const long long bpad = (nblocks + kTcM - 1) / kTcM * kTcM;
     return (size_t)(2 * bpad * kpad) * sizeof(float);
 }
@@ -338,21 +380,34 @@ int launch_subproj_tc(const Layout& L, const Layout& Lc, int s, int nf, int rows
                       float* Xsplit, const uint8_t* bobs, float* u, float* v, float* w, int* err, cudaStream_t st,
                       LaunchCounter& lc) {
     MSplit m;
-    int rc = get_msplit(s, m);
-    if (rc) return rc;
-    static bool attr_set = false;
-    if (!attr_set) {
-        ZQS_CUDA_TRY(cudaFuncSetAttribute(k_subproj_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem));
-        attr_set = true;
+    {
+        // prepared by subproj_tc_prepare (no allocation here: this may run
+        // inside a stream capture)
+        std::lock_guard<std::mutex> lk(g_ms_mu);
+        auto it = g_ms.find(s);
+        if (it == g_ms.end()) {
+            set_error("tensor-core sub-projection: matrix for this sub_size not prepared");
+            return ZQS_ENOTREADY;
+        }
+        m = it->second;
     }
+    // as many stages as fit (kTcAhead + 1 .. kTcMaxStages); the copies run
+    // nstages - kTcAhead chunks ahead (at most 5 pending groups)
+    const int stage_bytes = 2 * kTileA + 2 * m.bn * kTcK * 4;
+    const int nstages = std::min(std::min(kTcMaxStages, kTcAhead + 5), (kSmemBudget - kSmemExtra) / stage_bytes);
+    if (nstages < kTcAhead + 1) {
+        set_error("tensor-core sub-projection: the operand stages do not fit in shared memory");
+        return ZQS_EUNSUPPORTED;
+    }
+    const size_t smem = (size_t)nstages * stage_bytes + kSmemExtra;
     const long long bpad = (nblocks + kTcM - 1) / kTcM * kTcM;
     const long long total = bpad * m.kpad;
     float* Xh = Xsplit;
     float* Xl = Xsplit + total;
     k_split_tf32<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(X, nf, nblocks, m.kpad, total, Xh, Xl);
     const dim3 grid(m.ntiles, (unsigned)(bpad / kTcM), 1);
-    k_subproj_tc<<<grid, kTcThreads, kTcSmem, st>>>(L, Lc, s, rows, nblocks, m.kpad, m.bn, Xh, Xl, m.h, m.l, bobs, u,
-                                                    v, w, err);
+    k_subproj_tc<<<grid, kTcThreads, smem, st>>>(L, Lc, s, rows, nblocks, m.kpad, m.bn, Xh, Xl, m.h, m.l, bobs, u,
+                                                 v, w, nstages, err);
     lc.n += 2;
     ZQS_LAUNCH_CHECK("k_subproj_tc");
     return ZQS_OK;

@@ -82,6 +82,9 @@ __device__ __forceinline__ int subproj_interior_face(int s, int r) {
 int coarse_prepare(CoarseState*& cs, const Layout& L, int s, int tc);
 void coarse_free(CoarseState*& cs);
 
+// The split matrix of block edge s on the device (cached per s) and the
+// kernel's shared-memory limit: before the first launch, outside any capture.
+int subproj_tc_prepare(int s);
 // Bytes of the tensor-core operand split (xh, xl) for nblocks blocks of nf faces.
 size_t subproj_tc_split_bytes(int nblocks, int nf);
 // Obstacle-free blocks on the tensor cores: split X into Xsplit, then
