@@ -9,19 +9,23 @@
 // tensor memory (128 lanes x BN fp32 columns) as two accumulators, the main
 // products xh mh in one and the small corrections xh ml + xl mh in the other,
 // added in FP32 at the end: the tensor cores' accumulation rounding then acts
-// on one third of the accumulation steps of the large sum.  K advances in chunks
-// of 16 faces (64-byte rows); each chunk's four operand tiles (xh, xl, mh, ml)
-// are copied to shared memory with cp.async into the 64-byte-swizzled K-major
-// layout, as many stages as shared memory holds (5 at BN = 224), the copies
-// running two chunks behind the stage ring so that one elected thread can
-// queue the 6 MMAs of a chunk (3 products x 2 K-steps of 8) while the previous
-// chunk's MMAs still run; each chunk's MMAs commit to its stage's mbarrier,
-// which frees the stage for the copy of a later chunk.  The epilogue reads the accumulator with tcgen05.ld (one
-// TMEM lane per thread = one block) and writes each interior face.
+// on one third of the accumulation steps of the large sum.
+//
+// Operands are stored in global memory as the exact shared-memory images the
+// MMAs read: per (tile, chunk of 16 faces) the hi then the lo tile, each row
+// 64 bytes in the 64-byte-swizzled K-major layout.  So one chunk is two
+// contiguous bulk copies (cp.async.bulk, 16 KB of X and 2 BN x 64 bytes of M)
+// whose arrival an mbarrier counts in bytes.  Warp 0 (one lane) produces:
+// waits for a stage to be released, posts the byte count, issues the copies;
+// warp 1 (one lane) consumes: waits for the bytes, issues the 6 MMAs of the
+// chunk (3 products x 2 K-steps of 8) and commits them to the stage's release
+// barrier; a last commit marks the accumulators complete.  Then all four warps
+// read the accumulators with tcgen05.ld (one TMEM lane per thread = one block)
+// and write each interior face through a per-row offset table.
 //
 // Every wait is bounded: on timeout the CTA records an error flag, stops
-// issuing work, waits (bounded) for the MMAs it issued, frees its tensor
-// memory and returns; the host reports the flag.
+// issuing work, waits (bounded) for what it issued, frees its tensor memory
+// and returns; the host reports the flag.
 #include <algorithm>
 #include <cstdint>
 #include <cstring>
@@ -40,13 +44,12 @@ constexpr int kTcK = 16;          // faces per K chunk (64 bytes of fp32)
 constexpr int kTcPad = 32;        // faces are padded to a multiple of this
 constexpr int kTcThreads = 128;   // one TMEM lane per thread
 constexpr int kTcMaxStages = 8;
-constexpr int kTcAhead = 2;       // stages between the chunk being copied and the chunk consumed
 constexpr int kTcMaxN = 256;      // rows per tile at most (MMA N)
 constexpr uint32_t kTcTmemCols = 512;   // two accumulators of up to 256 columns
 constexpr uint32_t kTcCorr = 256;       // column of the correction accumulator
-constexpr int kTileA = kTcM * kTcK * 4;      // 8 KB
+constexpr int kTileA = kTcM * kTcK * 4;      // 8 KB: one hi or lo tile of X
 constexpr int kSmemBudget = 224 * 1024;       // dynamic: 227 KB less the kernel's static shared memory
-constexpr int kSmemExtra = 1024 + 128;       // alignment slack, barriers, TMEM address
+constexpr int kSmemExtra = 1024 + 256;       // alignment slack, barriers, TMEM address
 constexpr long long kWaitLimit = 1LL << 24;  // try_wait polls before a wait gives up
 
 // FP32 -> TF32 (1 + 8 + 10 bits) by round to nearest even, as an FP32 bit pattern.
@@ -79,20 +82,21 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
     return false;
 }
 
-__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
 }
 
-// Wait until at most n of this thread's cp.async groups are pending.
-__device__ __forceinline__ void cp_async_wait_pending(int n) {
-    switch (n) {
-        case 0: asm volatile("cp.async.wait_group 0;" ::: "memory"); break;
-        case 1: asm volatile("cp.async.wait_group 1;" ::: "memory"); break;
-        case 2: asm volatile("cp.async.wait_group 2;" ::: "memory"); break;
-        case 3: asm volatile("cp.async.wait_group 3;" ::: "memory"); break;
-        case 4: asm volatile("cp.async.wait_group 4;" ::: "memory"); break;
-        default: asm volatile("cp.async.wait_group 5;" ::: "memory"); break;
-    }
+// Contiguous global -> shared copy whose bytes the mbarrier counts.
+__device__ __forceinline__ void bulk_copy(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+
+// Byte offset of element (row r, face f of the chunk) in a 64-byte-swizzled
+// K-major tile image: 16-byte chunk c = f / 4 of row r sits at c ^ ((r >> 1) & 3).
+__host__ __device__ __forceinline__ uint32_t sw64_offset(int r, int f) {
+    return (uint32_t)(r * 64 + ((((f >> 2) ^ ((r >> 1) & 3)) & 3) << 4) + (f & 3) * 4);
 }
 
 // Shared-memory matrix descriptor: K-major operand, 64-byte swizzle (16-byte
@@ -131,39 +135,32 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
         : "r"(taddr));
 }
 
-// Copy one operand tile (nrow rows of 16 floats from row-major src with
-// leading dimension ld) into the 64-byte-swizzled layout at dst.
-__device__ __forceinline__ void load_tile(uint32_t dst, const float* __restrict__ src, long long ld, int nrow) {
-    for (int e = threadIdx.x; e < nrow * 4; e += kTcThreads) {
-        const int r = e >> 2, c = e & 3;
-        cp_async16(dst + r * 64 + ((c ^ ((r >> 1) & 3)) << 4), src + (long long)r * ld + c * 4);
-    }
-}
-
 __global__ void __launch_bounds__(kTcThreads, 1)
-    k_subproj_tc(Layout L, Layout Lc, int s, int rows, int nblocks, int kpad, int bn,
-                 const float* __restrict__ Xh, const float* __restrict__ Xl, const float* __restrict__ Mh,
-                 const float* __restrict__ Ml, const uint8_t* __restrict__ bobs, float* __restrict__ u,
-                 float* __restrict__ v, float* __restrict__ w, int nstages, int* __restrict__ err) {
+    k_subproj_tc(Layout L, Layout Lc, int s, int rows, int nblocks, int nk, int bn,
+                 const unsigned char* __restrict__ Xs, const unsigned char* __restrict__ Ms,
+                 const uint8_t* __restrict__ bobs, float* __restrict__ u, float* __restrict__ v,
+                 float* __restrict__ w, int nstages, int* __restrict__ err) {
     extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
     // 1024-byte alignment for the swizzle atoms
     const uint32_t raw = smem_u32(tc_smem_raw);
     const uint32_t base = (raw + 1023u) & ~1023u;
     unsigned char* gbase = tc_smem_raw + (base - raw);
     const int tile_b = bn * kTcK * 4;                     // a multiple of 1024 (bn % 16 == 0)
-    const int stage_bytes = 2 * kTileA + 2 * tile_b;
-    const uint32_t bars = base + nstages * stage_bytes;   // nstages mbarriers
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(gbase + nstages * stage_bytes + 8 * kTcMaxStages);
+    const int bytes_a = 2 * kTileA, bytes_b = 2 * tile_b;  // hi + lo images, contiguous
+    const int stage_bytes = bytes_a + bytes_b;
+    const uint32_t full = base + nstages * stage_bytes;   // nstages "bytes landed" barriers
+    const uint32_t empty = full + 8 * kTcMaxStages;       // nstages "stage released" barriers
+    const uint32_t done = empty + 8 * kTcMaxStages;       // accumulators complete
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(gbase + nstages * stage_bytes + 16 * kTcMaxStages + 16);
     __shared__ int s_fail;
     // per row of the tile: the face's offset from its block's corner cell in
     // the padded layout (i + j px + k plane) and its component, -1 past the rows
     __shared__ int s_off[kTcMaxN];
     __shared__ int s_comp[kTcMaxN];
 
-    const int tid = threadIdx.x, warp = tid >> 5;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int n0 = blockIdx.x * bn;        // first row of the tile
     const int b0 = blockIdx.y * kTcM;      // first block of the tile
-    const int nk = kpad / kTcK;
 
     for (int q = tid; q < bn; q += kTcThreads) {
         const int row = n0 + q;
@@ -172,10 +169,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         s_off[q] = off;
         s_comp[q] = comp;
     }
-
     if (tid == 0) {
         s_fail = 0;
-        for (int q = 0; q < nstages; q++) mbar_init(bars + 8 * q, 1);
+        for (int q = 0; q < nstages; q++) {
+            mbar_init(full + 8 * q, 1);
+            mbar_init(empty + 8 * q, 1);
+        }
+        mbar_init(done, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
@@ -189,53 +189,40 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
 
-    // kind::tf32: D f32 (bits 4-5 = 1), A and B tf32 (bits 7-9, 10-12 = 2), both
-    // K-major, N >> 3 at bit 17, M >> 4 at bit 24
-    const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(bn >> 3) << 17) | ((uint32_t)(kTcM >> 4) << 24);
-
-    const float* xh = Xh + (long long)b0 * kpad;
-    const float* xl = Xl + (long long)b0 * kpad;
-    const float* mh = Mh + (long long)n0 * kpad;
-    const float* ml = Ml + (long long)n0 * kpad;
-    auto stage_addr = [&](int st) { return base + st * stage_bytes; };
-    // one commit group per chunk index (empty past the last chunk), so that
-    // "at most PD groups pending" always means "chunk kc has landed"
-    auto issue_load = [&](int kc) {
-        if (kc < nk) {
-            const uint32_t sa = stage_addr(kc % nstages);
-            const int k0 = kc * kTcK;
-            load_tile(sa, xh + k0, kpad, kTcM);
-            load_tile(sa + kTileA, xl + k0, kpad, kTcM);
-            load_tile(sa + 2 * kTileA, mh + k0, kpad, bn);
-            load_tile(sa + 2 * kTileA + tile_b, ml + k0, kpad, bn);
+    const unsigned char* xs = Xs + (size_t)blockIdx.y * nk * bytes_a;
+    const unsigned char* ms = Ms + (size_t)blockIdx.x * nk * bytes_b;
+    int produced = 0;  // producer: chunks whose copies were issued
+    if (warp == 0 && lane == 0) {
+        for (int j = 0; j < nk; j++) {
+            const int st = j % nstages;
+            // the stage's previous chunk (j - nstages) released by its MMAs
+            if (j >= nstages && !mbar_wait(empty + 8 * st, (uint32_t)((j / nstages - 1) & 1))) {
+                s_fail = 1;
+                break;
+            }
+            if (s_fail) break;
+            const uint32_t sa = base + st * stage_bytes;
+            mbar_expect_tx(full + 8 * st, (uint32_t)stage_bytes);
+            bulk_copy(sa, xs + (size_t)j * bytes_a, (uint32_t)bytes_a, full + 8 * st);
+            bulk_copy(sa + bytes_a, ms + (size_t)j * bytes_b, (uint32_t)bytes_b, full + 8 * st);
+            produced = j + 1;
         }
-        asm volatile("cp.async.commit_group;" ::: "memory");
-    };
-    const int PD = nstages - kTcAhead;  // chunks copied ahead of the one consumed
-
-    int issued = 0;  // chunks whose MMAs were issued (thread 0)
-    for (int j = 0; j < PD; j++) issue_load(j);
-    for (int kc = 0; kc < nk; kc++) {
-        const int st = kc % nstages;
-        bool my_fail = false;
-        // chunk j goes into the stage chunk j - nstages used: its MMAs (issued
-        // kTcAhead chunks ago, at kc - kTcAhead) must have completed; the MMAs
-        // of chunk kc - 1 may still run
-        const int j = kc + PD;
-        if (j < nk && j >= nstages)
-            my_fail = !mbar_wait(bars + 8 * (j % nstages), (uint32_t)(((j - nstages) / nstages) & 1));
-        if (!my_fail) issue_load(j);
-        cp_async_wait_pending(PD);
-        if (my_fail) s_fail = 1;
-        // the copies of chunk kc, written through the generic proxy, become
-        // visible to the tensor cores (async proxy)
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        if (s_fail) break;  // uniform: read by every thread after the barrier
-        if (tid == 0) {
+    } else if (warp == 1 && lane == 0) {
+        // kind::tf32: D f32 (bits 4-5 = 1), A and B tf32 (bits 7-9, 10-12 = 2),
+        // both K-major, N >> 3 at bit 17, M >> 4 at bit 24
+        const uint32_t idesc =
+            (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(bn >> 3) << 17) | ((uint32_t)(kTcM >> 4) << 24);
+        int consumed = 0;
+        for (int kc = 0; kc < nk; kc++) {
+            const int st = kc % nstages;
+            if (!mbar_wait(full + 8 * st, (uint32_t)((kc / nstages) & 1))) {
+                s_fail = 1;
+                break;
+            }
+            if (s_fail) break;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t sa = stage_addr(st);
-            const uint32_t ah = sa, al = sa + kTileA, bh = sa + 2 * kTileA, bl = sa + 2 * kTileA + tile_b;
+            const uint32_t sa = base + st * stage_bytes;
+            const uint32_t ah = sa, al = sa + kTileA, bh = sa + bytes_a, bl = sa + bytes_a + tile_b;
 #pragma unroll
             for (int k = 0; k < kTcK / 8; k++) {
                 const uint32_t off = k * 32;  // 8 tf32 = 32 bytes along K
@@ -244,21 +231,25 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 mma_tf32(tmem + kTcCorr, sw64_desc(ah + off), sw64_desc(bl + off), idesc, acc);
                 mma_tf32(tmem + kTcCorr, sw64_desc(al + off), sw64_desc(bh + off), idesc, 1u);
             }
-            mma_commit(bars + 8 * st);
-            issued = kc + 1;
+            mma_commit(empty + 8 * st);
+            consumed = kc + 1;
         }
+        // the accumulators are complete when every MMA issued so far is
+        if (consumed > 0) mma_commit(done);
+        if (consumed < nk) s_fail = 1;
     }
     __syncthreads();
-    // every issued MMA done: a commit tracks all earlier MMAs of the thread
-    if (tid == 0 && issued > 0) {
-        const int last = issued - 1;
-        if (!mbar_wait(bars + 8 * (last % nstages), (uint32_t)((last / nstages) & 1))) s_fail = 1;
+    const bool ok = !s_fail;
+    // bounded waits for everything issued, whatever happened
+    if (tid == 0 && !mbar_wait(done, 0u)) s_fail = 1;
+    if (warp == 0 && lane == 0 && !ok) {
+        // copies issued but never consumed still land before the CTA leaves
+        for (int j = (produced > nstages ? produced - nstages : 0); j < produced; j++)
+            mbar_wait(full + 8 * (j % nstages), (uint32_t)((j / nstages) & 1));
     }
-    asm volatile("cp.async.wait_group 0;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    const bool ok = !s_fail;
-    if (ok) {
+    if (!s_fail) {
         const int gb = b0 + tid;  // this thread's block (TMEM lane tid)
         const bool live = gb < nblocks && !bobs[gb];
         const int bi = gb % Lc.W, bj = (gb / Lc.W) % Lc.H, bk = gb / (Lc.W * Lc.H);
@@ -291,22 +282,27 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     }
 }
 
-// xh / xl split of the gathered faces, row-padded to kpad and block-padded to
-// a multiple of 128 with zeros.
-__global__ void k_split_tf32(const float* __restrict__ X, int nf, int nblocks, int kpad, long long total,
-                             float* __restrict__ Xh, float* __restrict__ Xl) {
+// xh / xl split of the gathered faces into the swizzled tile images: per
+// (128-block tile t, chunk c of 16 faces) the 8 KB hi image then the lo one;
+// faces past nf and blocks past nblocks are 0.
+__global__ void k_split_tf32(const float* __restrict__ X, int nf, int nblocks, int nk, long long total,
+                             unsigned char* __restrict__ Xs) {
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= total) return;
+    const int kpad = nk * kTcK;
     const int b = (int)(e / kpad), q = (int)(e - (long long)b * kpad);
     const float x = (b < nblocks && q < nf) ? __ldg(X + (long long)b * nf + q) : 0.0f;
     const float hi = __uint_as_float(tf32_rne_bits(__float_as_uint(x)));
-    Xh[e] = hi;
-    Xl[e] = __uint_as_float(tf32_rne_bits(__float_as_uint(x - hi)));
+    const float lo = __uint_as_float(tf32_rne_bits(__float_as_uint(x - hi)));
+    const int t = b / kTcM, r = b % kTcM, c = q / kTcK, f = q % kTcK;
+    unsigned char* img = Xs + ((size_t)t * nk + c) * (2 * kTileA);
+    const uint32_t o = sw64_offset(r, f);
+    *reinterpret_cast<float*>(img + o) = hi;
+    *reinterpret_cast<float*>(img + kTileA + o) = lo;
 }
 
 struct MSplit {
-    float* h = nullptr;
-    float* l = nullptr;
+    unsigned char* img = nullptr;  // per (row tile, chunk): hi image then lo image, bn x 64 bytes each
     int kpad = 0, bn = 0, ntiles = 0;
 };
 std::mutex g_ms_mu;
@@ -325,11 +321,13 @@ int get_msplit(int s, MSplit& out) {
     m.kpad = (nf + kTcPad - 1) / kTcPad * kTcPad;
     m.ntiles = (rows + kTcMaxN - 1) / kTcMaxN;
     m.bn = ((rows + m.ntiles - 1) / m.ntiles + 15) / 16 * 16;
-    const size_t n = (size_t)m.ntiles * m.bn * m.kpad;
-    std::vector<float> h(n, 0.0f), l(n, 0.0f);
-    for (int r = 0; r < rows; r++)
+    const int nk = m.kpad / kTcK;
+    const size_t tile = (size_t)m.bn * kTcK * 4;
+    const size_t bytes = (size_t)m.ntiles * nk * 2 * tile;
+    std::vector<unsigned char> img(bytes, 0);
+    for (int row = 0; row < rows; row++)
         for (int q = 0; q < nf; q++) {
-            const float x = M[(size_t)r * nf + q];
+            const float x = M[(size_t)row * nf + q];
             uint32_t bits;
             std::memcpy(&bits, &x, 4);
             bits = tf32_rne_bits(bits);
@@ -339,16 +337,16 @@ int get_msplit(int s, MSplit& out) {
             std::memcpy(&bits, &rest, 4);
             bits = tf32_rne_bits(bits);
             std::memcpy(&lo, &bits, 4);
-            h[(size_t)r * m.kpad + q] = hi;
-            l[(size_t)r * m.kpad + q] = lo;
+            const int t = row / m.bn, r = row % m.bn, c = q / kTcK, f = q % kTcK;
+            unsigned char* im = img.data() + ((size_t)t * nk + c) * 2 * tile;
+            const uint32_t o = sw64_offset(r, f);
+            std::memcpy(im + o, &hi, 4);
+            std::memcpy(im + tile + o, &lo, 4);
         }
-    ZQS_CUDA_TRY(cudaMalloc(&m.h, n * sizeof(float)));
-    cudaError_t e = cudaMalloc(&m.l, n * sizeof(float));
-    if (e == cudaSuccess) e = cudaMemcpy(m.h, h.data(), n * sizeof(float), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(m.l, l.data(), n * sizeof(float), cudaMemcpyHostToDevice);
+    ZQS_CUDA_TRY(cudaMalloc(&m.img, bytes));
+    cudaError_t e = cudaMemcpy(m.img, img.data(), bytes, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
-        cudaFree(m.h);
-        cudaFree(m.l);
+        cudaFree(m.img);
         return cuda_fail(e, "tensor-core sub-projection matrix upload");
     }
     g_ms[s] = m;
@@ -391,23 +389,22 @@ int launch_subproj_tc(const Layout& L, const Layout& Lc, int s, int nf, int rows
         }
         m = it->second;
     }
-    // as many stages as fit (kTcAhead + 1 .. kTcMaxStages); the copies run
-    // nstages - kTcAhead chunks ahead (at most 5 pending groups)
+    // as many stages as fit (2 .. kTcMaxStages)
     const int stage_bytes = 2 * kTileA + 2 * m.bn * kTcK * 4;
-    const int nstages = std::min(std::min(kTcMaxStages, kTcAhead + 5), (kSmemBudget - kSmemExtra) / stage_bytes);
-    if (nstages < kTcAhead + 1) {
+    const int nstages = std::min(kTcMaxStages, (kSmemBudget - kSmemExtra) / stage_bytes);
+    if (nstages < 2) {
         set_error("tensor-core sub-projection: the operand stages do not fit in shared memory");
         return ZQS_EUNSUPPORTED;
     }
     const size_t smem = (size_t)nstages * stage_bytes + kSmemExtra;
+    const int nk = m.kpad / kTcK;
     const long long bpad = (nblocks + kTcM - 1) / kTcM * kTcM;
     const long long total = bpad * m.kpad;
-    float* Xh = Xsplit;
-    float* Xl = Xsplit + total;
-    k_split_tf32<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(X, nf, nblocks, m.kpad, total, Xh, Xl);
+    unsigned char* Xs = reinterpret_cast<unsigned char*>(Xsplit);
+    k_split_tf32<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(X, nf, nblocks, nk, total, Xs);
     const dim3 grid(m.ntiles, (unsigned)(bpad / kTcM), 1);
-    k_subproj_tc<<<grid, kTcThreads, smem, st>>>(L, Lc, s, rows, nblocks, m.kpad, m.bn, Xh, Xl, m.h, m.l, bobs, u,
-                                                 v, w, nstages, err);
+    k_subproj_tc<<<grid, kTcThreads, smem, st>>>(L, Lc, s, rows, nblocks, nk, m.bn, Xs, m.img, bobs, u, v, w,
+                                                 nstages, err);
     lc.n += 2;
     ZQS_LAUNCH_CHECK("k_subproj_tc");
     return ZQS_OK;
