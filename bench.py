@@ -290,12 +290,20 @@ def measure_coarse(args, stream):
     g.project(sp)
     ms_proj = timed(lambda: g.project(sp), 3)
     mx = g.stats().max_abs_div
+    # the same projection with the obstacle-free blocks on the FP32 SIMT path
+    g.set_coarse_gemm(0)
+    g.project(sp)
+    ms_proj_simt = timed(lambda: g.project(sp), 3)
+    g.set_coarse_gemm(1)
+    g.sync(sp)
     g.close()
     return {"workload": args.coarse, "grid": [w.W, w.H, w.D], "sub_size": int(w.params.sub_size),
             "coarse_grid": [w.W // w.params.sub_size] * 3, "sor_iters": int(w.params.sor_iters),
             "advection": "inReg_outReg + Reg scalar", "steps": steps, "ms_per_step": ms,
             "value": w.cells / (ms * 1e-3) / 1e9, "unit": UNIT, "gpu_launches_per_step": launches,
-            "projection_ms": ms_proj, "max_abs_div_after_projection": mx}
+            "projection_ms": ms_proj, "max_abs_div_after_projection": mx,
+            "block_product": "tcgen05 TF32, 3xTF32 split (zqs_grid_set_coarse_gemm 1)",
+            "projection_ms_fp32_simt_blocks": ms_proj_simt}
 
 
 def measure_render(args, stream):

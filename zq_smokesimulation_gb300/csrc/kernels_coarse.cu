@@ -545,9 +545,13 @@ __device__ int block_min(int x, int* redi) {
 // relative residual of 1e-12 (the reference's PCG tolerance), one thread per
 // cell.  Pressures rounded to float; interior faces between free cells get
 // -(p_b - p_a).
+//
+// The block's faces are read from u, v, w directly: the divergence reads
+// happen before any write, and each interior face is written only by the
+// thread that read its value (the +x/+y/+z faces of other cells are boundary
+// faces of the block, never written here).
 __global__ void k_subproj_obstacle(Layout L, Layout Lc, int s, int nf, const uint8_t* __restrict__ flags,
-                                   const float* __restrict__ X, const uint8_t* __restrict__ bobs,
-                                   float* __restrict__ u, float* __restrict__ v, float* __restrict__ w) {
+                                   const uint8_t* __restrict__ bobs, float* u, float* v, float* w) {
     const int b = blockIdx.x;
     if (!bobs[b]) return;
     extern __shared__ double sm[];
@@ -593,16 +597,12 @@ __global__ void k_subproj_obstacle(Layout L, Layout Lc, int s, int nf, const uin
         if (ch) lab[c] = m;
         if (!__syncthreads_or(ch)) break;
     }
-    const float* xb = X + (size_t)b * nf;
-    const int nu = s * s * (s + 1);
-    auto fu = [&](int i, int j, int k) { return (k * s + j) * (s + 1) + i; };
-    auto fv = [&](int i, int j, int k) { return nu + (k * (s + 1) + j) * s + i; };
-    auto fw = [&](int i, int j, int k) { return 2 * nu + (k * s + j) * s + i; };
+    // this cell's padded index: its -x/-y/-z faces sit there in u/v/w
+    const int fc = lidx(L, bi * s + ci, bj * s + cj, bk * s + ck);
     // right-hand side: the float divergence of the free cell, minus its region's mean
     double bval = 0.0;
     if (fr) {
-        const float dvg = ((((__ldg(xb + fu(ci + 1, cj, ck)) - __ldg(xb + fu(ci, cj, ck))) + __ldg(xb + fv(ci, cj + 1, ck))) -
-                            __ldg(xb + fv(ci, cj, ck))) + __ldg(xb + fw(ci, cj, ck + 1))) - __ldg(xb + fw(ci, cj, ck));
+        const float dvg = ((((u[fc + 1] - u[fc]) + v[fc + L.px]) - v[fc]) + w[fc + (int)L.plane]) - w[fc];
         bval = (double)dvg;
     }
     double bp = bval;
@@ -653,14 +653,14 @@ __global__ void k_subproj_obstacle(Layout L, Layout Lc, int s, int nf, const uin
     pf[c] = (float)xv;
     __syncthreads();
     if (!fr) return;
-    auto put = [&](int q, int comp, int lo) {
+    auto put = [&](int comp, int lo) {
         const float d = -(pf[c] - pf[lo]);
-        const int fc = lidx(L, bi * s + ci, bj * s + cj, bk * s + ck);
-        comp_ptr(comp, u, v, w)[fc] = __ldg(xb + q) + d;
+        float* f = comp_ptr(comp, u, v, w) + fc;
+        *f = *f + d;
     };
-    if (nbm & (1u << 4)) put(fu(ci, cj, ck), 0, c - 1);
-    if (nbm & (1u << 2)) put(fv(ci, cj, ck), 1, c - s);
-    if (nbm & (1u << 0)) put(fw(ci, cj, ck), 2, c - s * s);
+    if (nbm & (1u << 4)) put(0, c - 1);
+    if (nbm & (1u << 2)) put(1, c - s);
+    if (nbm & (1u << 0)) put(2, c - s * s);
 }
 
 // The sub-projection matrix per block edge, transposed on the device, shared by
@@ -858,25 +858,25 @@ int launch_project_coarse(DevGrid& g, const KParams& kp, int K, cudaStream_t st,
     lc.n += 2;
     ZQS_LAUNCH_CHECK("coarse correction");
     if (s > 1) {
-        const long long total = (long long)cs->nblocks * cs->nf;
-        k_subproj_gather<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(L, Lc, s, cs->nf, total, g.u, g.v, g.w,
-                                                                            cs->X);
         if (cs->tc && cs->Xsplit) {
-            int rc = launch_subproj_tc(L, Lc, s, cs->nf, cs->rows, cs->nblocks, cs->X, cs->Xsplit, cs->bobs, g.u,
-                                       g.v, g.w, cs->err, st, lc);
+            // gathers the block faces itself, into the tensor-core operand images
+            int rc = launch_subproj_tc(L, Lc, s, cs->nf, cs->rows, cs->nblocks, cs->Xsplit, cs->bobs, g.u, g.v, g.w,
+                                       cs->err, st, lc);
             if (rc) return rc;
-            lc.n--;  // counted below with the other two
         } else {
+            const long long total = (long long)cs->nblocks * cs->nf;
+            k_subproj_gather<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(L, Lc, s, cs->nf, total, g.u, g.v,
+                                                                                g.w, cs->X);
             const dim3 gf((cs->rows + kGemmTile - 1) / kGemmTile, (cs->nblocks + kGemmTile - 1) / kGemmTile, 1);
             k_subproj_fast<<<gf, kGemmThreads, 0, st>>>(L, Lc, s, cs->nf, cs->rows, cs->nblocks, cs->MT, cs->X,
                                                         cs->bobs, g.u, g.v, g.w);
+            lc.n += 2;
         }
         int nthr = 32;
         while (nthr < s * s * s) nthr <<= 1;
         const size_t smo = (size_t)2 * nthr * sizeof(double) + (size_t)nthr * sizeof(int);
-        k_subproj_obstacle<<<cs->nblocks, nthr, smo, st>>>(L, Lc, s, cs->nf, g.flags, cs->X, cs->bobs, g.u, g.v,
-                                                           g.w);
-        lc.n += 3;
+        k_subproj_obstacle<<<cs->nblocks, nthr, smo, st>>>(L, Lc, s, cs->nf, g.flags, cs->bobs, g.u, g.v, g.w);
+        lc.n += 1;
         ZQS_LAUNCH_CHECK("block sub-projection");
     }
     return ZQS_OK;

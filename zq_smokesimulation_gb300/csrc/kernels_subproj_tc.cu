@@ -282,16 +282,23 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     }
 }
 
-// xh / xl split of the gathered faces into the swizzled tile images: per
-// (128-block tile t, chunk c of 16 faces) the 8 KB hi image then the lo one;
-// faces past nf and blocks past nblocks are 0.
-__global__ void k_split_tf32(const float* __restrict__ X, int nf, int nblocks, int nk, long long total,
-                             unsigned char* __restrict__ Xs) {
+// Block faces gathered and split into the swizzled tile images: per (128-block
+// tile t, chunk c of 16 faces) the 8 KB hi image then the lo one; faces past nf
+// and blocks past nblocks are 0.
+__global__ void k_gather_split_tf32(Layout L, Layout Lc, int s, int nf, int nblocks, int nk, long long total,
+                                    const float* __restrict__ u, const float* __restrict__ v,
+                                    const float* __restrict__ w, unsigned char* __restrict__ Xs) {
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= total) return;
     const int kpad = nk * kTcK;
     const int b = (int)(e / kpad), q = (int)(e - (long long)b * kpad);
-    const float x = (b < nblocks && q < nf) ? __ldg(X + (long long)b * nf + q) : 0.0f;
+    float x = 0.0f;
+    if (b < nblocks && q < nf) {
+        const int bi = b % Lc.W, bj = (b / Lc.W) % Lc.H, bk = b / (Lc.W * Lc.H);
+        int comp;
+        const int c = subproj_block_face(L, s, q, bi, bj, bk, comp);
+        x = __ldg((comp == 0 ? u : (comp == 1 ? v : w)) + c);
+    }
     const float hi = __uint_as_float(tf32_rne_bits(__float_as_uint(x)));
     const float lo = __uint_as_float(tf32_rne_bits(__float_as_uint(x - hi)));
     const int t = b / kTcM, r = b % kTcM, c = q / kTcK, f = q % kTcK;
@@ -374,8 +381,8 @@ size_t subproj_tc_split_bytes(int nblocks, int nf) {
     return (size_t)(2 * bpad * kpad) * sizeof(float);
 }
 
-int launch_subproj_tc(const Layout& L, const Layout& Lc, int s, int nf, int rows, int nblocks, const float* X,
-                      float* Xsplit, const uint8_t* bobs, float* u, float* v, float* w, int* err, cudaStream_t st,
+int launch_subproj_tc(const Layout& L, const Layout& Lc, int s, int nf, int rows, int nblocks, float* Xsplit,
+                      const uint8_t* bobs, float* u, float* v, float* w, int* err, cudaStream_t st,
                       LaunchCounter& lc) {
     MSplit m;
     {
@@ -401,7 +408,8 @@ int launch_subproj_tc(const Layout& L, const Layout& Lc, int s, int nf, int rows
     const long long bpad = (nblocks + kTcM - 1) / kTcM * kTcM;
     const long long total = bpad * m.kpad;
     unsigned char* Xs = reinterpret_cast<unsigned char*>(Xsplit);
-    k_split_tf32<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(X, nf, nblocks, nk, total, Xs);
+    k_gather_split_tf32<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(L, Lc, s, nf, nblocks, nk, total, u, v, w,
+                                                                         Xs);
     const dim3 grid(m.ntiles, (unsigned)(bpad / kTcM), 1);
     k_subproj_tc<<<grid, kTcThreads, smem, st>>>(L, Lc, s, rows, nblocks, nk, m.bn, Xs, m.img, bobs, u, v, w,
                                                  nstages, err);

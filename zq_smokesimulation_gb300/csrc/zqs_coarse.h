@@ -87,10 +87,11 @@ void coarse_free(CoarseState*& cs);
 int subproj_tc_prepare(int s);
 // Bytes of the tensor-core operand split (xh, xl) for nblocks blocks of nf faces.
 size_t subproj_tc_split_bytes(int nblocks, int nf);
-// Obstacle-free blocks on the tensor cores: split X into Xsplit, then
-// Y = X M^T written to the blocks' interior faces (blocks with bobs set skipped).
-int launch_subproj_tc(const Layout& L, const Layout& Lc, int s, int nf, int rows, int nblocks, const float* X,
-                      float* Xsplit, const uint8_t* bobs, float* u, float* v, float* w, int* err, cudaStream_t st,
+// Obstacle-free blocks on the tensor cores: the block faces gathered from
+// u, v, w and split into Xsplit, then Y = X M^T written to the blocks' interior
+// faces (blocks with bobs set skipped).
+int launch_subproj_tc(const Layout& L, const Layout& Lc, int s, int nf, int rows, int nblocks, float* Xsplit,
+                      const uint8_t* bobs, float* u, float* v, float* w, int* err, cudaStream_t st,
                       LaunchCounter& lc);
 // A tensor-core wait of an earlier projection timed out (reads and clears the
 // device flag; synchronises the stream).
