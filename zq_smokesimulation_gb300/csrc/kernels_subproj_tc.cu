@@ -282,34 +282,47 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     }
 }
 
-// Block faces gathered and split into the swizzled tile images: per (128-block
-// tile t, chunk c of 16 faces) the 8 KB hi image then the lo one; faces past nf
-// and blocks past nblocks are 0.
-__global__ void k_gather_split_tf32(Layout L, Layout Lc, int s, int nf, int nblocks, int nk, long long total,
-                                    const float* __restrict__ u, const float* __restrict__ v,
-                                    const float* __restrict__ w, unsigned char* __restrict__ Xs) {
-    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= total) return;
-    const int kpad = nk * kTcK;
-    const int b = (int)(e / kpad), q = (int)(e - (long long)b * kpad);
-    float x = 0.0f;
-    if (b < nblocks && q < nf) {
-        const int bi = b % Lc.W, bj = (b / Lc.W) % Lc.H, bk = b / (Lc.W * Lc.H);
-        int comp;
-        const int c = subproj_block_face(L, s, q, bi, bj, bk, comp);
-        x = __ldg((comp == 0 ? u : (comp == 1 ? v : w)) + c);
-    }
+// The xh / xl pair of one value at (tile t, row r, face q) of the images.
+__device__ __forceinline__ void store_split(unsigned char* __restrict__ Xs, int nk, int t, int r, int q, float x) {
     const float hi = __uint_as_float(tf32_rne_bits(__float_as_uint(x)));
     const float lo = __uint_as_float(tf32_rne_bits(__float_as_uint(x - hi)));
-    const int t = b / kTcM, r = b % kTcM, c = q / kTcK, f = q % kTcK;
-    unsigned char* img = Xs + ((size_t)t * nk + c) * (2 * kTileA);
-    const uint32_t o = sw64_offset(r, f);
+    unsigned char* img = Xs + ((size_t)t * nk + q / kTcK) * (2 * kTileA);
+    const uint32_t o = sw64_offset(r, q % kTcK);
     *reinterpret_cast<float*>(img + o) = hi;
     *reinterpret_cast<float*>(img + kTileA + o) = lo;
 }
 
+// Block faces gathered and split into the swizzled tile images: per (128-block
+// tile t, chunk c of 16 faces) the 8 KB hi image then the lo one; faces past nf
+// and blocks past nblocks are 0.  One CTA per block; face q's position in the
+// block comes from ftab[q] = i | j << 8 | k << 16 | component << 24.
+__global__ void __launch_bounds__(256) k_gather_split_tf32(Layout L, Layout Lc, int s, int nf, int nblocks, int nk,
+                                                           const uint32_t* __restrict__ ftab,
+                                                           const float* __restrict__ u, const float* __restrict__ v,
+                                                           const float* __restrict__ w,
+                                                           unsigned char* __restrict__ Xs) {
+    const int b = blockIdx.x;
+    const int kpad = nk * kTcK;
+    const bool live = b < nblocks;
+    const int bi = b % Lc.W, bj = (b / Lc.W) % Lc.H, bk = b / (Lc.W * Lc.H);
+    const int corner = live ? lidx(L, bi * s, bj * s, bk * s) : 0;
+    const int t = b / kTcM, r = b % kTcM;
+    for (int q = threadIdx.x; q < kpad; q += blockDim.x) {
+        float x = 0.0f;
+        if (live && q < nf) {
+            const uint32_t f = __ldg(ftab + q);
+            const int off = (int)(f & 255u) + (int)((f >> 8) & 255u) * L.px + (int)((f >> 16) & 255u) * (int)L.plane;
+            const uint32_t comp = f >> 24;
+            x = __ldg((comp == 0 ? u : (comp == 1 ? v : w)) + corner + off);
+        }
+        store_split(Xs, nk, t, r, q, x);
+    }
+}
+
+
 struct MSplit {
     unsigned char* img = nullptr;  // per (row tile, chunk): hi image then lo image, bn x 64 bytes each
+    uint32_t* ftab = nullptr;      // per block face: i | j << 8 | k << 16 | component << 24
     int kpad = 0, bn = 0, ntiles = 0;
 };
 std::mutex g_ms_mu;
@@ -350,10 +363,24 @@ int get_msplit(int s, MSplit& out) {
             std::memcpy(im + o, &hi, 4);
             std::memcpy(im + tile + o, &lo, 4);
         }
+    // face table: the padded index in a layout with 256-wide rows and 256-row
+    // planes is exactly i + 256 j + 65536 k
+    std::vector<uint32_t> ft(nf);
+    Layout P{};
+    P.px = 256;
+    P.py = 256;
+    for (int q = 0; q < nf; q++) {
+        int comp;
+        const int packed = subproj_block_face(P, s, q, 0, 0, 0, comp);
+        ft[q] = (uint32_t)packed | ((uint32_t)comp << 24);
+    }
     ZQS_CUDA_TRY(cudaMalloc(&m.img, bytes));
-    cudaError_t e = cudaMemcpy(m.img, img.data(), bytes, cudaMemcpyHostToDevice);
+    cudaError_t e = cudaMalloc(&m.ftab, ft.size() * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemcpy(m.img, img.data(), bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(m.ftab, ft.data(), ft.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
         cudaFree(m.img);
+        cudaFree(m.ftab);
         return cuda_fail(e, "tensor-core sub-projection matrix upload");
     }
     g_ms[s] = m;
@@ -406,10 +433,8 @@ int launch_subproj_tc(const Layout& L, const Layout& Lc, int s, int nf, int rows
     const size_t smem = (size_t)nstages * stage_bytes + kSmemExtra;
     const int nk = m.kpad / kTcK;
     const long long bpad = (nblocks + kTcM - 1) / kTcM * kTcM;
-    const long long total = bpad * m.kpad;
     unsigned char* Xs = reinterpret_cast<unsigned char*>(Xsplit);
-    k_gather_split_tf32<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(L, Lc, s, nf, nblocks, nk, total, u, v, w,
-                                                                         Xs);
+    k_gather_split_tf32<<<(unsigned)bpad, 256, 0, st>>>(L, Lc, s, nf, nblocks, nk, m.ftab, u, v, w, Xs);
     const dim3 grid(m.ntiles, (unsigned)(bpad / kTcM), 1);
     k_subproj_tc<<<grid, kTcThreads, smem, st>>>(L, Lc, s, rows, nblocks, nk, m.bn, Xs, m.img, bobs, u, v, w,
                                                  nstages, err);

@@ -34,7 +34,7 @@ struct CoarseState {
 
 // Block face q (u: k, j, i <= s; v: k, j <= s, i; w: k <= s, j, i) of block
 // (bi, bj, bk) -> the fine face's padded index and component.
-__device__ __forceinline__ int subproj_block_face(const Layout& L, int s, int q, int bi, int bj, int bk, int& comp) {
+__host__ __device__ __forceinline__ int subproj_block_face(const Layout& L, int s, int q, int bi, int bj, int bk, int& comp) {
     const int nu = s * s * (s + 1);
     int i, j, k;
     if (q < nu) {
