@@ -208,13 +208,16 @@ __global__ void k_coarse_sor(Layout Lc, const float* __restrict__ ru, const floa
 // keeps planes [r P, (r+1) P) of p in its shared memory and reads the z
 // neighbours across the slab boundary from the adjacent CTA's shared memory
 // (distributed shared memory); a hardware cluster barrier separates the
-// half-sweeps.  Each thread holds up to kClusterCpt cells with their six
-// weights, neighbour mask, 1/diag weight and divergence in registers.  Same
+// half-sweeps.  Each thread owns kClusterPairs pairs of x-adjacent cells, so
+// that every half-sweep updates exactly one cell of each pair (the one of that
+// colour) and no lane of a warp idles; the cells' six weights, neighbour mask,
+// omega/diag weight and divergence stay in registers, ordered by colour.  Same
 // arithmetic as k_coarse_sor (a colour reads only the other colour, so the
 // order of updates inside a half-sweep does not matter): identical results.
 constexpr int kClusterCtas = 8;
 constexpr int kClusterThreads = 1024;
-constexpr int kClusterCpt = 4;
+constexpr int kClusterPairs = 2;
+constexpr int kClusterCpt = 2 * kClusterPairs;
 
 __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterThreads)
     k_coarse_sor_cluster(Layout Lc, int P, const float* __restrict__ ru, const float* __restrict__ rv,
@@ -231,25 +234,36 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterT
     for (int e = threadIdx.x; e < P * H * W; e += blockDim.x) ps[e] = 0.0f;
     float* below = rank > 0 ? cluster.map_shared_rank(ps, rank - 1) : nullptr;   // planes z0-P .. z0-1
     float* above = rank < kClusterCtas - 1 ? cluster.map_shared_rank(ps, rank + 1) : nullptr;
+    // cell m = 2 q + colour: the cell of that colour in this thread's pair q
     float w6[kClusterCpt][6], wc[kClusterCpt], dv[kClusterCpt];
-    unsigned mk[kClusterCpt];
-    int le[kClusterCpt], col[kClusterCpt];
+    unsigned mk[kClusterCpt];  // bits 0-5 free neighbours, 6 z- in the CTA below, 7 z+ in the CTA above
+    int le[kClusterCpt];
+    bool act[kClusterCpt];
+    const int Wp = (W + 1) / 2;
+    const int npairs = max(0, min(P, D - z0)) * H * Wp;
 #pragma unroll
     for (int m = 0; m < kClusterCpt; m++) {
-        const int e = threadIdx.x + m * kClusterThreads;
-        le[m] = e;
+        const int pr = threadIdx.x + (m >> 1) * kClusterThreads;
+        const int colour = m & 1;
+        le[m] = 0;
         mk[m] = 0;
-        col[m] = -1;
+        act[m] = false;
         wc[m] = 0.0f;
         dv[m] = 0.0f;
 #pragma unroll
         for (int q = 0; q < 6; q++) w6[m][q] = 0.0f;
-        if (e >= nloc) continue;
-        const int i = e % W, j = (e / W) % H, k = z0 + e / (W * H);
+        if (pr >= npairs) continue;
+        const int pi = pr % Wp, j = (pr / Wp) % H, zl = pr / (Wp * H), k = z0 + zl;
+        const int i = 2 * pi + ((colour + j + k) & 1);
+        if (i >= W) continue;
+        const int e = (zl * H + j) * W + i;
+        le[m] = e;
         const int c = lidx(Lc, i, j, k);
         if (occ[c] || diag[c] == 0.0f) continue;
         const int px = Lc.px, pl = (int)Lc.plane;
-        col[m] = (i + j + k) & 1;
+        act[m] = true;
+        if (zl == 0) mk[m] |= 64u;
+        if (zl == P - 1) mk[m] |= 128u;
         // neighbours x-, x+, y-, y+, z-, z+ (bit q) that are in the domain and free
         if (i > 0 && !occ[c - 1]) mk[m] |= 1u, w6[m][0] = ru[c];
         if (i < W - 1 && !occ[c + 1]) mk[m] |= 2u, w6[m][1] = ru[c + 1];
@@ -263,24 +277,25 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterT
     cluster.sync();
     const int plane = H * W;
     for (int it = 0; it < K; it++) {
+#pragma unroll
         for (int colour = 0; colour < 2; colour++) {
 #pragma unroll
-            for (int m = 0; m < kClusterCpt; m++) {
-                if (col[m] != colour) continue;
+            for (int q = 0; q < kClusterPairs; q++) {
+                const int m = 2 * q + colour;
+                if (!act[m]) continue;
                 const int e = le[m];
                 const float* pe = ps + e;
-                const int zl = e / plane;
                 const float xm = (mk[m] & 1u) ? w6[m][0] * pe[-1] : 0.0f;
                 const float xp = (mk[m] & 2u) ? w6[m][1] * pe[1] : 0.0f;
                 const float ym = (mk[m] & 4u) ? w6[m][2] * pe[-W] : 0.0f;
                 const float yp = (mk[m] & 8u) ? w6[m][3] * pe[W] : 0.0f;
                 float zm = 0.0f, zp = 0.0f;
                 if (mk[m] & 16u) {
-                    const float pn = zl > 0 ? pe[-plane] : below[e + (P - 1) * plane];
+                    const float pn = (mk[m] & 64u) ? below[e + (P - 1) * plane] : pe[-plane];
                     zm = w6[m][4] * pn;
                 }
                 if (mk[m] & 32u) {
-                    const float pn = zl < P - 1 ? pe[plane] : above[e - (P - 1) * plane];
+                    const float pn = (mk[m] & 128u) ? above[e - (P - 1) * plane] : pe[plane];
                     zp = w6[m][5] * pn;
                 }
                 const float sum = ((xm + xp) + (ym + yp)) + (zm + zp);
@@ -289,10 +304,7 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterT
             cluster.sync();
         }
     }
-#pragma unroll
-    for (int m = 0; m < kClusterCpt; m++) {
-        const int e = le[m];
-        if (e >= nloc) continue;
+    for (int e = threadIdx.x; e < nloc; e += blockDim.x) {
         const int i = e % W, j = (e / W) % H, k = z0 + e / (W * H);
         pout[lidx(Lc, i, j, k)] = ps[e];
     }
@@ -838,7 +850,7 @@ int launch_project_coarse(DevGrid& g, const KParams& kp, int K, cudaStream_t st,
     lc.n += 5;
     // small coarse grids: every iteration in one cluster launch; else one launch per colour
     const int P = (Lc.D + kClusterCtas - 1) / kClusterCtas;
-    if (K > 0 && P * Lc.H * Lc.W <= kClusterThreads * kClusterCpt) {
+    if (K > 0 && P * Lc.H * ((Lc.W + 1) / 2) <= kClusterThreads * kClusterPairs) {
         const size_t smc = (size_t)P * Lc.H * Lc.W * sizeof(float);
         k_coarse_sor_cluster<<<kClusterCtas, kClusterThreads, smc, st>>>(Lc, P, cs->ru, cs->rv, cs->rw, cs->occ,
                                                                        cs->diag, cs->div, cs->p, K, kp.omega,
