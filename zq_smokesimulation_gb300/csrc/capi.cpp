@@ -170,6 +170,29 @@ int copy3d(void* dst, size_t dpitch, size_t dysize, const void* src, size_t spit
     return ZQS_OK;
 }
 
+// Dense device buffer of at least n floats for host transfers (grown on
+// demand).  Transfers on different streams share it: each use waits for the
+// previous one (stage_ev, recorded by stage_done) on the device.
+int host_stage(zqs_grid* g, size_t n, cudaStream_t s, float** out) {
+    if (!g->stage_ev) ZQS_CUDA_TRY(cudaEventCreateWithFlags(&g->stage_ev, cudaEventDisableTiming));
+    if (n > g->stage_cap) {
+        ZQS_CUDA_TRY(cudaEventSynchronize(g->stage_ev));
+        if (g->stage) cudaFree(g->stage);
+        g->stage = nullptr;
+        g->stage_cap = 0;
+        ZQS_CUDA_TRY(cudaMalloc(&g->stage, n * sizeof(float)));
+        g->stage_cap = n;
+    }
+    ZQS_CUDA_TRY(cudaStreamWaitEvent(s, g->stage_ev, 0));
+    *out = g->stage;
+    return ZQS_OK;
+}
+
+int stage_done(zqs_grid* g, cudaStream_t s) {
+    ZQS_CUDA_TRY(cudaEventRecord(g->stage_ev, s));
+    return ZQS_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -317,6 +340,8 @@ ZQS_API int zqs_grid_destroy(zqs_grid* g) {
     cudaFree(g->base);
     coarse_free(g->g.coarse);
     if (g->obj_mask) cudaFree(g->obj_mask);
+    if (g->stage) cudaFree(g->stage);
+    if (g->stage_ev) cudaEventDestroy(g->stage_ev);
     if (g->fext_base) cudaFree(g->fext_base);
     delete g;
     return ZQS_OK;
@@ -406,6 +431,19 @@ ZQS_API int zqs_grid_upload(zqs_grid* g, int field, const void* src, int src_on_
         return ZQS_OK;
     }
     float* dst = field_ptr(g, field);
+    if (!src_on_device) {
+        // one contiguous host -> device copy into a dense staging buffer, then
+        // the strided placement on the device (row-by-row host copies of the
+        // padded layout run far below the link's bandwidth)
+        const size_t n = (size_t)nx * ny * nz;
+        float* st = nullptr;
+        int rc = host_stage(g, n, s, &st);
+        if (rc) return rc;
+        ZQS_CUDA_TRY(cudaMemcpyAsync(st, src, n * sizeof(float), cudaMemcpyHostToDevice, s));
+        rc = copy3d(dst, (size_t)L.px * 4, (size_t)L.py, st, (size_t)nx * 4, (size_t)ny, (size_t)nx * 4, ny, nz,
+                    cudaMemcpyDeviceToDevice, s);
+        return rc ? rc : stage_done(g, s);
+    }
     return copy3d(dst, (size_t)L.px * 4, (size_t)L.py, src, (size_t)nx * 4, (size_t)ny, (size_t)nx * 4, ny, nz, kind,
                   s);
 }
@@ -429,6 +467,18 @@ ZQS_API int zqs_grid_download(zqs_grid* g, int field, void* dst, int dst_on_devi
         return ZQS_OK;
     }
     const float* src = field_ptr(g, field);
+    if (!dst_on_device) {
+        // dense gather on the device, then one contiguous device -> host copy
+        const size_t n = (size_t)nx * ny * nz;
+        float* st = nullptr;
+        int rc = host_stage(g, n, s, &st);
+        if (rc) return rc;
+        rc = copy3d(st, (size_t)nx * 4, (size_t)ny, src, (size_t)L.px * 4, (size_t)L.py, (size_t)nx * 4, ny, nz,
+                    cudaMemcpyDeviceToDevice, s);
+        if (rc) return rc;
+        ZQS_CUDA_TRY(cudaMemcpyAsync(dst, st, n * sizeof(float), cudaMemcpyDeviceToHost, s));
+        return stage_done(g, s);
+    }
     return copy3d(dst, (size_t)nx * 4, (size_t)ny, src, (size_t)L.px * 4, (size_t)L.py, (size_t)nx * 4, ny, nz, kind,
                   s);
 }

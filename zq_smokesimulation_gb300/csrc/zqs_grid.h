@@ -32,6 +32,9 @@ struct zqs_grid {
     int coarse_tc = 1;            // coarse solver's obstacle-free blocks: 1 tensor cores, 0 FP32 SIMT
     uint8_t* obj_mask = nullptr;  // device copy of a moving object's voxel mask (grown on demand)
     size_t obj_mask_cap = 0;
+    float* stage = nullptr;       // dense staging buffer of host transfers (grown on demand)
+    size_t stage_cap = 0;
+    cudaEvent_t stage_ev = nullptr;  // the staging buffer's last use
 
     cudaStream_t pick(void* s) const { return s ? (cudaStream_t)s : own; }
 
