@@ -1,9 +1,9 @@
 """GPU parity: the CUDA library (through its C ABI) against the FP32 CPU oracle.
 
 The kernels reproduce the oracle's operation order with no contraction, so
-FP32 results are expected to be bit-identical (-0 == +0); the north-star
-tolerances (relative L2 1e-5 per step, 1e-4 after 100 steps) are asserted as
-well where a trajectory is compared.
+FP32 results are expected to be bit-identical (-0 == +0); the floating-point
+tolerances of the path (relative L2 1e-5 per step, 1e-4 after 100 steps) are
+asserted as well where a trajectory is compared.
 """
 import ctypes as C
 import json
