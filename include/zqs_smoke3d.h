@@ -267,6 +267,29 @@ ZQS_CXX_API bool LoadMovingObjects3D(const char* file, std::vector<ZQ_SmokeMovin
 ZQS_CXX_API bool ZQ_ApplyMovingObject3D(ZQ_SmokeGrid3D* fineGrid, const std::vector<ZQ_SmokeMovingObject3D*>& mvobjs,
                                         const ZQ_SmokeSimulationPara3D& para);
 
+/* Headless counterpart of the viewer's volume display (SampleSmokeGUI:
+ * LoadDataToVolumeTex, ZQ_SmokeGUI.cpp:521-680; DrawVolumeData and its
+ * sequence mode, :680-752), rendered by zqs_render_density on the GPU.
+ *
+ * ZQ_LoadVolume3D: a .di3 file (16-byte type tag "float", int32 width,
+ * height, depth, channels, one flag byte, the floats; channels averaged into
+ * one), or else a raw file of N^3 floats whose first and last axes the viewer
+ * swaps (tmp[i N^2 + j N + k] = raw[k N^2 + j N + i]).  .zqci / .zqwv
+ * (ZQlib formats) return false. */
+ZQS_CXX_API bool ZQ_LoadVolume3D(const char* file, int N, std::vector<float>& data, int& W, int& H, int& D);
+/* Ray march a host density (W*H*D floats, x fastest) into host RGBA floats
+ * (cam.width * cam.height * 4, bottom row first). */
+ZQS_CXX_API bool ZQ_RenderVolume3D(const float* density, int W, int H, int D, const zqs_camera& cam,
+                                   std::vector<float>& rgba);
+/* Binary PPM of an RGBA render over a black background: rgb clamped to
+ * [0, 1], * 255 + 0.5 truncated, top row first. */
+ZQS_CXX_API bool ZQ_WriteRenderPPM(const char* file, const std::vector<float>& rgba, int width, int height);
+/* The viewer's sequence mode: files fold/<prefix><baseID+n><suffix>, n < num,
+ * each shown in the viewer's start-up view (zqs_camera_default) and written
+ * to outFold/render<baseID+n>.ppm.  N: edge of raw files (ignored for .di3). */
+ZQS_CXX_API bool ZQ_RenderSequence3D(const char* fold, const char* prefix, int baseID, int num, const char* suffix,
+                                     int N, int imageWidth, int imageHeight, const char* outFold);
+
 class ZQS_CXX_API ZQ_SmokeSimulation3D {
 public:
     ZQ_SmokeSimulation3D();

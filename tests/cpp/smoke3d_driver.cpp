@@ -4,12 +4,16 @@
 //   smoke3d_driver run    <config> <outdir>   ZQ_SmokeSimulation3D::Init + Run (resident)
 //   smoke3d_driver stages <config> <outdir>   ZQ_InitFineGrid3D + ZQ_UpdateOneFrame3D per frame
 //                                             (+ ZQ_ApplyMovingObject3D as the class does)
+//   smoke3d_driver loadvol <file> <outdir> [N] ZQ_LoadVolume3D, then vol.bin: int32 W, H, D and the floats (no GPU)
+//   smoke3d_driver sequence <fold> <outdir> <prefix> <baseID> <num> <suffix> <N> <imgW> <imgH>
+//                                             ZQ_RenderSequence3D into <outdir>
 //   smoke3d_driver objects <file> <outdir>    LoadMovingObjects3D, then objects.txt: per object
 //                                             size, centre, step count, mask sum and the
 //                                             positions and current velocities over 4 steps (no GPU)
 // Outputs in <outdir>: params.bin (zqs_params bytes), occupancy.bin (W*H*D bytes),
 // init.guidedat (u, v, w, density, temperature) and frame files.
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -33,11 +37,28 @@ static bool dump_setup(const ZQ_SmokeSimulationPara3D& para, ZQ_SmokeGrid3D& g, 
 }
 
 int main(int argc, char** argv) {
-    if (argc != 4) {
-        fprintf(stderr, "usage: %s parse|run|stages <config> <outdir>\n", argv[0]);
+    if (argc < 4) {
+        fprintf(stderr, "usage: %s parse|run|stages|objects|loadvol|sequence <config> <outdir> ...\n", argv[0]);
         return 2;
     }
     const std::string mode = argv[1], cfg = argv[2], out = argv[3];
+    if (mode == "loadvol") {
+        std::vector<float> vol;
+        int W = 0, H = 0, D = 0;
+        if (!ZQ_LoadVolume3D(cfg.c_str(), argc > 4 ? atoi(argv[4]) : 0, vol, W, H, D)) return 3;
+        const int32_t dims[3] = {W, H, D};
+        return write_bytes(out + "/vol.bin", dims, sizeof(dims)) &&
+                       write_bytes(out + "/vol_data.bin", vol.data(), vol.size() * sizeof(float))
+                   ? 0
+                   : 4;
+    }
+    if (mode == "sequence") {
+        if (argc != 11) return 2;
+        return ZQ_RenderSequence3D(cfg.c_str(), argv[4], atoi(argv[5]), atoi(argv[6]), argv[7], atoi(argv[8]),
+                                   atoi(argv[9]), atoi(argv[10]), out.c_str())
+                   ? 0
+                   : 3;
+    }
     if (mode == "parse") {
         ZQ_SmokeSimulationPara3D para;
         if (!para.LoadFromFile(cfg.c_str(), false)) return 3;

@@ -265,3 +265,75 @@ def test_moving_objects_match_oracle(driver, tmp_path, oracle32):
     fin = load_guide(run_out / "final.guidedat", W, H, D)
     for k in ("u", "v", "w", "T", "rho"):
         np.testing.assert_array_equal(fin[k], ref[k])
+
+
+# headless viewer (ZQ_LoadVolume3D / ZQ_RenderSequence3D)
+def write_di3(path, vol, channels=1):
+    D, H, W = vol.shape[:3]
+    with open(path, "wb") as f:
+        f.write(b"float" + b"\0" * 11)
+        f.write(np.array([W, H, D, channels], np.int32).tobytes())
+        f.write(b"\0")
+        f.write(np.ascontiguousarray(vol, np.float32).tobytes())
+
+
+def read_vol(outdir):
+    W, H, D = np.fromfile(outdir / "vol.bin", np.int32)
+    return np.fromfile(outdir / "vol_data.bin", np.float32).reshape(D, H, W)
+
+
+def test_load_volume_formats(driver, tmp_path):
+    rng = np.random.default_rng(2)
+    vol = rng.random((5, 4, 6), dtype=np.float32)
+    write_di3(tmp_path / "a.di3", vol)
+    r = subprocess.run([str(driver), "loadvol", str(tmp_path / "a.di3"), str(tmp_path)], capture_output=True)
+    assert r.returncode == 0
+    np.testing.assert_array_equal(read_vol(tmp_path), vol)
+    # two channels are averaged into one
+    two = np.stack([vol, 3 * vol], axis=-1)
+    write_di3(tmp_path / "b.di3", two, channels=2)
+    assert subprocess.run([str(driver), "loadvol", str(tmp_path / "b.di3"), str(tmp_path)]).returncode == 0
+    np.testing.assert_array_equal(read_vol(tmp_path), ((vol + 3 * vol) / np.float32(2)).astype(np.float32))
+    # raw N^3 floats: the viewer swaps the first and last axes
+    N = 5
+    raw = rng.random((N, N, N), dtype=np.float32)
+    raw.tofile(tmp_path / "c.dat")
+    assert subprocess.run([str(driver), "loadvol", str(tmp_path / "c.dat"), str(tmp_path), str(N)]).returncode == 0
+    np.testing.assert_array_equal(read_vol(tmp_path), raw.transpose(2, 1, 0))
+    # ZQlib formats and truncated files are refused
+    (tmp_path / "d.zqci").write_bytes(b"x")
+    assert subprocess.run([str(driver), "loadvol", str(tmp_path / "d.zqci"), str(tmp_path)]).returncode == 3
+    (tmp_path / "e.di3").write_bytes((tmp_path / "a.di3").read_bytes()[:-8])
+    assert subprocess.run([str(driver), "loadvol", str(tmp_path / "e.di3"), str(tmp_path)]).returncode == 3
+
+
+def ppm_of(rgba):
+    rgb = (np.clip(rgba[..., :3], 0.0, 1.0)[::-1] * np.float32(255.0) + np.float32(0.5)).astype(np.uint8)
+    return b"P6\n%d %d\n255\n" % (rgb.shape[1], rgb.shape[0]) + rgb.tobytes()
+
+
+@pytest.mark.gpu
+def test_render_sequence_matches_oracle(driver, tmp_path, oracle32):
+    """The viewer's sequence mode without a window: two .di3 frames and one raw
+    frame in the start-up view, PPM bytes equal to the oracle's render."""
+    rng = np.random.default_rng(4)
+    frames = [rng.random((12, 16, 20), dtype=np.float32) * 0.2, rng.random((12, 16, 20), dtype=np.float32)]
+    for n, v in enumerate(frames):
+        write_di3(tmp_path / f"frame{n + 3}.di3", v)
+    out = tmp_path / "out"
+    out.mkdir()
+    r = subprocess.run([str(driver), "sequence", str(tmp_path), str(out), "frame", "3", "2", ".di3", "0", "40", "30"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    for n, v in enumerate(frames):
+        cam = capi.default_camera(40, 30, 20, 16, 12)
+        ref = oracle32.render(v, cam)
+        assert (out / f"render{n + 3}.ppm").read_bytes() == ppm_of(ref)
+    N = 8
+    raw = rng.random((N, N, N), dtype=np.float32)
+    raw.tofile(tmp_path / "raw0.dat")
+    r = subprocess.run([str(driver), "sequence", str(tmp_path), str(out), "raw", "0", "1", ".dat", str(N), "24", "24"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    ref = oracle32.render(np.ascontiguousarray(raw.transpose(2, 1, 0)), capi.default_camera(24, 24, N, N, N))
+    assert (out / "render0.ppm").read_bytes() == ppm_of(ref)

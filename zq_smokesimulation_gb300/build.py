@@ -23,7 +23,9 @@ LIB = LIBDIR / "libzqs_gb300.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NUMERICS = ["-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"]
-COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden,-O2",
+# host code: no contraction either (the host-side arithmetic, e.g. image
+# quantisation, must match the CPU restatement on x86 and Arm alike)
+COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden,-O2,-ffp-contract=off",
           f"-I{INCLUDE}", f"-I{CSRC}"]
 
 

@@ -4,6 +4,7 @@
 // ZQ_InitFineGrid3D (:1523-1664), the stage wrappers (:2049-2168, 2349-2440,
 // 3796-3904), ZQ_SmokeGrid3D (ZQ_SmokeGrid3D.cpp:5-121) and
 // ZQ_SmokeSimulation3D::Init/Run/UpdateOneFrame (ZQ_SmokeSimulation3D.cpp:60-243).
+#include <cuda_runtime.h>
 #include <strings.h>
 
 #include <algorithm>
@@ -841,6 +842,108 @@ bool ZQ_ApplyMovingObject3D(ZQ_SmokeGrid3D* g, const std::vector<ZQ_SmokeMovingO
     if (!d || !stamp_objects(d, mvobjs, para)) return false;
     g->MarkHostStale();
     return g->Download() || fail("ZQ_ApplyMovingObject3D");
+}
+
+// ----------------------------------------------------------------- headless viewer
+
+bool ZQ_LoadVolume3D(const char* file, int N, std::vector<float>& data, int& W, int& H, int& D) {
+    if (!file) return false;
+    const size_t len = strlen(file);
+    auto ext = [&](const char* e) { return len >= strlen(e) && strcasecmp(file + len - strlen(e), e) == 0; };
+    if (ext(".zqci") || ext(".zqwv")) return false;
+    FILE* f = fopen(file, "rb");
+    if (!f) return false;
+    bool ok = false;
+    if (ext(".di3")) {
+        char tag[16];
+        int32_t hdr[4];
+        uint8_t flag;
+        if (fread(tag, 1, 16, f) == 16 && strncmp(tag, "float", 5) == 0 && fread(hdr, 4, 4, f) == 4 &&
+            fread(&flag, 1, 1, f) == 1 && hdr[0] > 0 && hdr[1] > 0 && hdr[2] > 0 && hdr[3] > 0) {
+            W = hdr[0], H = hdr[1], D = hdr[2];
+            const int ch = hdr[3];
+            const size_t n = (size_t)W * H * D;
+            std::vector<float> raw(n * ch);
+            if (fread(raw.data(), 4, raw.size(), f) == raw.size()) {
+                data.assign(n, 0.0f);
+                for (size_t c = 0; c < n; c++) {
+                    float s = 0.0f;
+                    for (int q = 0; q < ch; q++) s += raw[c * ch + q];
+                    data[c] = ch == 1 ? s : s / (float)ch;
+                }
+                ok = true;
+            }
+        }
+    } else if (N > 0) {
+        const size_t n = (size_t)N * N * N;
+        std::vector<float> raw(n);
+        if (fread(raw.data(), 4, n, f) == n) {
+            W = H = D = N;
+            data.assign(n, 0.0f);
+            for (int i = 0; i < N; i++)
+                for (int j = 0; j < N; j++)
+                    for (int k = 0; k < N; k++)
+                        data[((size_t)i * N + j) * N + k] = raw[((size_t)k * N + j) * N + i];
+            ok = true;
+        }
+    }
+    fclose(f);
+    return ok;
+}
+
+bool ZQ_RenderVolume3D(const float* density, int W, int H, int D, const zqs_camera& cam, std::vector<float>& rgba) {
+    if (!density || W <= 0 || H <= 0 || D <= 0 || cam.width <= 0 || cam.height <= 0) return false;
+    const size_t nv = (size_t)W * H * D, ni = (size_t)cam.width * cam.height * 4;
+    float *dv = nullptr, *di = nullptr;
+    bool ok = cudaMalloc(&dv, nv * sizeof(float)) == cudaSuccess && cudaMalloc(&di, ni * sizeof(float)) == cudaSuccess &&
+              cudaMemcpy(dv, density, nv * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess;
+    if (ok) ok = zqs_render_density(dv, W, H, D, &cam, di, nullptr) == ZQS_OK || fail("ZQ_RenderVolume3D");
+    if (ok) {
+        rgba.resize(ni);
+        ok = cudaMemcpy(rgba.data(), di, ni * sizeof(float), cudaMemcpyDeviceToHost) == cudaSuccess;
+    }
+    cudaFree(dv);
+    cudaFree(di);
+    return ok;
+}
+
+bool ZQ_WriteRenderPPM(const char* file, const std::vector<float>& rgba, int width, int height) {
+    if (!file || width <= 0 || height <= 0 || rgba.size() < (size_t)width * height * 4) return false;
+    FILE* f = fopen(file, "wb");
+    if (!f) return false;
+    fprintf(f, "P6\n%d %d\n255\n", width, height);
+    std::vector<uint8_t> row((size_t)width * 3);
+    bool ok = true;
+    for (int y = height - 1; y >= 0 && ok; y--) {  // top row first
+        for (int x = 0; x < width; x++)
+            for (int c = 0; c < 3; c++) {
+                const float v = std::min(std::max(rgba[((size_t)y * width + x) * 4 + c], 0.0f), 1.0f);
+                row[(size_t)x * 3 + c] = (uint8_t)(v * 255.0f + 0.5f);
+            }
+        ok = fwrite(row.data(), 1, row.size(), f) == row.size();
+    }
+    fclose(f);
+    return ok;
+}
+
+bool ZQ_RenderSequence3D(const char* fold, const char* prefix, int baseID, int num, const char* suffix, int N,
+                         int imageWidth, int imageHeight, const char* outFold) {
+    if (!fold || !prefix || !suffix || !outFold || num < 0) return false;
+    for (int n = 0; n < num; n++) {
+        const std::string in = std::string(fold) + "/" + prefix + std::to_string(baseID + n) + suffix;
+        std::vector<float> vol, img;
+        int W = 0, H = 0, D = 0;
+        if (!ZQ_LoadVolume3D(in.c_str(), N, vol, W, H, D)) {
+            fprintf(stderr, "zqs: cannot read %s\n", in.c_str());
+            return false;
+        }
+        zqs_camera cam;
+        zqs_camera_default(&cam, imageWidth, imageHeight, W, H, D);
+        if (!ZQ_RenderVolume3D(vol.data(), W, H, D, cam, img)) return false;
+        const std::string out = std::string(outFold) + "/render" + std::to_string(baseID + n) + ".ppm";
+        if (!ZQ_WriteRenderPPM(out.c_str(), img, imageWidth, imageHeight)) return false;
+    }
+    return true;
 }
 
 // ----------------------------------------------------------------- simulation
