@@ -68,29 +68,7 @@ __device__ __forceinline__ float tri_unscaled(const float* __restrict__ f, const
     float c1 = lerpf(c01, c11, c.ty);
     return lerpf(c0, c1, c.tz);
 }
-__device__ __forceinline__ float3 tri4(const float4* __restrict__ f, const Corners& c) {
-    float4 a00 = __ldg(f + c.r00 + c.i0), b00 = __ldg(f + c.r00 + c.i1);
-    float4 a10 = __ldg(f + c.r10 + c.i0), b10 = __ldg(f + c.r10 + c.i1);
-    float4 a01 = __ldg(f + c.r01 + c.i0), b01 = __ldg(f + c.r01 + c.i1);
-    float4 a11 = __ldg(f + c.r11 + c.i0), b11 = __ldg(f + c.r11 + c.i1);
-    float3 r;
-    {
-        float c00 = lerpf(a00.x, b00.x, c.tx), c10 = lerpf(a10.x, b10.x, c.tx);
-        float c01 = lerpf(a01.x, b01.x, c.tx), c11 = lerpf(a11.x, b11.x, c.tx);
-        r.x = lerpf(lerpf(c00, c10, c.ty), lerpf(c01, c11, c.ty), c.tz);
-    }
-    {
-        float c00 = lerpf(a00.y, b00.y, c.tx), c10 = lerpf(a10.y, b10.y, c.tx);
-        float c01 = lerpf(a01.y, b01.y, c.tx), c11 = lerpf(a11.y, b11.y, c.tx);
-        r.y = lerpf(lerpf(c00, c10, c.ty), lerpf(c01, c11, c.ty), c.tz);
-    }
-    {
-        float c00 = lerpf(a00.z, b00.z, c.tx), c10 = lerpf(a10.z, b10.z, c.tx);
-        float c01 = lerpf(a01.z, b01.z, c.tx), c11 = lerpf(a11.z, b11.z, c.tx);
-        r.z = lerpf(lerpf(c00, c10, c.ty), lerpf(c01, c11, c.ty), c.tz);
-    }
-    return r;
-}
+__device__ __forceinline__ float3 tri4(const float4* __restrict__ f, const Corners& c);
 __device__ __forceinline__ float tri4c(const float4* __restrict__ f4, int q, const Corners& c) {
     const float* f = reinterpret_cast<const float*>(f4);
     auto at = [&](int o) -> float { return __ldg(f + (size_t)o * 4 + q); };
@@ -172,6 +150,39 @@ __device__ __forceinline__ float2 lerp_step2(float a0, float a1, float b0, float
     asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pack2(b0, b1)), "l"(pack2(a0, a1)));
     asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(m) : "l"(pack2(t0, t1)), "l"(d));
     return unpack2(m);
+}
+
+// x, then y, then z per component as in tri(); the x and y components go
+// through the packed sub/mul of lerp_step2 (same roundings), z stays scalar.
+__device__ __forceinline__ float3 tri4(const float4* __restrict__ f, const Corners& c) {
+    const float4 a00 = __ldg(f + c.r00 + c.i0), b00 = __ldg(f + c.r00 + c.i1);
+    const float4 a10 = __ldg(f + c.r10 + c.i0), b10 = __ldg(f + c.r10 + c.i1);
+    const float4 a01 = __ldg(f + c.r01 + c.i0), b01 = __ldg(f + c.r01 + c.i1);
+    const float4 a11 = __ldg(f + c.r11 + c.i0), b11 = __ldg(f + c.r11 + c.i1);
+    // along x: (x, y) packed, z scalar
+    auto lx = [&](const float4& a, const float4& b, float& ox, float& oy, float& oz) {
+        const float2 m = lerp_step2(a.x, a.y, b.x, b.y, c.tx, c.tx);
+        ox = __fadd_rn(a.x, m.x);
+        oy = __fadd_rn(a.y, m.y);
+        oz = lerpf(a.z, b.z, c.tx);
+    };
+    float x00, y00, z00, x10, y10, z10, x01, y01, z01, x11, y11, z11;
+    lx(a00, b00, x00, y00, z00);
+    lx(a10, b10, x10, y10, z10);
+    lx(a01, b01, x01, y01, z01);
+    lx(a11, b11, x11, y11, z11);
+    // along y
+    const float2 m0 = lerp_step2(x00, y00, x10, y10, c.ty, c.ty);
+    const float2 m1 = lerp_step2(x01, y01, x11, y11, c.ty, c.ty);
+    const float x0 = __fadd_rn(x00, m0.x), y0 = __fadd_rn(y00, m0.y), z0 = lerpf(z00, z10, c.ty);
+    const float x1 = __fadd_rn(x01, m1.x), y1 = __fadd_rn(y01, m1.y), z1 = lerpf(z01, z11, c.ty);
+    // along z
+    const float2 mz = lerp_step2(x0, y0, x1, y1, c.tz, c.tz);
+    float3 r;
+    r.x = __fadd_rn(x0, mz.x);
+    r.y = __fadd_rn(y0, mz.y);
+    r.z = lerpf(z0, z1, c.tz);
+    return r;
 }
 __device__ __forceinline__ float tri0_quad(const float4* __restrict__ q, const Layout& L, const Tri0& c) {
     const float4 a = __ldg(q + c.r);
