@@ -4,6 +4,7 @@
 // object's velocity, then the cell flags are rebuilt.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <string>
 #include <vector>
 
@@ -64,23 +65,34 @@ extern "C" ZQS_API int zqs_grid_stamp_objects(zqs_grid* g, const zqs_object* obj
         set_error("zqs_grid_stamp_objects: set the parameters first (h / dt scales the velocities)");
         return ZQS_ENOTREADY;
     }
-    size_t need = 0;
+    // every mask in one host buffer, copied once: the stamping kernels then
+    // read their object's slice (no synchronisation between objects)
+    std::vector<size_t> off(n + 1, 0);
     for (int q = 0; q < n; q++) {
         const zqs_object& o = objs[q];
         if (o.size[0] < 0 || o.size[1] < 0 || o.size[2] < 0 || (!o.mask && o.size[0] * o.size[1] * o.size[2] > 0)) {
             set_error("zqs_grid_stamp_objects: object " + std::to_string(q) + " has a bad size or no mask");
             return ZQS_EINVAL;
         }
-        need = std::max(need, (size_t)o.size[0] * o.size[1] * o.size[2]);
+        off[q + 1] = off[q] + (size_t)o.size[0] * o.size[1] * o.size[2];
     }
+    const size_t need = off[n];
     cudaStream_t s = g->pick(stream);
+    // the previous call's copy and kernels may still read the buffer
+    ZQS_CUDA_TRY(cudaStreamSynchronize(s));
     if (need > g->obj_mask_cap) {
-        ZQS_CUDA_TRY(cudaStreamSynchronize(s));
         if (g->obj_mask) cudaFree(g->obj_mask);
         g->obj_mask = nullptr;
         g->obj_mask_cap = 0;
         ZQS_CUDA_TRY(cudaMalloc(&g->obj_mask, need));
         g->obj_mask_cap = need;
+    }
+    if (need > 0) {
+        std::vector<uint8_t> all(need);
+        for (int q = 0; q < n; q++)
+            if (off[q + 1] > off[q]) std::memcpy(all.data() + off[q], objs[q].mask, off[q + 1] - off[q]);
+        // pageable source: the copy has completed when the call returns
+        ZQS_CUDA_TRY(cudaMemcpyAsync(g->obj_mask, all.data(), need, cudaMemcpyHostToDevice, s));
     }
     const Layout& L = g->g.L;
     const dim3 b(32, 8, 1);
@@ -91,18 +103,15 @@ extern "C" ZQS_API int zqs_grid_stamp_objects(zqs_grid* g, const zqs_object* obj
     const double scale = (double)(g->params.voxel_size / g->params.step_time);
     for (int q = 0; q < n; q++) {
         const zqs_object& o = objs[q];
-        const size_t nb = (size_t)o.size[0] * o.size[1] * o.size[2];
+        const size_t nb = off[q + 1] - off[q];
         if (nb == 0) continue;
-        ZQS_CUDA_TRY(cudaMemcpyAsync(g->obj_mask, o.mask, nb, cudaMemcpyHostToDevice, s));
         const int cu = (int)((double)o.vel[0] * scale);
         const int cv = (int)((double)o.vel[1] * scale);
         const int cw = (int)((double)o.vel[2] * scale);
         k_stamp_object<<<dim3((o.size[0] + 31) / 32, (o.size[1] + 7) / 8, o.size[2]), b, 0, s>>>(
-            L, g->occ_dense, g->g.u, g->g.v, g->g.w, g->obj_mask, o.size[0], o.size[1], o.size[2],
+            L, g->occ_dense, g->g.u, g->g.v, g->g.w, g->obj_mask + off[q], o.size[0], o.size[1], o.size[2],
             o.pos[0] - o.center[0], o.pos[1] - o.center[1], o.pos[2] - o.center[2], (float)cu, (float)cv, (float)cw);
         ZQS_LAUNCH_CHECK("k_stamp_object");
-        // the mask buffer is reused by the next object
-        ZQS_CUDA_TRY(cudaStreamSynchronize(s));
     }
     LaunchCounter lc;
     int rc = launch_build_flags(g->g, g->occ_dense, g->params.solver, s, lc);

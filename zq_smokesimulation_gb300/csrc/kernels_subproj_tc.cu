@@ -394,11 +394,12 @@ int subproj_tc_prepare(int s) {
     MSplit m;
     int rc = get_msplit(s, m);
     if (rc) return rc;
-    static bool attr_set = false;
-    if (!attr_set) {
-        ZQS_CUDA_TRY(cudaFuncSetAttribute(k_subproj_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBudget));
-        attr_set = true;
-    }
+    static std::once_flag once;
+    static cudaError_t attr = cudaSuccess;
+    std::call_once(once, [] {
+        attr = cudaFuncSetAttribute(k_subproj_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBudget);
+    });
+    ZQS_CUDA_TRY(attr);
     return ZQS_OK;
 }
 
