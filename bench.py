@@ -63,6 +63,19 @@ def parse():
     return ap.parse_args()
 
 
+def replicas_value(ms_local: float, world: int, cells: int, steps: int, dist=None, device="cuda"):
+    """Replicas only (a grid does not shard): every rank steps its own grid; the
+    job's time is the slowest rank's (max over ranks) and the value is all
+    ranks' cell-steps over that time.  Returns (ms, Gcell-steps/s)."""
+    ms = float(ms_local)
+    if dist is not None:
+        import torch
+        t = torch.tensor([ms], device=device, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, world * cells * steps / (ms * 1e-3) / 1e9
+
+
 def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
@@ -540,12 +553,8 @@ def run_ours(args):
                 g.download_into(f, host[f].data_ptr(), sp)
         b.record(stream)
         b.synchronize()
-        e2e_ms = a.elapsed_time(b)
-        if dist is not None:
-            t = torch.tensor([e2e_ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_ms = float(t.item())
-        e2e = {"value": world * cells * e2e_steps / (e2e_ms * 1e-3) / 1e9, "unit": UNIT,
+        e2e_ms, e2e_value = replicas_value(a.elapsed_time(b), world, cells, e2e_steps, dist)
+        e2e = {"value": e2e_value, "unit": UNIT,
                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                "path": "zqs_grid_upload x5 (pinned host) + zqs_grid_step + zqs_grid_download x5"}
     batch = None
@@ -562,11 +571,7 @@ def run_ours(args):
         adjoint = {f"control{n}": measure_adjoint(args, stream, int(n)) for n in args.adjoint.split(",") if n}
     clocks = sampler.stop()
 
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * cells * args.steps / (ms * 1e-3) / 1e9
+    ms, value = replicas_value(ms, world, cells, args.steps, dist)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
