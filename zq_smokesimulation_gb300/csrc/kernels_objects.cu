@@ -70,11 +70,15 @@ extern "C" ZQS_API int zqs_grid_stamp_objects(zqs_grid* g, const zqs_object* obj
     std::vector<size_t> off(n + 1, 0);
     for (int q = 0; q < n; q++) {
         const zqs_object& o = objs[q];
-        if (o.size[0] < 0 || o.size[1] < 0 || o.size[2] < 0 || (!o.mask && o.size[0] * o.size[1] * o.size[2] > 0)) {
+        const size_t nb = (o.size[0] < 0 || o.size[1] < 0 || o.size[2] < 0)
+                              ? 0
+                              : (size_t)o.size[0] * (size_t)o.size[1] * (size_t)o.size[2];
+        // z is a launch dimension (at most 65535 planes)
+        if (o.size[0] < 0 || o.size[1] < 0 || o.size[2] < 0 || o.size[2] > 65535 || (!o.mask && nb > 0)) {
             set_error("zqs_grid_stamp_objects: object " + std::to_string(q) + " has a bad size or no mask");
             return ZQS_EINVAL;
         }
-        off[q + 1] = off[q] + (size_t)o.size[0] * o.size[1] * o.size[2];
+        off[q + 1] = off[q] + nb;
     }
     const size_t need = off[n];
     cudaStream_t s = g->pick(stream);
