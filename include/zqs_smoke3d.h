@@ -242,6 +242,8 @@ public:
     };
     ZQ_SmokeMovingObject3D();
     ~ZQ_SmokeMovingObject3D();
+    ZQ_SmokeMovingObject3D(const ZQ_SmokeMovingObject3D&) = delete;  /* owns occupy */
+    ZQ_SmokeMovingObject3D& operator=(const ZQ_SmokeMovingObject3D&) = delete;
     int cx, cy, cz;        // rotation centre
     int posx, posy, posz;  // position in the grid
     int sizex, sizey, sizez;
@@ -294,6 +296,8 @@ class ZQS_CXX_API ZQ_SmokeSimulation3D {
 public:
     ZQ_SmokeSimulation3D();
     ~ZQ_SmokeSimulation3D();
+    ZQ_SmokeSimulation3D(const ZQ_SmokeSimulation3D&) = delete;  /* owns the grid and the objects */
+    ZQ_SmokeSimulation3D& operator=(const ZQ_SmokeSimulation3D&) = delete;
 
     bool Init(const char* file);
     /* frameCount frames; frame i's density to <fold>/frame<i>.di3 (plus
