@@ -117,3 +117,51 @@ def test_moving_sequence_matches_oracle(zqs_lib, oracle32, solver):
         for k in ("u", "v", "w", "T", "rho"):
             np.testing.assert_array_equal(out[k], st[k], err_msg=f"step {t} field {k}")
     g.close()
+
+
+def python_stamp(W, H, D, u, v, w, objs, closed, h, dt):
+    """ZQ_ApplyMovingObject3D (Utils3D:1933-2046) restated in plain Python: the
+    occupancy is cleared, each object's solid in-domain voxels occupy their
+    cell and set its six faces to int(vel * (double)(h / dt)), then the closed
+    solvers' walls (mode 2: all but the y = H-1 layer) are occupied."""
+    occ = np.zeros((D, H, W), np.uint8)
+    scale = float(np.float32(h) / np.float32(dt))
+    for o in objs:
+        m = np.asarray(o["mask"], bool)
+        sz, sy, sx = m.shape
+        cx, cy, cz = o["center"]
+        px, py, pz = o["pos"]
+        vel = [int(c * scale) for c in o["vel"]]
+        for k in range(sz):
+            for j in range(sy):
+                for i in range(sx):
+                    if not m[k, j, i]:
+                        continue
+                    x, y, z = i + px - cx, j + py - cy, k + pz - cz
+                    if 0 <= x < W and 0 <= y < H and 0 <= z < D:
+                        occ[z, y, x] = 1
+                        u[z, y, x] = u[z, y, x + 1] = vel[0]
+                        v[z, y, x] = v[z, y + 1, x] = vel[1]
+                        w[z, y, x] = w[z + 1, y, x] = vel[2]
+    if closed:
+        occ[:, :, 0] = occ[:, :, W - 1] = 1
+        occ[:, 0, :] = 1
+        if closed == 1:
+            occ[:, H - 1, :] = 1
+        occ[0, :, :] = occ[D - 1, :, :] = 1
+    return occ
+
+
+@pytest.mark.parametrize("closed", [0, 1, 2])
+def test_oracle_stamp_matches_python_restatement(oracle32, closed):
+    w = base(closed == 1)
+    p = w.params
+    st = oracle32.state(w)
+    occ = np.ascontiguousarray(w.occ, np.uint8).copy()
+    objs = objects(seed=11)
+    oracle32.stamp_objects(W, H, D, st, occ, objs, closed, p)
+    ref = oracle32.state(w)
+    ref_occ = python_stamp(W, H, D, ref["u"], ref["v"], ref["w"], objs, closed, p.voxel_size, p.step_time)
+    np.testing.assert_array_equal(occ, ref_occ)
+    for k in ("u", "v", "w"):
+        np.testing.assert_array_equal(st[k], ref[k])
