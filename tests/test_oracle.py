@@ -353,3 +353,35 @@ def test_golden_fixtures(oracle32, oracle64):
                     assert np.array_equal(st[k], ref), (f.name, k)
                 else:
                     np.testing.assert_allclose(st[k], ref, rtol=0, atol=1e-13, err_msg=f"{f.name} {k}")
+
+
+def _py_advect_scalar_mac(phi, u, v, w, occ, steps, dt, h):
+    """One semi-Lagrangian pass of a cell field with MAC velocity (every cell
+    backtraced from its centre, sampled at the last accepted point)."""
+    D, H, W = occ.shape
+    out = np.empty_like(phi)
+    for k in range(D):
+        for j in range(H):
+            for i in range(W):
+                last, tri = _py_backtrace_mac(u, v, w, occ, (i + 0.5, j + 0.5, k + 0.5), steps, dt, h)
+                out[k, j, i] = tri(phi, (last[0] - 0.5, last[1] - 0.5, last[2] - 0.5))
+    return out
+
+
+def test_scalar_bfecc_matches_pure_python_restatement(oracle64):
+    """cu_Advect_Scalar_MAC_Velocity_BFECC (Adv3D:1586-1648): forward pass,
+    a pass back with the negated velocity, input = input*1.5 - back*0.5
+    (Input_Increment_Kernel, Adv3D:56-64, in double), forward pass again."""
+    w_ = wl.small_case(6, 5, 4, vel_amp=0.4, substeps=2)
+    st = {k: np.asarray(v, np.float64).copy() for k, v in w_.state().items()}
+    T0 = st["T"].copy()
+    assert oracle64.advect_scalar(w_.W, w_.H, w_.D, st, w_.occ, w_.params, capi.ADV_SCA_MAC_BFECC) == 0
+    dt = float(w_.params.step_time) / w_.params.substeps
+    h = float(np.float32(w_.params.voxel_size))
+    n = w_.params.substeps
+    u, v, w = st["u"], st["v"], st["w"]
+    f1 = _py_advect_scalar_mac(T0, u, v, w, w_.occ, n, dt, h)
+    f2 = _py_advect_scalar_mac(f1, -u, -v, -w, w_.occ, n, dt, h)
+    corrected = T0 * 1.5 - f2 * 0.5
+    expect = _py_advect_scalar_mac(corrected, u, v, w, w_.occ, n, dt, h)
+    np.testing.assert_array_equal(st["T"], expect)
