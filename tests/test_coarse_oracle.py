@@ -56,6 +56,54 @@ def test_submatrix_leaves_the_mean_divergence(oracle32, s):
     np.testing.assert_allclose(d1, np.full_like(d1, d0.mean()), atol=2e-5 * np.abs(d0).max())
 
 
+@pytest.mark.parametrize("s", [2, 3, 4])
+def test_submatrix_equals_the_svd_pseudo_inverse_form(oracle32, s):
+    """ZQ_InitSubMatPoisson3D (Utils3D:1151-1391) forms the block matrix with
+    an SVD pseudo-inverse (ZQ_SVD::Invert): with L the block's Neumann
+    Laplacian, P = L without cell 0's column, V the cell divergence over the
+    block faces, pressures p = [0; P+ V x] and the interior faces x - (p_b - p_a).
+    The oracle builds P+ by Cholesky on the normal equations; numpy's pinv (an
+    SVD) gives the same matrix to rounding."""
+    n, nf = s ** 3, 3 * s * s * (s + 1)
+    uix, vix, wix, rows = block_faces(s)
+    cell = lambda i, j, k: (k * s + j) * s + i
+    L = np.zeros((n, n))
+    V = np.zeros((n, nf))
+    for k in range(s):
+        for j in range(s):
+            for i in range(s):
+                c = cell(i, j, k)
+                for di, dj, dk in ((-1, 0, 0), (1, 0, 0), (0, -1, 0), (0, 1, 0), (0, 0, -1), (0, 0, 1)):
+                    a, b, e = i + di, j + dj, k + dk
+                    if 0 <= a < s and 0 <= b < s and 0 <= e < s:
+                        L[c, cell(a, b, e)] = 1.0
+                        L[c, c] -= 1.0
+                V[c, uix(i + 1, j, k)] += 1.0
+                V[c, uix(i, j, k)] -= 1.0
+                V[c, vix(i, j + 1, k)] += 1.0
+                V[c, vix(i, j, k)] -= 1.0
+                V[c, wix(i, j, k + 1)] += 1.0
+                V[c, wix(i, j, k)] -= 1.0
+    pres = np.vstack([np.zeros((1, nf)), np.linalg.pinv(L[:, 1:]) @ V])   # n x nf, cell 0 pinned to 0
+    ref = []
+    for k in range(s):
+        for j in range(s):
+            for i in range(1, s):
+                ref.append(np.eye(nf)[uix(i, j, k)] - (pres[cell(i, j, k)] - pres[cell(i - 1, j, k)]))
+    for k in range(s):
+        for j in range(1, s):
+            for i in range(s):
+                ref.append(np.eye(nf)[vix(i, j, k)] - (pres[cell(i, j, k)] - pres[cell(i, j - 1, k)]))
+    for k in range(1, s):
+        for j in range(s):
+            for i in range(s):
+                ref.append(np.eye(nf)[wix(i, j, k)] - (pres[cell(i, j, k)] - pres[cell(i, j, k - 1)]))
+    ref = np.array(ref)
+    M = oracle32.submatrix(s).astype(np.float64)
+    assert M.shape == ref.shape
+    np.testing.assert_allclose(M, ref, rtol=0, atol=2e-6 * np.abs(ref).max())
+
+
 def coarse_case(W, H, D, s, K, seed=5, walls=True, omega=1.5):
     occ = wl.walls_open_top(W, H, D) if walls else np.zeros((D, H, W), np.uint8)
     p = wl.smoke_params(W, K, omega=omega, solver=capi.SOLVER_COARSE_OPEN)
