@@ -385,3 +385,75 @@ def test_scalar_bfecc_matches_pure_python_restatement(oracle64):
     corrected = T0 * 1.5 - f2 * 0.5
     expect = _py_advect_scalar_mac(corrected, u, v, w, w_.occ, n, dt, h)
     np.testing.assert_array_equal(st["T"], expect)
+    assert not np.array_equal(st["T"], T0)
+
+
+def _py_advect_faces(inp, vel, occ, steps, dt, h):
+    """Advect_Velocity_inMAC_outMAC_{u,v,w}_Kernel (Adv3D:233-278 and the v, w
+    forms): every face backtraced from its centre through the MAC velocity
+    `vel`, the field `inp` (u, v, w) sampled at the last accepted point."""
+    D, H, W = occ.shape
+    u, v, w = vel
+    out = {k: np.empty_like(inp[k]) for k in ("u", "v", "w")}
+    starts = {"u": lambda i, j, k: (i, j + 0.5, k + 0.5), "v": lambda i, j, k: (i + 0.5, j, k + 0.5),
+              "w": lambda i, j, k: (i + 0.5, j + 0.5, k)}
+    shift = {"u": (0.0, 0.5, 0.5), "v": (0.5, 0.0, 0.5), "w": (0.5, 0.5, 0.0)}
+    for c in ("u", "v", "w"):
+        nz, ny, nx = inp[c].shape
+        for k in range(nz):
+            for j in range(ny):
+                for i in range(nx):
+                    last, tri = _py_backtrace_mac(u, v, w, occ, starts[c](i, j, k), steps, dt, h)
+                    sx, sy, sz = shift[c]
+                    out[c][k, j, i] = tri(inp[c], (last[0] - sx, last[1] - sy, last[2] - sz))
+    return out
+
+
+def _py_apply_open(adv, occ, fld):
+    """Apply_Advect_Velocity_Result_Open_{u,v,w}_Kernel (Adv3D:470-576): a face
+    takes the advected value when its in-domain cells are free."""
+    D, H, W = occ.shape
+    free = occ == 0
+    for k in range(D):
+        for j in range(H):
+            for i in range(W + 1):
+                if (i == 0 and free[k, j, 0]) or (i == W and free[k, j, W - 1]) or \
+                        (0 < i < W and free[k, j, i] and free[k, j, i - 1]):
+                    fld["u"][k, j, i] = adv["u"][k, j, i]
+    for k in range(D):
+        for j in range(H + 1):
+            for i in range(W):
+                if (j == 0 and free[k, 0, i]) or (j == H and free[k, H - 1, i]) or \
+                        (0 < j < H and free[k, j, i] and free[k, j - 1, i]):
+                    fld["v"][k, j, i] = adv["v"][k, j, i]
+    for k in range(D + 1):
+        for j in range(H):
+            for i in range(W):
+                if (k == 0 and free[0, j, i]) or (k == D and free[D - 1, j, i]) or \
+                        (0 < k < D and free[k, j, i] and free[k - 1, j, i]):
+                    fld["w"][k, j, i] = adv["w"][k, j, i]
+
+
+def test_velocity_bfecc_matches_pure_python_restatement(oracle64):
+    """cu_Advect_Velocity_inMAC_outMAC_BFECC (Adv3D:1240-1335): forward pass,
+    a pass of that result with the negated velocity, u = u*1.5 - back*0.5 in
+    place, a forward pass of the corrected field through the original
+    velocity, then the open write-back into the corrected field (faces it
+    leaves alone keep the corrected value)."""
+    w_ = wl.small_case(5, 4, 4, vel_amp=0.4, substeps=2)
+    st = {k: np.asarray(v, np.float64).copy() for k, v in w_.state().items()}
+    vel0 = {k: st[k].copy() for k in ("u", "v", "w")}
+    assert oracle64.advect_velocity(w_.W, w_.H, w_.D, st, w_.occ, w_.params, capi.ADV_VEL_INMAC_OUTMAC_BFECC) == 0
+    dt = float(w_.params.step_time) / w_.params.substeps
+    h = float(np.float32(w_.params.voxel_size))
+    n = w_.params.substeps
+    vel = (vel0["u"], vel0["v"], vel0["w"])
+    neg = (-vel0["u"], -vel0["v"], -vel0["w"])
+    f1 = _py_advect_faces(vel0, vel, w_.occ, n, dt, h)
+    f2 = _py_advect_faces(f1, neg, w_.occ, n, dt, h)
+    corrected = {k: vel0[k] * 1.5 - f2[k] * 0.5 for k in ("u", "v", "w")}
+    f3 = _py_advect_faces(corrected, vel, w_.occ, n, dt, h)
+    _py_apply_open(f3, w_.occ, corrected)
+    for k in ("u", "v", "w"):
+        np.testing.assert_array_equal(st[k], corrected[k], err_msg=k)
+        assert not np.array_equal(st[k], vel0[k]), k   # the case moves something
