@@ -457,3 +457,56 @@ def test_velocity_bfecc_matches_pure_python_restatement(oracle64):
     for k in ("u", "v", "w"):
         np.testing.assert_array_equal(st[k], corrected[k], err_msg=k)
         assert not np.array_equal(st[k], vel0[k]), k   # the case moves something
+
+
+def test_regular_velocity_advection_matches_pure_python_restatement(oracle64):
+    """cu_Advect_Velocity_inRegular_outRegular (Adv3D:1061-1101 with the kernel
+    at :77-113): cell-centred velocity from the MAC faces, each cell
+    backtraced through it and the cell velocity sampled at the last accepted
+    point, back to faces (interior faces average their two cells, domain faces
+    copy the inner cell), then the open write-back."""
+    w_ = wl.small_case(5, 4, 4, vel_amp=0.4, substeps=2)
+    st = {k: np.asarray(v, np.float64).copy() for k, v in w_.state().items()}
+    u, v, w = (st[k].copy() for k in ("u", "v", "w"))
+    assert oracle64.advect_velocity(w_.W, w_.H, w_.D, st, w_.occ, w_.params, capi.ADV_VEL_INREG_OUTREG) == 0
+    D, H, W = w_.occ.shape
+    dt = float(w_.params.step_time) / w_.params.substeps
+    h = float(np.float32(w_.params.voxel_size))
+    n = w_.params.substeps
+    cx = 0.5 * (u[:, :, :-1] + u[:, :, 1:])
+    cy = 0.5 * (v[:, :-1, :] + v[:, 1:, :])
+    cz = 0.5 * (w[:-1, :, :] + w[1:, :, :])
+    # the MAC helper's tri() applies to any cell field; sample cells at pos - 0.5
+    _, tri = _py_backtrace_mac(u, v, w, w_.occ, (0.5, 0.5, 0.5), 0, dt, h)
+    cellv = lambda x, y, z: tuple(tri(f, (x - 0.5, y - 0.5, z - 0.5)) for f in (cx, cy, cz))
+    out = np.zeros((D, H, W, 3))
+    for k in range(D):
+        for j in range(H):
+            for i in range(W):
+                x, y, z = i + 0.5, j + 0.5, k + 0.5
+                vx, vy, vz = cellv(x, y, z)
+                last = (x, y, z)
+                for _ in range(n):
+                    if not (0 <= x <= W and 0 <= y <= H and 0 <= z <= D):
+                        break
+                    if w_.occ[min(max(int(math.floor(z)), 0), D - 1), min(max(int(math.floor(y)), 0), H - 1),
+                              min(max(int(math.floor(x)), 0), W - 1)]:
+                        break
+                    last = (x, y, z)
+                    x, y, z = x - (vx * dt) / h, y - (vy * dt) / h, z - (vz * dt) / h
+                    vx, vy, vz = cellv(x, y, z)
+                out[k, j, i] = cellv(*last)
+    fu = np.empty_like(u)
+    fu[:, :, 0], fu[:, :, W] = out[:, :, 0, 0], out[:, :, W - 1, 0]
+    fu[:, :, 1:W] = 0.5 * (out[:, :, 1:, 0] + out[:, :, :-1, 0])
+    fv = np.empty_like(v)
+    fv[:, 0, :], fv[:, H, :] = out[:, 0, :, 1], out[:, H - 1, :, 1]
+    fv[:, 1:H, :] = 0.5 * (out[:, 1:, :, 1] + out[:, :-1, :, 1])
+    fw = np.empty_like(w)
+    fw[0], fw[D] = out[0, :, :, 2], out[D - 1, :, :, 2]
+    fw[1:D] = 0.5 * (out[1:, :, :, 2] + out[:-1, :, :, 2])
+    ref = {"u": u.copy(), "v": v.copy(), "w": w.copy()}
+    _py_apply_open({"u": fu, "v": fv, "w": fw}, w_.occ, ref)
+    for k in ("u", "v", "w"):
+        np.testing.assert_array_equal(st[k], ref[k], err_msg=k)
+        assert not np.array_equal(st[k], {"u": u, "v": v, "w": w}[k]), k
