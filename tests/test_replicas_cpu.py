@@ -39,7 +39,7 @@ def _rank_main(rank, world, port, out):
 def test_two_replicas_take_the_slowest_rank(tmp_path):
     world = 2
     port = _free_port()
-    out = mp.Manager().dict()
+    out = mp.get_context("spawn").Manager().dict()   # no fork of this (threaded) process
     mp.start_processes(_rank_main, args=(world, port, out), nprocs=world, start_method="spawn", join=True)
     for r in range(world):
         ms, value = out[r]
