@@ -510,3 +510,103 @@ def test_regular_velocity_advection_matches_pure_python_restatement(oracle64):
     for k in ("u", "v", "w"):
         np.testing.assert_array_equal(st[k], ref[k], err_msg=k)
         assert not np.array_equal(st[k], {"u": u, "v": v, "w": w}[k]), k
+
+
+def test_force_matches_pure_python_restatement(oracle64):
+    """cu_AddForce3D (ZQ_CUDA_AddForce3D.cu:510-556 with the kernels at :11-420):
+    cell-centred velocity, vorticity by central differences / (2h) on interior
+    cells, the gradient of its magnitude (one-sided at the domain faces,
+    normalised when non-zero), force = confine h (N x w) plus buoyancy on y,
+    then every face adds dt times the mean of its two free cells' force (one
+    cell at a domain face).  Gravity on the density is 0 here (the reference
+    has no such term)."""
+    W, H, D = 6, 5, 5
+    occ = wl.walls_open_top(W, H, D)
+    p = wl.smoke_params(W, 1)
+    p.confine = 0.3
+    p.gravity = 0.0
+    rng = np.random.default_rng(8)
+    st = {"u": rng.standard_normal((D, H, W + 1)), "v": rng.standard_normal((D, H + 1, W)),
+          "w": rng.standard_normal((D + 1, H, W)), "T": rng.random((D, H, W)), "rho": rng.random((D, H, W))}
+    u0, v0, w0 = st["u"].copy(), st["v"].copy(), st["w"].copy()
+    oracle64.add_force(W, H, D, st, occ, p)
+    h, dt = float(np.float32(p.voxel_size)), float(np.float32(p.step_time))
+    eps, beta, tamb = float(np.float32(p.confine)), float(np.float32(p.buoyancy)), float(np.float32(p.tamb))
+    cu = 0.5 * (u0[:, :, :-1] + u0[:, :, 1:])
+    cv = 0.5 * (v0[:, :-1, :] + v0[:, 1:, :])
+    cw = 0.5 * (w0[:-1, :, :] + w0[1:, :, :])
+    vort = np.zeros((D, H, W, 3))
+    vs = np.zeros((D, H, W))
+    for k in range(1, D - 1):
+        for j in range(1, H - 1):
+            for i in range(1, W - 1):
+                a = (cw[k, j + 1, i] - cw[k, j - 1, i] - cv[k + 1, j, i] + cv[k - 1, j, i]) / (2 * h)
+                b = (cu[k + 1, j, i] - cu[k - 1, j, i] - cw[k, j, i + 1] + cw[k, j, i - 1]) / (2 * h)
+                c = (cv[k, j, i + 1] - cv[k, j, i - 1] - cu[k, j + 1, i] + cu[k, j - 1, i]) / (2 * h)
+                vort[k, j, i] = (a, b, c)
+                vs[k, j, i] = math.sqrt(a * a + b * b + c * c)
+    force = np.zeros((D, H, W, 3))
+    for k in range(D):
+        for j in range(H):
+            for i in range(W):
+                def g(axis):
+                    # d|w|/d(axis): one-sided at the domain faces, central inside
+                    n, pos = (W, H, D)[axis], (i, j, k)[axis]
+
+                    def at(q):
+                        t = [i, j, k]
+                        t[axis] = q
+                        return vs[t[2], t[1], t[0]]
+                    if pos == 0:
+                        return at(1) - at(0)
+                    if pos == n - 1:
+                        return at(n - 1) - at(n - 2)
+                    return 0.5 * (at(pos + 1) - at(pos - 1))
+                gx, gy, gz = g(0), g(1), g(2)
+                ln = math.sqrt(gx * gx + gy * gy + gz * gz)
+                if ln != 0:
+                    gx, gy, gz = gx / ln, gy / ln, gz / ln
+                wx, wy, wz = vort[k, j, i]
+                fx = eps * h * (gy * wz - gz * wy)
+                fy = eps * h * (gz * wx - gx * wz)
+                fz = eps * h * (gx * wy - gy * wx)
+                fy = fy + beta * (st["T"][k, j, i] - tamb)
+                force[k, j, i] = (fx, fy, fz)
+    free = occ == 0
+    eu, ev, ew = u0.copy(), v0.copy(), w0.copy()
+    for k in range(D):
+        for j in range(H):
+            for i in range(W + 1):
+                if i == 0:
+                    if free[k, j, 0]:
+                        eu[k, j, i] += dt * force[k, j, 0, 0]
+                elif i == W:
+                    if free[k, j, W - 1]:
+                        eu[k, j, i] += dt * force[k, j, W - 1, 0]
+                elif free[k, j, i] and free[k, j, i - 1]:
+                    eu[k, j, i] += dt * 0.5 * (force[k, j, i, 0] + force[k, j, i - 1, 0])
+    for k in range(D):
+        for j in range(H + 1):
+            for i in range(W):
+                if j == 0:
+                    if free[k, 0, i]:
+                        ev[k, j, i] += dt * force[k, 0, i, 1]
+                elif j == H:
+                    if free[k, H - 1, i]:
+                        ev[k, j, i] += dt * force[k, H - 1, i, 1]
+                elif free[k, j, i] and free[k, j - 1, i]:
+                    ev[k, j, i] += dt * 0.5 * (force[k, j, i, 1] + force[k, j - 1, i, 1])
+    for k in range(D + 1):
+        for j in range(H):
+            for i in range(W):
+                if k == 0:
+                    if free[0, j, i]:
+                        ew[k, j, i] += dt * force[0, j, i, 2]
+                elif k == D:
+                    if free[D - 1, j, i]:
+                        ew[k, j, i] += dt * force[D - 1, j, i, 2]
+                elif free[k, j, i] and free[k - 1, j, i]:
+                    ew[k, j, i] += dt * 0.5 * (force[k, j, i, 2] + force[k - 1, j, i, 2])
+    for name, got, exp in (("u", st["u"], eu), ("v", st["v"], ev), ("w", st["w"], ew)):
+        np.testing.assert_array_equal(got, exp, err_msg=name)
+        assert not np.array_equal(got, {"u": u0, "v": v0, "w": w0}[name]), name
