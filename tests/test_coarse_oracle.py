@@ -149,3 +149,66 @@ def test_coarse_rejects_sizes_not_divisible(oracle32):
     occ, p, st = coarse_case(12, 12, 12, 4, K=2)
     p.sub_size = 5
     assert oracle32.project_coarse(12, 12, 12, st, occ, p) == capi.ZQS_EINVAL
+
+
+def _py_block_projection(u, v, w, occ, s):
+    """ZQ_SubProjection3D / ZQ_SolveSubGrid3D restated with numpy: in every
+    s^3 block, the pressure of the least-squares Poisson problem of its free
+    cells (weight 1 between free in-block neighbours, right-hand side the
+    cell divergence over the block's faces; numpy's lstsq gives the
+    minimum-norm least-squares solution, as the reference's SVD / PCG do), then
+    u_face -= p_b - p_a on the faces between two free cells of the block."""
+    D, H, W = occ.shape
+    u, v, w = u.copy(), v.copy(), w.copy()
+    for bk in range(D // s):
+        for bj in range(H // s):
+            for bi in range(W // s):
+                cells = [(i, j, k) for k in range(bk * s, bk * s + s) for j in range(bj * s, bj * s + s)
+                         for i in range(bi * s, bi * s + s) if not occ[k, j, i]]
+                if not cells:
+                    continue
+                ix = {c: n for n, c in enumerate(cells)}
+                L = np.zeros((len(cells), len(cells)))
+                b = np.zeros(len(cells))
+                inb = lambda i, j, k: bi * s <= i < bi * s + s and bj * s <= j < bj * s + s and bk * s <= k < bk * s + s
+                for (i, j, k), n in ix.items():
+                    b[n] = (u[k, j, i + 1] - u[k, j, i]) + (v[k, j + 1, i] - v[k, j, i]) + (w[k + 1, j, i] - w[k, j, i])
+                    for di, dj, dk in ((-1, 0, 0), (1, 0, 0), (0, -1, 0), (0, 1, 0), (0, 0, -1), (0, 0, 1)):
+                        nb = (i + di, j + dj, k + dk)
+                        if inb(*nb) and nb in ix:
+                            L[n, ix[nb]] += 1.0
+                            L[n, n] -= 1.0
+                # lstsq cuts the zero singular values (pinv without a cutoff
+                # would invert the rounding noise of the singular direction)
+                p = np.linalg.lstsq(L, b, rcond=None)[0]
+                for (i, j, k), n in ix.items():
+                    if (i - 1, j, k) in ix and inb(i - 1, j, k):
+                        u[k, j, i] -= p[n] - p[ix[(i - 1, j, k)]]
+                    if (i, j - 1, k) in ix and inb(i, j - 1, k):
+                        v[k, j, i] -= p[n] - p[ix[(i, j - 1, k)]]
+                    if (i, j, k - 1) in ix and inb(i, j, k - 1):
+                        w[k, j, i] -= p[n] - p[ix[(i, j, k - 1)]]
+    return u, v, w
+
+
+@pytest.mark.parametrize("s", [2, 4])
+def test_block_projection_matches_least_squares_restatement(oracle64, s):
+    """With no coarse iterations (K = 0) the coarse correction is exactly zero
+    and the projection is the block step alone: dense-matrix blocks and
+    obstacle blocks against the numpy least-squares restatement."""
+    W, H, D = 8, 8, 8
+    occ = wl.walls_open_top(W, H, D)
+    wl.add_box(occ, 3, 4, 2, 5, 3, 3)
+    p = wl.smoke_params(W, 0, omega=1.5, solver=capi.SOLVER_COARSE_OPEN)
+    p.sub_size = s
+    u, v, w = wl.initial_velocity(occ, 4, amp=1.0)
+    st = {"u": np.asarray(u, np.float64).copy(), "v": np.asarray(v, np.float64).copy(),
+          "w": np.asarray(w, np.float64).copy()}
+    assert oracle64.project_coarse(W, H, D, st, occ, p) == 0
+    eu, ev, ew = _py_block_projection(np.asarray(u, np.float64), np.asarray(v, np.float64),
+                                      np.asarray(w, np.float64), occ, s)
+    scale = max(np.abs(eu).max(), np.abs(ev).max(), np.abs(ew).max())
+    for name, got, exp in (("u", st["u"], eu), ("v", st["v"], ev), ("w", st["w"], ew)):
+        # the dense blocks use the block matrix rounded to float, as the reference stores it
+        np.testing.assert_allclose(got, exp, rtol=0, atol=2e-6 * scale, err_msg=name)
+    assert not np.allclose(st["u"], u)
