@@ -212,3 +212,137 @@ def test_block_projection_matches_least_squares_restatement(oracle64, s):
         # the dense blocks use the block matrix rounded to float, as the reference stores it
         np.testing.assert_allclose(got, exp, rtol=0, atol=2e-6 * scale, err_msg=name)
     assert not np.allclose(st["u"], u)
+
+
+def _py_coarse_correction(u, v, w, occ, s, K, omega):
+    """The coarse stages of ZQ_TotalProjection3D restated with numpy loops:
+    face un-occupancy ratios and coarse occupancy (ZQ_InitCoarseGrid3D,
+    Utils3D:1666-1888), fine faces averaged onto coarse faces
+    (ZQ_MapFine2Coarse3D, :2170-2258), K red-black SOR iterations of the
+    face-ratio system (domain faces weight 1, p = 0 outside), the correction
+    (u - g) - u on faces with ratio > 0, added to the fine faces on coarse
+    faces whose cells are free (ZQ_MapCoarse2Fine3D, :3172-3296)."""
+    D, H, W = occ.shape
+    cD, cH, cW = D // s, H // s, W // s
+    ru, rv, rw = np.zeros((cD, cH, cW + 1)), np.zeros((cD, cH + 1, cW)), np.zeros((cD + 1, cH, cW))
+    for k in range(cD):
+        for j in range(cH):
+            for i in range(cW + 1):
+                n = 0
+                for sk in range(s):
+                    for sj in range(s):
+                        z, y, x = k * s + sk, j * s + sj, i * s
+                        n += bool(occ[z, y, 0]) if i == 0 else bool(occ[z, y, W - 1]) if i == cW else \
+                            bool(occ[z, y, x] or occ[z, y, x - 1])
+                ru[k, j, i] = 1.0 - n / (s * s)
+    for k in range(cD):
+        for j in range(cH + 1):
+            for i in range(cW):
+                n = 0
+                for sk in range(s):
+                    for si in range(s):
+                        z, y, x = k * s + sk, j * s, i * s + si
+                        n += bool(occ[z, 0, x]) if j == 0 else bool(occ[z, H - 1, x]) if j == cH else \
+                            bool(occ[z, y, x] or occ[z, y - 1, x])
+                rv[k, j, i] = 1.0 - n / (s * s)
+    for k in range(cD + 1):
+        for j in range(cH):
+            for i in range(cW):
+                n = 0
+                for sj in range(s):
+                    for si in range(s):
+                        z, y, x = k * s, j * s + sj, i * s + si
+                        n += bool(occ[0, y, x]) if k == 0 else bool(occ[D - 1, y, x]) if k == cD else \
+                            bool(occ[z, y, x] or occ[z - 1, y, x])
+                rw[k, j, i] = 1.0 - n / (s * s)
+    cocc = ((ru[:, :, :-1] == 0) & (ru[:, :, 1:] == 0) & (rv[:, :-1, :] == 0) & (rv[:, 1:, :] == 0) &
+            (rw[:-1] == 0) & (rw[1:] == 0))
+    cu = np.array([[[sum(u[k * s + sk, j * s + sj, i * s] for sk in range(s) for sj in range(s)) / (s * s)
+                     for i in range(cW + 1)] for j in range(cH)] for k in range(cD)])
+    cv = np.array([[[sum(v[k * s + sk, j * s, i * s + si] for sk in range(s) for si in range(s)) / (s * s)
+                     for i in range(cW)] for j in range(cH + 1)] for k in range(cD)])
+    cw = np.array([[[sum(w[k * s, j * s + sj, i * s + si] for sj in range(s) for si in range(s)) / (s * s)
+                     for i in range(cW)] for j in range(cH)] for k in range(cD + 1)])
+    nb = [((-1, 0, 0), lambda i, j, k: ru[k, j, i]), ((1, 0, 0), lambda i, j, k: ru[k, j, i + 1]),
+          ((0, -1, 0), lambda i, j, k: rv[k, j, i]), ((0, 1, 0), lambda i, j, k: rv[k, j + 1, i]),
+          ((0, 0, -1), lambda i, j, k: rw[k, j, i]), ((0, 0, 1), lambda i, j, k: rw[k + 1, j, i])]
+    inside = lambda i, j, k: 0 <= i < cW and 0 <= j < cH and 0 <= k < cD
+    div = np.zeros((cD, cH, cW))
+    diag = np.zeros((cD, cH, cW))
+    for k in range(cD):
+        for j in range(cH):
+            for i in range(cW):
+                if cocc[k, j, i]:
+                    continue
+                div[k, j, i] = (cu[k, j, i + 1] - cu[k, j, i]) + (cv[k, j + 1, i] - cv[k, j, i]) + \
+                    (cw[k + 1, j, i] - cw[k, j, i])
+                d = 0.0
+                for (di, dj, dk), r in nb:
+                    a, b, c = i + di, j + dj, k + dk
+                    if not inside(a, b, c):
+                        d += 1.0            # a domain face: weight 1
+                    elif not cocc[c, b, a]:
+                        d += r(i, j, k)
+                diag[k, j, i] = d
+    p = np.zeros((cD, cH, cW))
+    for _ in range(K):
+        for colour in (0, 1):
+            for k in range(cD):
+                for j in range(cH):
+                    for i in range(cW):
+                        if (i + j + k) % 2 != colour or cocc[k, j, i] or diag[k, j, i] == 0:
+                            continue
+                        sm = 0.0
+                        for (di, dj, dk), r in nb:
+                            a, b, c = i + di, j + dj, k + dk
+                            if inside(a, b, c) and not cocc[c, b, a]:
+                                sm += r(i, j, k) * p[c, b, a]
+                        p[k, j, i] = omega / diag[k, j, i] * (sm - div[k, j, i]) + (1 - omega) * p[k, j, i]
+    pp = np.pad(p, 1)   # p = 0 outside the domain
+    du = np.where(ru > 0, -(pp[1:-1, 1:-1, 1:] - pp[1:-1, 1:-1, :-1]), 0.0)
+    dv = np.where(rv > 0, -(pp[1:-1, 1:, 1:-1] - pp[1:-1, :-1, 1:-1]), 0.0)
+    dw = np.where(rw > 0, -(pp[1:, 1:-1, 1:-1] - pp[:-1, 1:-1, 1:-1]), 0.0)
+    u, v, w = u.copy(), v.copy(), w.copy()
+    free = occ == 0
+    for z in range(D):
+        for y in range(H):
+            for x in range(0, W + 1, s):
+                ok = free[z, y, 0] if x == 0 else free[z, y, W - 1] if x == W else free[z, y, x] and free[z, y, x - 1]
+                if ok:
+                    u[z, y, x] += du[z // s, y // s, x // s]
+    for z in range(D):
+        for y in range(0, H + 1, s):
+            for x in range(W):
+                ok = free[z, 0, x] if y == 0 else free[z, H - 1, x] if y == H else free[z, y, x] and free[z, y - 1, x]
+                if ok:
+                    v[z, y, x] += dv[z // s, y // s, x // s]
+    for z in range(0, D + 1, s):
+        for y in range(H):
+            for x in range(W):
+                ok = free[0, y, x] if z == 0 else free[D - 1, y, x] if z == D else free[z, y, x] and free[z - 1, y, x]
+                if ok:
+                    w[z, y, x] += dw[z // s, y // s, x // s]
+    return u, v, w
+
+
+@pytest.mark.parametrize("s", [2, 4])
+def test_coarse_projection_matches_numpy_restatement(oracle64, s):
+    """The whole coarse projection with K > 0: the numpy coarse stages, then the
+    numpy least-squares block step, against the oracle (FP64; the oracle's
+    fused multiply-adds and float block matrix give the tolerance)."""
+    W, H, D = 8, 8, 8
+    occ = wl.walls_open_top(W, H, D)
+    wl.add_box(occ, 3, 4, 2, 5, 3, 3)
+    p = wl.smoke_params(W, 7, omega=1.5, solver=capi.SOLVER_COARSE_OPEN)
+    p.sub_size = s
+    u, v, w = (np.asarray(a, np.float64) for a in wl.initial_velocity(occ, 4, amp=1.0))
+    st = {"u": u.copy(), "v": v.copy(), "w": w.copy()}
+    assert oracle64.project_coarse(W, H, D, st, occ, p) == 0
+    cu, cv, cw = _py_coarse_correction(u, v, w, occ, s, 7, float(np.float32(p.omega)))
+    eu, ev, ew = _py_block_projection(cu, cv, cw, occ, s)
+    scale = max(np.abs(eu).max(), np.abs(ev).max(), np.abs(ew).max())
+    for name, got, exp in (("u", st["u"], eu), ("v", st["v"], ev), ("w", st["w"], ew)):
+        np.testing.assert_allclose(got, exp, rtol=0, atol=2e-6 * scale, err_msg=name)
+    # the coarse stage did something: without it the result differs
+    bu, _, _ = _py_block_projection(u, v, w, occ, s)
+    assert np.abs(bu - eu).max() > 1e-3
