@@ -648,3 +648,56 @@ def test_regular_velocity_scalar_advection_matches_pure_python_restatement(oracl
                 assert st["T"][k, j, i] == tri(T0, g), (i, j, k)
                 assert st["rho"][k, j, i] == tri(R0, g), (i, j, k)
     assert not np.array_equal(st["T"], T0)
+
+
+def test_regular_in_mac_out_velocity_advection_matches_pure_python_restatement(oracle64):
+    """cu_Advect_Velocity_inRegular_outMAC (Adv3D:1337-1380 with the kernels at
+    :116-230): every face backtraced from its centre through the cell-centred
+    velocity, the face's own component of that velocity sampled at the last
+    accepted point, then the open write-back."""
+    w_ = wl.small_case(5, 4, 4, vel_amp=0.4, substeps=2)
+    st = {k: np.asarray(v, np.float64).copy() for k, v in w_.state().items()}
+    u, v, w = (st[k].copy() for k in ("u", "v", "w"))
+    assert oracle64.advect_velocity(w_.W, w_.H, w_.D, st, w_.occ, w_.params, capi.ADV_VEL_INREG_OUTMAC) == 0
+    D, H, W = w_.occ.shape
+    dt = float(w_.params.step_time) / w_.params.substeps
+    h = float(np.float32(w_.params.voxel_size))
+    n = w_.params.substeps
+    cx = 0.5 * (u[:, :, :-1] + u[:, :, 1:])
+    cy = 0.5 * (v[:, :-1, :] + v[:, 1:, :])
+    cz = 0.5 * (w[:-1, :, :] + w[1:, :, :])
+    _, tri = _py_backtrace_mac(u, v, w, w_.occ, (0.5, 0.5, 0.5), 0, dt, h)
+    cellv = lambda x, y, z: tuple(tri(f, (x - 0.5, y - 0.5, z - 0.5)) for f in (cx, cy, cz))
+
+    def trace(x, y, z):
+        vx, vy, vz = cellv(x, y, z)
+        last = (x, y, z)
+        for _ in range(n):
+            if not (0 <= x <= W and 0 <= y <= H and 0 <= z <= D):
+                break
+            if w_.occ[min(max(int(math.floor(z)), 0), D - 1), min(max(int(math.floor(y)), 0), H - 1),
+                      min(max(int(math.floor(x)), 0), W - 1)]:
+                break
+            last = (x, y, z)
+            x, y, z = x - (vx * dt) / h, y - (vy * dt) / h, z - (vz * dt) / h
+            vx, vy, vz = cellv(x, y, z)
+        return cellv(*last)
+
+    adv = {"u": np.empty_like(u), "v": np.empty_like(v), "w": np.empty_like(w)}
+    for k in range(D):
+        for j in range(H):
+            for i in range(W + 1):
+                adv["u"][k, j, i] = trace(i, j + 0.5, k + 0.5)[0]
+    for k in range(D):
+        for j in range(H + 1):
+            for i in range(W):
+                adv["v"][k, j, i] = trace(i + 0.5, j, k + 0.5)[1]
+    for k in range(D + 1):
+        for j in range(H):
+            for i in range(W):
+                adv["w"][k, j, i] = trace(i + 0.5, j + 0.5, k)[2]
+    ref = {"u": u.copy(), "v": v.copy(), "w": w.copy()}
+    _py_apply_open(adv, w_.occ, ref)
+    for k in ("u", "v", "w"):
+        np.testing.assert_array_equal(st[k], ref[k], err_msg=k)
+        assert not np.array_equal(st[k], {"u": u, "v": v, "w": w}[k]), k
