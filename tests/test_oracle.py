@@ -701,3 +701,25 @@ def test_regular_in_mac_out_velocity_advection_matches_pure_python_restatement(o
     for k in ("u", "v", "w"):
         np.testing.assert_array_equal(st[k], ref[k], err_msg=k)
         assert not np.array_equal(st[k], {"u": u, "v": v, "w": w}[k]), k
+
+
+def test_mac_velocity_advection_closed_writeback_matches_restatement(oracle64):
+    """cu_Advect_Velocity_inMAC_outMAC with the closed write-back
+    (Apply_Advect_Velocity_Result_Closed_*, Adv3D:577-650): only interior faces
+    between two free cells take the advected value; domain faces keep theirs."""
+    w_ = wl.small_case(5, 4, 4, vel_amp=0.4, substeps=2)
+    st = {k: np.asarray(v, np.float64).copy() for k, v in w_.state().items()}
+    vel0 = {k: st[k].copy() for k in ("u", "v", "w")}
+    assert oracle64.advect_velocity(w_.W, w_.H, w_.D, st, w_.occ, w_.params, capi.ADV_VEL_INMAC_OUTMAC,
+                                    is_open=False) == 0
+    D, H, W = w_.occ.shape
+    dt = float(w_.params.step_time) / w_.params.substeps
+    h = float(np.float32(w_.params.voxel_size))
+    adv = _py_advect_faces(vel0, (vel0["u"], vel0["v"], vel0["w"]), w_.occ, w_.params.substeps, dt, h)
+    free = w_.occ == 0
+    ref = {k: vel0[k].copy() for k in ("u", "v", "w")}
+    ref["u"][:, :, 1:W] = np.where(free[:, :, 1:] & free[:, :, :-1], adv["u"][:, :, 1:W], ref["u"][:, :, 1:W])
+    ref["v"][:, 1:H, :] = np.where(free[:, 1:, :] & free[:, :-1, :], adv["v"][:, 1:H, :], ref["v"][:, 1:H, :])
+    ref["w"][1:D] = np.where(free[1:] & free[:-1], adv["w"][1:D], ref["w"][1:D])
+    for k in ("u", "v", "w"):
+        np.testing.assert_array_equal(st[k], ref[k], err_msg=k)
