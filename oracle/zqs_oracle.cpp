@@ -11,7 +11,10 @@
  * golden outputs, cannot be built here (Windows/VS2015, legacy texture
  * references, missing ZQlib/ZQlibCuda), and its SOR solver lives in the
  * un-vendored ZQlibCuda library; see the per-function citations for the
- * in-tree evidence each rule is restated from.
+ * in-tree evidence each rule is restated from.  Independent plain-Python /
+ * numpy restatements of the reference loops check it in the tests (SOR, the
+ * advection modes and BFECC, the write-backs, forces, object stamping, the
+ * coarse stages and block step, the viewer's shader).
  *
  * Arithmetic contract (shared with the CUDA kernels so FP32 results can match
  * bit for bit): no contraction (built with -ffp-contract=off; kernels with
