@@ -87,3 +87,20 @@ def test_enum_values_follow_reference_cuda_header():
 def test_missing_library_fails_loudly(tmp_path):
     with pytest.raises(FileNotFoundError):
         capi.load(tmp_path / "nope.so")
+
+
+def test_added_structs_match_c(tmp_path):
+    """zqs_object, zqs_camera and zqs_sor_variant as compiled C sees them."""
+    gcc = shutil.which("gcc")
+    if not gcc:
+        pytest.skip("gcc missing")
+    src = tmp_path / "sz2.c"
+    src.write_text('#include "zqs_capi.h"\n#include <stdio.h>\n#include <stddef.h>\n'
+                   'int main(void){printf("%zu %zu %zu %zu %zu %zu %zu\\n", sizeof(zqs_object), offsetof(zqs_object, vel),'
+                   ' sizeof(zqs_camera), offsetof(zqs_camera, eye), offsetof(zqs_camera, steps),'
+                   ' offsetof(zqs_camera, density_scale), sizeof(zqs_sor_variant));return 0;}\n')
+    exe = tmp_path / "sz2"
+    subprocess.run([gcc, "-std=c99", "-Wall", "-Werror", f"-I{INC}", str(src), "-o", str(exe)], check=True)
+    vals = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    assert vals == [C.sizeof(capi.Object), capi.Object.vel.offset, C.sizeof(capi.Camera), capi.Camera.eye.offset,
+                    capi.Camera.steps.offset, capi.Camera.density_scale.offset, C.sizeof(capi.SorVariant)]
