@@ -723,3 +723,87 @@ def test_mac_velocity_advection_closed_writeback_matches_restatement(oracle64):
     ref["w"][1:D] = np.where(free[1:] & free[:-1], adv["w"][1:D], ref["w"][1:D])
     for k in ("u", "v", "w"):
         np.testing.assert_array_equal(st[k], ref[k], err_msg=k)
+
+
+def _py_advect_scalar_reg(phi, cx, cy, cz, occ, steps, dt, h, tri):
+    """One pass of Advect_Scalar_Regular_Velocity_Kernel over a cell field with
+    the cell-centred velocity (cx, cy, cz)."""
+    D, H, W = occ.shape
+    cellv = lambda x, y, z: tuple(tri(f, (x - 0.5, y - 0.5, z - 0.5)) for f in (cx, cy, cz))
+    out = np.empty_like(phi)
+    for k in range(D):
+        for j in range(H):
+            for i in range(W):
+                x, y, z = i + 0.5, j + 0.5, k + 0.5
+                vx, vy, vz = cellv(x, y, z)
+                last = (x, y, z)
+                for _ in range(steps):
+                    if not (0 <= x <= W and 0 <= y <= H and 0 <= z <= D):
+                        break
+                    if occ[min(max(int(math.floor(z)), 0), D - 1), min(max(int(math.floor(y)), 0), H - 1),
+                           min(max(int(math.floor(x)), 0), W - 1)]:
+                        break
+                    last = (x, y, z)
+                    x, y, z = x - (vx * dt) / h, y - (vy * dt) / h, z - (vz * dt) / h
+                    vx, vy, vz = cellv(x, y, z)
+                out[k, j, i] = tri(phi, (last[0] - 0.5, last[1] - 0.5, last[2] - 0.5))
+    return out
+
+
+def test_regular_scalar_bfecc_matches_pure_python_restatement(oracle64):
+    """cu_Advect_Scalar_Regular_Velocity_BFECC (Adv3D:1507-1554): forward with
+    the cell-centred velocity, back with it negated
+    (Velocity_Negative_4channels), input = input*1.5 - back*0.5, forward."""
+    w_ = wl.small_case(6, 5, 4, vel_amp=0.4, substeps=2)
+    st = {k: np.asarray(v, np.float64).copy() for k, v in w_.state().items()}
+    T0 = st["T"].copy()
+    u, v, w = st["u"], st["v"], st["w"]
+    assert oracle64.advect_scalar(w_.W, w_.H, w_.D, st, w_.occ, w_.params, capi.ADV_SCA_REG_BFECC) == 0
+    dt = float(w_.params.step_time) / w_.params.substeps
+    h = float(np.float32(w_.params.voxel_size))
+    n = w_.params.substeps
+    cx = 0.5 * (u[:, :, :-1] + u[:, :, 1:])
+    cy = 0.5 * (v[:, :-1, :] + v[:, 1:, :])
+    cz = 0.5 * (w[:-1, :, :] + w[1:, :, :])
+    _, tri = _py_backtrace_mac(u, v, w, w_.occ, (0.5, 0.5, 0.5), 0, dt, h)
+    f1 = _py_advect_scalar_reg(T0, cx, cy, cz, w_.occ, n, dt, h, tri)
+    f2 = _py_advect_scalar_reg(f1, -cx, -cy, -cz, w_.occ, n, dt, h, tri)
+    corrected = T0 * 1.5 - f2 * 0.5
+    expect = _py_advect_scalar_reg(corrected, cx, cy, cz, w_.occ, n, dt, h, tri)
+    np.testing.assert_array_equal(st["T"], expect)
+    assert not np.array_equal(st["T"], T0)
+
+
+def test_regular_velocity_bfecc_matches_pure_python_restatement(oracle64):
+    """cu_Advect_Velocity_inRegular_outRegular_BFECC (Adv3D:1103-1176): on the
+    cell-centred velocity c, c1 = A(c; c), c2 = A(c1; -c), c' = c*1.5 - c2*0.5
+    (Input_Increment_4channels_Kernel), c3 = A(c'; c), back to faces and the
+    open write-back into the untouched MAC fields."""
+    w_ = wl.small_case(5, 4, 4, vel_amp=0.4, substeps=2)
+    st = {k: np.asarray(v, np.float64).copy() for k, v in w_.state().items()}
+    u, v, w = (st[k].copy() for k in ("u", "v", "w"))
+    assert oracle64.advect_velocity(w_.W, w_.H, w_.D, st, w_.occ, w_.params, capi.ADV_VEL_INREG_OUTREG_BFECC) == 0
+    D, H, W = w_.occ.shape
+    dt = float(w_.params.step_time) / w_.params.substeps
+    h = float(np.float32(w_.params.voxel_size))
+    n = w_.params.substeps
+    c = [0.5 * (u[:, :, :-1] + u[:, :, 1:]), 0.5 * (v[:, :-1, :] + v[:, 1:, :]), 0.5 * (w[:-1, :, :] + w[1:, :, :])]
+    _, tri = _py_backtrace_mac(u, v, w, w_.occ, (0.5, 0.5, 0.5), 0, dt, h)
+    adv = lambda fields, vel: [_py_advect_scalar_reg(f, *vel, w_.occ, n, dt, h, tri) for f in fields]
+    c1 = adv(c, c)
+    c2 = adv(c1, [-a for a in c])
+    cc = [a * 1.5 - b * 0.5 for a, b in zip(c, c2)]
+    c3 = adv(cc, c)
+    fu = np.empty_like(u)
+    fu[:, :, 0], fu[:, :, W] = c3[0][:, :, 0], c3[0][:, :, W - 1]
+    fu[:, :, 1:W] = 0.5 * (c3[0][:, :, 1:] + c3[0][:, :, :-1])
+    fv = np.empty_like(v)
+    fv[:, 0, :], fv[:, H, :] = c3[1][:, 0, :], c3[1][:, H - 1, :]
+    fv[:, 1:H, :] = 0.5 * (c3[1][:, 1:, :] + c3[1][:, :-1, :])
+    fw = np.empty_like(w)
+    fw[0], fw[D] = c3[2][0], c3[2][D - 1]
+    fw[1:D] = 0.5 * (c3[2][1:] + c3[2][:-1])
+    ref = {"u": u.copy(), "v": v.copy(), "w": w.copy()}
+    _py_apply_open({"u": fu, "v": fv, "w": fw}, w_.occ, ref)
+    for k in ("u", "v", "w"):
+        np.testing.assert_array_equal(st[k], ref[k], err_msg=k)
