@@ -807,3 +807,63 @@ def test_regular_velocity_bfecc_matches_pure_python_restatement(oracle64):
     _py_apply_open({"u": fu, "v": fv, "w": fw}, w_.occ, ref)
     for k in ("u", "v", "w"):
         np.testing.assert_array_equal(st[k], ref[k], err_msg=k)
+
+
+def test_regular_in_mac_out_velocity_bfecc_matches_pure_python_restatement(oracle64):
+    """cu_Advect_Velocity_inRegular_outMAC_BFECC (Adv3D:1389-1466): faces
+    out1 = A(c; c) traced through the cell velocity c, out2 = A(reg(out1); -c),
+    then the input c*1.5 - reg(out2)*0.5 (the velocity texture is copied
+    before Input_Increment_4channels, so the trace stays on c), out3 =
+    A(that; c) and the open write-back into the untouched MAC fields."""
+    w_ = wl.small_case(5, 4, 4, vel_amp=0.4, substeps=2)
+    st = {k: np.asarray(v, np.float64).copy() for k, v in w_.state().items()}
+    u, v, w = (st[k].copy() for k in ("u", "v", "w"))
+    assert oracle64.advect_velocity(w_.W, w_.H, w_.D, st, w_.occ, w_.params, capi.ADV_VEL_INREG_OUTMAC_BFECC) == 0
+    D, H, W = w_.occ.shape
+    dt = float(w_.params.step_time) / w_.params.substeps
+    h = float(np.float32(w_.params.voxel_size))
+    n = w_.params.substeps
+    reg = lambda fu, fv, fw: [0.5 * (fu[:, :, :-1] + fu[:, :, 1:]), 0.5 * (fv[:, :-1, :] + fv[:, 1:, :]),
+                              0.5 * (fw[:-1, :, :] + fw[1:, :, :])]
+    c = reg(u, v, w)
+    _, tri = _py_backtrace_mac(u, v, w, w_.occ, (0.5, 0.5, 0.5), 0, dt, h)
+    at = lambda fields, x, y, z: tuple(tri(f, (x - 0.5, y - 0.5, z - 0.5)) for f in fields)
+
+    def trace(vel, inp, x, y, z, comp):
+        vx, vy, vz = at(vel, x, y, z)
+        last = (x, y, z)
+        for _ in range(n):
+            if not (0 <= x <= W and 0 <= y <= H and 0 <= z <= D):
+                break
+            if w_.occ[min(max(int(math.floor(z)), 0), D - 1), min(max(int(math.floor(y)), 0), H - 1),
+                      min(max(int(math.floor(x)), 0), W - 1)]:
+                break
+            last = (x, y, z)
+            x, y, z = x - (vx * dt) / h, y - (vy * dt) / h, z - (vz * dt) / h
+            vx, vy, vz = at(vel, x, y, z)
+        return tri(inp[comp], (last[0] - 0.5, last[1] - 0.5, last[2] - 0.5))
+
+    def faces(vel, inp):
+        fu, fv, fw = np.empty_like(u), np.empty_like(v), np.empty_like(w)
+        for k in range(D):
+            for j in range(H):
+                for i in range(W + 1):
+                    fu[k, j, i] = trace(vel, inp, i, j + 0.5, k + 0.5, 0)
+        for k in range(D):
+            for j in range(H + 1):
+                for i in range(W):
+                    fv[k, j, i] = trace(vel, inp, i + 0.5, j, k + 0.5, 1)
+        for k in range(D + 1):
+            for j in range(H):
+                for i in range(W):
+                    fw[k, j, i] = trace(vel, inp, i + 0.5, j + 0.5, k, 2)
+        return fu, fv, fw
+
+    out1 = faces(c, c)
+    out2 = faces([-a for a in c], reg(*out1))
+    cc = [a * 1.5 - b * 0.5 for a, b in zip(c, reg(*out2))]
+    out3 = faces(c, cc)
+    ref = {"u": u.copy(), "v": v.copy(), "w": w.copy()}
+    _py_apply_open(dict(zip(("u", "v", "w"), out3)), w_.occ, ref)
+    for k in ("u", "v", "w"):
+        np.testing.assert_array_equal(st[k], ref[k], err_msg=k)
