@@ -1,7 +1,7 @@
 """ctypes binding of the CPU oracle (oracle/_build/libzqs_oracle.so).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
-CPU-baseline / reference arm of bench.py, always as the checker.  The oracle
+CPU-baseline / reference arm of bench.py, always to check results.  The oracle
 restates the reference's per-timestep path (see zqs_oracle.cpp); parity of the
 reference itself is unpinned (no golden outputs exist in the reference).
 """

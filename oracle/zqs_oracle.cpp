@@ -3,7 +3,7 @@
  *
  * This file restates, in plain C++ templated on the arithmetic type R
  * (float or double), the per-timestep path of ZQ_SmokeSimulation3D as the
- * reference computes it.  It is the checker for the CUDA library: only the
+ * reference computes it.  It checks the results of the CUDA library: only the
  * tests, the smoke check and bench.py's CPU-baseline / reference arm may load
  * it.  Nothing in the product links or calls it.
  *
@@ -202,7 +202,7 @@ void apply_advect_result(const Dims& d, const uint8_t* occ, const R* au, const R
  *  3. N = grad|w| (0.5*central inside, one-sided on the domain boundary),
  *     normalised when its length is nonzero (:64-111)
  *  4. f = (eps*h)*(N x w);  f_y += beta*(T - Tamb);  f_y -= alpha*rho (:161-184;
- *     the alpha term is an addition of this build, alpha = 0 reproduces it)
+ *     the alpha term is not in the reference, alpha = 0 reproduces it)
  *  5. faces: u += (dt*0.5)*(f_R + f_L) when both cells are free, u += dt*f_in on
  *     domain faces whose inner cell is free (:211-385; the w kernel at :360-385
  *     reads occupy[-1 plane] for z=0, its per-slice twin :387-420 is followed). */
@@ -677,7 +677,7 @@ int advect_scalar(const Dims& d, const R* u, const R* v, const R* w, const uint8
 
 /* ZQ_ReinjectTemperatureDensity3D (Utils3D:3842-3882): cells inside a source
  * get density and temperature overwritten; sources in order, the last wins.
- * Box test |i+.5-cx| <= hx (per axis); sphere test (new in this build)
+ * Box test |i+.5-cx| <= hx (per axis); sphere test (not in the reference)
  * ((dx*dx + dy*dy) + dz*dz) <= r*r with dx = (i+.5) - cx. */
 template <class R>
 void reinject(const Dims& d, R* T, R* rho, const zqs_params& P) {
