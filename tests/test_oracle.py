@@ -867,3 +867,38 @@ def test_regular_in_mac_out_velocity_bfecc_matches_pure_python_restatement(oracl
     _py_apply_open(dict(zip(("u", "v", "w"), out3)), w_.occ, ref)
     for k in ("u", "v", "w"):
         np.testing.assert_array_equal(st[k], ref[k], err_msg=k)
+
+
+def test_attenuation_matches_pure_python_restatement(oracle64):
+    """Atten_{u,v,w}_Kernel and Atten_temperature_density_Kernel
+    (ZQ_CUDA_Attenuation3D.cu:8-116): a face is scaled by the velocity factor
+    when both of its cells are free (a domain face: its one inner cell), and
+    every cell's temperature and density by their factors, occupied or not."""
+    w_ = wl.small_case(5, 4, 4, vel_amp=0.4, substeps=2)
+    p = w_.params
+    p.vel_atten, p.temp_atten, p.dens_atten = 0.75, 0.5, 0.25
+    st = {k: np.asarray(v, np.float64).copy() for k, v in w_.state().items()}
+    ref = {k: a.copy() for k, a in st.items()}
+    oracle64.attenuate(w_.W, w_.H, w_.D, st, w_.occ, p)
+    occ = w_.occ.astype(bool)
+    D, H, W = occ.shape
+    for k in range(D):
+        for j in range(H):
+            for i in range(W + 1):
+                if not (i > 0 and occ[k, j, i - 1]) and not (i < W and occ[k, j, i]):
+                    ref["u"][k, j, i] *= 0.75
+    for k in range(D):
+        for j in range(H + 1):
+            for i in range(W):
+                if not (j > 0 and occ[k, j - 1, i]) and not (j < H and occ[k, j, i]):
+                    ref["v"][k, j, i] *= 0.75
+    for k in range(D + 1):
+        for j in range(H):
+            for i in range(W):
+                if not (k > 0 and occ[k - 1, j, i]) and not (k < D and occ[k, j, i]):
+                    ref["w"][k, j, i] *= 0.75
+    ref["T"] *= 0.5
+    ref["rho"] *= 0.25
+    assert occ.any() and not occ.all()
+    for k in ref:
+        np.testing.assert_array_equal(st[k], ref[k], err_msg=k)
