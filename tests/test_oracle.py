@@ -902,3 +902,36 @@ def test_attenuation_matches_pure_python_restatement(oracle64):
     assert occ.any() and not occ.all()
     for k in ref:
         np.testing.assert_array_equal(st[k], ref[k], err_msg=k)
+
+
+@pytest.mark.parametrize("vmode,smode", [(capi.ADV_VEL_INMAC_OUTMAC, capi.ADV_SCA_MAC),
+                                         (capi.ADV_VEL_INREG_OUTREG_BFECC, capi.ADV_SCA_REG_BFECC)])
+def test_step_is_the_reference_stage_order(oracle64, vmode, smode):
+    """ZQ_SmokeSimulation3D::UpdateOneFrame (ZQ_SmokeSimulation3D.cpp:156-243):
+    force, attenuation, velocity advection, projection, scalar advection,
+    reinjection.  The oracle's step must equal its stages run in that order."""
+    w_ = wl.small_case(6, 5, 4, vel_amp=0.4, substeps=2)
+    p = w_.params
+    p.vel_atten, p.temp_atten, p.dens_atten = 0.9, 0.8, 0.7
+    p.adv_vel_mode, p.adv_sca_mode = vmode, smode
+    st = {k: np.asarray(v, np.float64).copy() for k, v in w_.state().items()}
+    ref = {k: a.copy() for k, a in st.items()}
+    rc, _ = oracle64.step(w_.W, w_.H, w_.D, st, w_.occ, p, 1)
+    assert rc == 0
+    oracle64.add_force(w_.W, w_.H, w_.D, ref, w_.occ, p)
+    oracle64.attenuate(w_.W, w_.H, w_.D, ref, w_.occ, p)
+    assert oracle64.advect_velocity(w_.W, w_.H, w_.D, ref, w_.occ, p, vmode) == 0
+    oracle64.project(w_.W, w_.H, w_.D, ref, w_.occ, p)
+    assert oracle64.advect_scalar(w_.W, w_.H, w_.D, ref, w_.occ, p, smode) == 0
+    oracle64.reinject(w_.W, w_.H, w_.D, ref, p)
+    for k in ("u", "v", "w", "T", "rho"):
+        np.testing.assert_array_equal(st[k], ref[k], err_msg=k)
+    # a different order gives a different state (the pin is not vacuous)
+    alt = {k: np.asarray(v, np.float64).copy() for k, v in w_.state().items()}
+    oracle64.attenuate(w_.W, w_.H, w_.D, alt, w_.occ, p)
+    oracle64.add_force(w_.W, w_.H, w_.D, alt, w_.occ, p)
+    oracle64.advect_velocity(w_.W, w_.H, w_.D, alt, w_.occ, p, vmode)
+    oracle64.project(w_.W, w_.H, w_.D, alt, w_.occ, p)
+    oracle64.advect_scalar(w_.W, w_.H, w_.D, alt, w_.occ, p, smode)
+    oracle64.reinject(w_.W, w_.H, w_.D, alt, p)
+    assert not np.array_equal(alt["v"], st["v"])
