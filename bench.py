@@ -183,7 +183,10 @@ def run_reference(args):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * wall / max(1, args.steps),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": args.workload, "sample": args.cpu_sample},
+            "config": {"workload": args.workload, "grid": [base.W, base.H, base.D],
+                       "sor_iters": int(base.params.sor_iters), "omega": round(float(base.params.omega), 6),
+                       "substeps": int(base.params.substeps), "advection": "inMAC_outMAC + MAC scalar",
+                       "parallelism": "single", "sample": args.cpu_sample},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
