@@ -337,3 +337,29 @@ def test_render_sequence_matches_oracle(driver, tmp_path, oracle32):
     assert r.returncode == 0, r.stderr
     ref = oracle32.render(np.ascontiguousarray(raw.transpose(2, 1, 0)), capi.default_camera(24, 24, N, N, N))
     assert (out / "render0.ppm").read_bytes() == ppm_of(ref)
+
+
+@pytest.mark.parametrize("name,walls_except_top,expect", [
+    ("TOTAL_OPEN_POISSON_SOR", "false", capi.SOLVER_OPEN),
+    ("TOTAL_CLOSED_POISSON_SOR", "false", capi.SOLVER_CLOSED),
+    ("TOTAL_CLOSED_POISSON_SOR", "true", capi.SOLVER_OPEN),
+    ("CLOSED_OCTREE_POISSON_SOR", "false", capi.SOLVER_CLOSED),
+    ("OPEN_OCTREE_POISSON", "false", capi.SOLVER_OPEN),
+    ("COARSE_OPEN_POISSON_SOR", "false", capi.SOLVER_COARSE_OPEN),
+    ("COARSE_CLOSED_POISSON_SOR", "false", capi.SOLVER_COARSE_OPEN),
+    ("COARSE_CLOSED_FLUX_SOR", "false", capi.SOLVER_CLOSED),
+    ("NOT_A_SOLVER", "false", capi.SOLVER_OPEN),
+])
+def test_global_solver_names_map_to_runtime_solver(driver, tmp_path, name, walls_except_top, expect):
+    """globalGridSolver names (ZQ_SmokeSimulationPara3D's parser): both coarse
+    Poisson settings run the open coarse solver, as ZQ_TotalProjection3D does
+    (Utils3D:3731-3745); every other setting the fine-grid SOR of its open or
+    closed kind (open with wallsExceptTop); an unknown name falls back to
+    OPEN_FLUX, an open solver."""
+    cfg = CONFIG.replace("wallsExceptTop true", "wallsExceptTop " + walls_except_top) \
+                .replace("globalGridSolver TOTAL_CLOSED_POISSON_SOR", "globalGridSolver " + name)
+    out = run_driver(driver, "parse", cfg, tmp_path / "s")
+    p, occ, _ = load_setup(out, 24, 20, 16)
+    assert p.solver == expect
+    if expect == capi.SOLVER_CLOSED:
+        np.testing.assert_array_equal(occ, wl.add_box(wl.walls_closed(24, 20, 16), 8, 10, 9, 11, 5, 8))
