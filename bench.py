@@ -44,7 +44,8 @@ def parse():
     ap.add_argument("--sor-depth", type=int, default=0, help="SOR iterations per fused pass (0 = default)")
     ap.add_argument("--sor-variant", type=int, default=-1, help="fused SOR kernel variant (-1 = default)")
     ap.add_argument("--zchunk", type=int, default=0, help="z planes per SOR CTA (0 = automatic)")
-    ap.add_argument("--cpu-sample", default="plain128", help="grid of the bounded CPU sample")
+    ap.add_argument("--cpu-sample", default="",
+                    help="workload of the CPU sample ('' = the bench workload itself, one full step per sample)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--batch", default="batch64", help="mixed-size batch measured beside the plain step ('' or none = skip)")
@@ -57,6 +58,9 @@ def parse():
     ap.add_argument("--coarse", default="coarse256",
                     help="coarse-grid projection configuration measured beside the plain step ('' or none = skip)")
     ap.add_argument("--coarse-steps", type=int, default=5)
+    ap.add_argument("--large", default="plain512",
+                    help="single-grid configuration measured beside the headline ('' or none = skip)")
+    ap.add_argument("--large-steps", type=int, default=3)
     ap.add_argument("--render", default="256:1024x768x300",
                     help="headless ray march N:WxHxSTEPS of an N^3 density in the viewer's default view "
                          "('' or none = skip)")
@@ -88,12 +92,17 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic(name: str):
-    """DRAM bytes per launch of the SOR kernel from the committed ncu summary."""
+def profile_traffic(name: str, variant: int):
+    """DRAM bytes per launch of the SOR kernel from the committed ncu summary,
+    when the summary is of the same variant."""
     f = ROOT / "profiles" / f"{name}.md"
     if not f.exists():
         return None
-    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", f.read_text())
+    text = f.read_text()
+    mv = re.search(r"sor_variant:\s*(-?[0-9]+)", text)
+    if not mv or int(mv.group(1)) != variant:
+        return None
+    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", text)
     return float(m.group(1)) if m else None
 
 
@@ -146,48 +155,79 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(rows)}
 
 
-def cpu_sample_time(args, base_wl, steps: int = 1):
-    """Time `steps` steps of the FP32 oracle on the bounded CPU sample grid."""
-    import numpy as np
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else the platform)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        for line in Path("/proc/cpuinfo").read_text().splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
 
-    from oracle.binding import Oracle, num_threads
-    from zq_smokesimulation_gb300 import workloads as wl
-    w = wl.make(args.cpu_sample, K=base_wl.params.sor_iters, substeps=base_wl.params.substeps)
-    o = Oracle(np.float32)
-    st = o.state(w)
-    t0 = time.perf_counter()
-    rc, _ = o.step(w.W, w.H, w.D, st, w.occ, w.params, steps)
-    dt = time.perf_counter() - t0
-    if rc != 0:
-        raise RuntimeError(f"oracle step failed: {rc}")
-    return w.cells * steps / dt / 1e9, num_threads(), \
-        f"{steps} full step(s) of the same configuration at {w.W}^3 (K={w.params.sor_iters}), FP32 oracle"
+
+class CpuRun:
+    """The FP32 oracle (the CPU restatement of the reference's step) stepping
+    the bench's own configuration on all host threads.  The state persists
+    across samples, as the GPU grid's does; each sample is one full step."""
+
+    def __init__(self, args, workload: str):
+        import numpy as np
+
+        from oracle.binding import Oracle, num_threads
+        from zq_smokesimulation_gb300 import workloads as wl
+        self.w = wl.make(args.cpu_sample or workload)
+        self.o = Oracle(np.float32)
+        self.st = self.o.state(self.w)
+        self.cores = num_threads()
+
+    def step_seconds(self) -> float:
+        w = self.w
+        t0 = time.perf_counter()
+        rc, _ = self.o.step(w.W, w.H, w.D, self.st, w.occ, w.params, 1)
+        dt = time.perf_counter() - t0
+        if rc != 0:
+            raise RuntimeError(f"oracle step failed: {rc}")
+        return dt
+
+    def describe(self, steps: int) -> dict:
+        w = self.w
+        return {"cores": self.cores, "cpu_model": cpu_model(), "kind": "port", "grid": [w.W, w.H, w.D],
+                "sample": f"{steps} full step(s) of {w.name} ({w.W}x{w.H}x{w.D}, K={w.params.sor_iters}), "
+                          f"FP32 oracle, state carried across steps"}
 
 
 def run_reference(args):
-    """Reference arm: the CPU path of the step (FP32 oracle port), rank 0 only."""
+    """Reference arm: the CPU path of the step (FP32 oracle port) on the bench's
+    own configuration, rank 0 only; one full step per timed step."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    from zq_smokesimulation_gb300 import workloads as wl
-    base = wl.make(args.workload, K=None)
+    run = CpuRun(args, args.workload)
+    w = run.w
     for _ in range(max(0, args.warmup)):
-        cpu_sample_time(args, base, 1)
-    vals = []
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        v, cores, sample = cpu_sample_time(args, base, 1)
-        vals.append(v)
-    wall = time.perf_counter() - t0
-    value = statistics.mean(vals)
+        run.step_seconds()
+    secs = [run.step_seconds() for _ in range(max(1, args.steps))]
+    total = sum(secs)
+    value = w.cells * len(secs) / total / 1e9
+    cpu = {"value": value, "unit": UNIT}
+    cpu.update(run.describe(len(secs)))
     line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * wall / max(1, args.steps),
+            "steps": len(secs), "warmup": args.warmup, "ms_per_step": 1000.0 * total / len(secs),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": args.workload, "grid": [base.W, base.H, base.D],
-                       "sor_iters": int(base.params.sor_iters), "omega": round(float(base.params.omega), 6),
-                       "substeps": int(base.params.substeps), "advection": "inMAC_outMAC + MAC scalar",
-                       "parallelism": "single", "sample": args.cpu_sample},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "config": {"workload": w.name, "grid": [w.W, w.H, w.D],
+                       "sor_iters": int(w.params.sor_iters), "omega": round(float(w.params.omega), 6),
+                       "substeps": int(w.params.substeps), "advection": "inMAC_outMAC + MAC scalar",
+                       "parallelism": "single"},
+            "cpu_baseline": cpu,
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -234,6 +274,7 @@ def measure_batch(args, stream, rel_check: bool = True):
     steps = max(1, args.batch_steps)
     ms_b = timed(lambda: batch.step(1, sp), steps)
     launches = batch.launch_count()
+    b_variant, b_us = batch.sor_choice()
     batch.sync(sp)
 
     gs = grids()
@@ -270,6 +311,7 @@ def measure_batch(args, stream, rel_check: bool = True):
             "one_at_a_time": {"value": v_1, "ms_per_step": ms_1 / steps1, "steps": steps1,
                               "gpu_launches_per_step": launches_1},
             "speedup": v_b / v_1, "max_rel_l2_vs_one_at_a_time": worst, "mismatched_values": mism,
+            "sor_variant": b_variant, "sor_tuned_us_per_iter": b_us,
             "step_alg_gbs": step_alg / (ms_b / steps * 1e-3) / 1e9}
 
 
@@ -320,6 +362,44 @@ def measure_coarse(args, stream):
             "projection_ms": ms_proj, "max_abs_div_after_projection": mx,
             "block_product": "tcgen05 TF32, 3xTF32 split (zqs_grid_set_coarse_gemm 1)",
             "projection_ms_fp32_simt_blocks": ms_proj_simt}
+
+
+def measure_large(args, stream):
+    """The large single grid of the same configuration (plain512: 512^3, K=600,
+    four seeded sphere sources): full steps, device-resident, graph-replayed,
+    and the step's algorithmic-byte rate against the HBM peak."""
+    import torch
+
+    from zq_smokesimulation_gb300 import capi
+    from zq_smokesimulation_gb300 import workloads as wl
+
+    w = wl.make(args.large)
+    sp = stream.cuda_stream
+    g = capi.Grid(w.W, w.H, w.D)
+    g.set_params(w.params)
+    g.load_state(w.occ, w.u, w.v, w.w, w.T, w.rho)
+    g.step(2, sp)
+    steps = max(1, args.large_steps)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record(stream)
+    g.step(steps, sp)
+    b.record(stream)
+    b.synchronize()
+    ms = a.elapsed_time(b) / steps
+    g.project(sp)
+    st = g.stats()
+    lay = g.layout()
+    K = int(w.params.sor_iters)
+    peak, peak_kind = load_peaks()
+    step_alg = (STEP_BYTES_FIXED + SOR_BYTES_PER_CELL_ITER * K) * w.cells
+    out = {"workload": args.large, "grid": [w.W, w.H, w.D], "sor_iters": K, "steps": steps, "ms_per_step": ms,
+           "value": w.cells / (ms * 1e-3) / 1e9, "unit": UNIT, "gpu_launches_per_step": g.launch_count(),
+           "step_alg_gbs": step_alg / (ms * 1e-3) / 1e9, "step_frac": step_alg / (ms * 1e-3) / 1e9 / peak,
+           "peak_kind": peak_kind, "max_abs_div_after_projection": st.max_abs_div,
+           "working_set_gb": lay.field_elems * 4 * 21.25 / 1e9}
+    g.close()
+    return out
 
 
 def measure_render(args, stream):
@@ -505,9 +585,9 @@ def run_ours(args):
     launches_per_step = g.launch_count()
 
     # -- dominant kernel (temporally blocked SOR): per-launch duration, live --
-    depth = args.sor_depth if args.sor_depth > 0 else 2
-    if args.sor_variant >= 0:
-        depth = capi.sor_variants()[args.sor_variant].depth
+    sor_v, sor_zc, sor_us = g.sor_choice(sp)   # the variant the steps ran (tuned unless forced)
+    vinfo = capi.sor_variants()[sor_v] if sor_v >= 0 else None
+    depth = vinfo.depth if vinfo is not None else max(1, args.sor_depth)
     passes = math.ceil(2 * K / (2 * depth))
     reps = 3
     p0 = w.params.copy()
@@ -527,11 +607,13 @@ def run_ours(args):
     t_K = time_project(w.params)
     t_0 = time_project(p0)
     g.set_params(w.params)
+    g.project(sp)
+    st_proj = g.stats()
     sor_ms_per_launch = max(1e-9, (t_K - t_0) / passes)
     alg_bytes = SOR_BYTES_PER_CELL_ITER * depth * cells
     peak, peak_kind = load_peaks()
     achieved = alg_bytes / (sor_ms_per_launch * 1e-3) / 1e9
-    traffic = profile_traffic(f"k_sor_{args.workload}") if args.sor_variant < 0 and args.sor_depth in (0, 2) else None
+    traffic = profile_traffic(f"k_sor_{args.workload}", sor_v)
 
     # -- end to end through the C ABI with pinned host buffers --
     e2e = None
@@ -566,6 +648,9 @@ def run_ours(args):
     coarse = None
     if args.coarse not in ("", "none") and world == 1:
         coarse = measure_coarse(args, stream)
+    large = None
+    if args.large not in ("", "none") and world == 1:
+        large = measure_large(args, stream)
     render = None
     if args.render not in ("", "none") and world == 1:
         render = measure_render(args, stream)
@@ -578,8 +663,10 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        v, cores, sample = cpu_sample_time(args, w, 1)
-        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+        run = CpuRun(args, args.workload)
+        secs = run.step_seconds()
+        cpu = {"value": run.w.cells / secs / 1e9, "unit": UNIT}
+        cpu.update(run.describe(1))
 
     if rank == 0:
         step_alg = (STEP_BYTES_FIXED + SOR_BYTES_PER_CELL_ITER * K) * cells
@@ -590,15 +677,21 @@ def run_ours(args):
             "config": {"workload": args.workload, "grid": [w.W, w.H, w.D], "sor_iters": K,
                        "omega": round(float(w.params.omega), 6), "substeps": int(w.params.substeps),
                        "advection": "inMAC_outMAC + MAC scalar", "sor_depth": depth, "graph": True,
+                       "sor_variant": sor_v, "sor_zchunk": sor_zc, "sor_tuned_us_per_iter": sor_us,
+                       "sor_kernel": (None if vinfo is None else
+                                      f"{'k_sor_quad' if vinfo.x_cells_per_thread == 4 else 'k_sor_reg/rb'}"
+                                      f"<depth {vinfo.depth}, {vinfo.tile_x}x{vinfo.tile_y}>"),
                        "l2": "working set %.2f GB > 129 MB L2, no flush" % (g.layout().field_elems * 4 * 21.25 / 1e9),
                        "parallelism": "replicas" if world > 1 else "single"},
-            "roofline": {"bound": "hbm", "kernel": "k_sor_reg", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "roofline": {"bound": "hbm", "kernel": "fused red-black SOR pass", "achieved": achieved, "peak": peak,
+                         "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "alg_bytes_per_launch": alg_bytes, "ms_per_launch": sor_ms_per_launch,
                          "step_alg_gbs": step_alg / (ms / args.steps * 1e-3) / 1e9,
                          "step_frac": step_alg / (ms / args.steps * 1e-3) / 1e9 / peak},
+            "max_abs_div_after_projection": st_proj.max_abs_div, "residual_l2_after_projection": st_proj.residual_l2,
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches_per_step * args.steps, "clocks": clocks,
-            "batch": batch, "adjoint": adjoint, "coarse": coarse, "render": render,
+            "batch": batch, "adjoint": adjoint, "coarse": coarse, "large": large, "render": render,
         }
         print(json.dumps(line), flush=True)
     g.close()

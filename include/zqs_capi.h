@@ -193,18 +193,35 @@ ZQS_API int zqs_grid_mac_to_regular4(zqs_grid* g, float* vel4, int dst_on_device
 ZQS_API int zqs_grid_stats(zqs_grid* g, zqs_stats* out, void* stream);
 
 /* SOR kernel selection: temporal_depth = red-black iterations fused per HBM
- * pass (0 = autotuned choice, 1 = one iteration per pass); split_colours != 0
- * runs the plain one-colour-per-launch kernel (the self-check path). */
+ * pass (1..4), or 0 (the default): the variant and z chunk an autotuner
+ * measured fastest for this grid's shape on this device.  The tuner times
+ * every fused variant that fits at a few z chunks (about 25 x 7 short runs of
+ * one pass) on the first step or projection that is not issued inside a
+ * stream capture, and keeps the choice per (device, shape) in memory and in
+ * the file $ZQS_TUNE_CACHE (default $XDG_CACHE_HOME/zqs_gb300/sor_tune.txt or
+ * ~/.cache/zqs_gb300/sor_tune.txt; ZQS_TUNE_CACHE="" keeps no file);
+ * ZQS_AUTOTUNE=0 uses the fixed default variant instead.  All variants give
+ * bit-identical results.  split_colours != 0 runs the plain
+ * one-colour-per-launch kernel (the self-check path). */
 ZQS_API int zqs_grid_set_sor_config(zqs_grid* g, int temporal_depth, int split_colours);
+
+/* The fused SOR variant (index for zqs_sor_variant_info; -1 for the split
+ * kernel), z chunk (0: automatic) and, when it was tuned, the measured time
+ * per iteration in microseconds that the next projection uses; runs the tuner
+ * first when it is due (synchronises the stream, not inside a capture). */
+ZQS_API int zqs_grid_get_sor_choice(zqs_grid* g, int* variant, int* zchunk, float* us_per_iter, void* stream);
 
 /* Fused SOR kernel variants (for tuning): iterations fused per HBM pass, xy
  * tile, cell pairs per thread, threads and shared memory per CTA, CTAs that fit
  * on one SM of the current device (0: does not fit), whether the update
- * weights are held in registers, registers per thread. */
+ * weights are held in registers, registers per thread, x-adjacent cells per
+ * thread (2: the pair forms, 4: the quad form). */
 typedef struct zqs_sor_variant {
     int32_t depth, tile_x, tile_y, pairs_per_thread, threads, ctas_per_sm;
     int64_t smem_bytes;
     int32_t weights_in_registers, registers;
+    int32_t x_cells_per_thread; /* 2: one red-black pair per row, 4: two x-adjacent pairs */
+    int32_t reserved;
 } zqs_sor_variant;
 ZQS_API int zqs_sor_variant_count(void);
 ZQS_API int zqs_sor_variant_info(int index, zqs_sor_variant* out);
@@ -250,6 +267,12 @@ ZQS_API int zqs_batch_set_sor_variant(zqs_batch* b, int index, int zchunk);
 
 /* Kernel launches of one batched step (for accounting). */
 ZQS_API int64_t zqs_batch_launch_count(const zqs_batch* b);
+/* The batch's fused SOR variant: the one set by zqs_batch_set_sor_variant, or
+ * (index -1, the default) the batchable variant that measured fastest per
+ * iteration on this batch's own tile lists when its tables were first built
+ * (ZQS_AUTOTUNE=0: the fixed default); us_per_iter is the measured time
+ * (0 when nothing was measured). */
+ZQS_API int zqs_batch_get_sor_choice(const zqs_batch* b, int* variant, float* us_per_iter);
 ZQS_API int zqs_batch_synchronize(zqs_batch* b, void* stream);
 
 /* Coarse solver, obstacle-free blocks (the dense block product of
@@ -259,6 +282,21 @@ ZQS_API int zqs_batch_synchronize(zqs_batch* b, void* stream);
  * tensor-core wait that times out is reported by zqs_grid_synchronize
  * (ZQS_ETIMEOUT). */
 ZQS_API int zqs_grid_set_coarse_gemm(zqs_grid* g, int mode);
+
+/* ---- failure injection (test hooks) -----------------------------------------
+ * Host-side only: neither hook faults, traps or hangs the GPU.
+ * zqs_debug_inject_tc_stall(1): the coarse solver's tensor-core block products
+ * launched from now on issue no operand copies, so their bounded mbarrier
+ * waits give up after about 4096 polls with nothing in flight; the kernel
+ * frees its tensor memory, skips the blocks and sets the error flag that
+ * zqs_grid_synchronize reports as ZQS_ETIMEOUT.  0 restores normal launches.
+ * (A CUDA graph keeps the setting it was captured with.)
+ * zqs_debug_fail_alloc(n): the n-th device allocation the library makes from
+ * now on (0 = the next one) fails as if the device were out of memory, so the
+ * call that makes it returns ZQS_ENOMEM and releases what it had taken; -1
+ * disables. */
+ZQS_API int zqs_debug_inject_tc_stall(int enable);
+ZQS_API int zqs_debug_fail_alloc(int nth);
 
 /* ---- moving voxel objects ---------------------------------------------------
  * ZQ_ApplyMovingObject3D (ZQ_SmokeSimulationUtils3D.cpp:1933-2046): the grid's

@@ -115,9 +115,14 @@ ZQS_API int zqs_project_sor(float* mac_u, float* mac_v, float* mac_w, const uint
  * 7.6 MB, held by every GPU that loads the library until the process exits),
  * which limits the grid to ZQS_NOALLOC_MAX_ELEMS padded elements per field,
  * (W+1 rounded up to 4)*(H+1)*(D+3); 64x64x64 fits.  Larger grids return
- * ZQS_EINVAL.  The first call on each device looks up the array's device
- * address; make that first call before any stream capture.  All calls share
- * the array, so calls that overlap on the GPU (different streams, or
+ * ZQS_EINVAL.  The first call on each device does the one-time setup for that
+ * device: the array's device address, the shared-memory attributes and
+ * occupancy of the SOR kernels, and the loading of the kernels it runs (the
+ * closed solver runs two more than the open one); make a first call with each
+ * solver type you use before any stream capture.  Every device that calls it
+ * has its own copy of the array; the devices of one process must be the same
+ * GPU model (another model returns ZQS_EUNSUPPORTED).  All calls on a device
+ * share its array, so calls that overlap on the GPU (different streams, or
  * concurrent host threads) race; serialise them.  Returns zqs_status. */
 #define ZQS_NOALLOC_MAX_ELEMS 300000
 ZQS_API int zqs_project_sor_noalloc(float* d_u, float* d_v, float* d_w, const uint8_t* d_occupy, int width,

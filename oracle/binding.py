@@ -2,8 +2,9 @@
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
 CPU-baseline / reference arm of bench.py, always to check results.  The oracle
-restates the reference's per-timestep path (see zqs_oracle.cpp); parity of the
-reference itself is unpinned (no golden outputs exist in the reference).
+restates the reference's per-timestep path (see zqs_oracle.cpp); the GPU tests
+pin it to the reference's own kernels for every stage but the SOR, whose
+source is not in the reference tree (tests/test_ref_pin_gpu.py).
 """
 from __future__ import annotations
 

@@ -7,14 +7,22 @@
  * tests, the smoke check and bench.py's CPU-baseline / reference arm may load
  * it.  Nothing in the product links or calls it.
  *
- * Parity status: UNPINNED by the reference.  The reference ships no tests or
- * golden outputs, cannot be built here (Windows/VS2015, legacy texture
- * references, missing ZQlib/ZQlibCuda), and its SOR solver lives in the
- * un-vendored ZQlibCuda library; see the per-function citations for the
- * in-tree evidence each rule is restated from.  Independent plain-Python /
- * numpy restatements of the reference loops check it in the tests (SOR, the
- * advection modes and BFECC, the write-backs, forces, object stamping, the
- * coarse stages and block step, the viewer's shader).
+ * Parity status: pinned to the reference's own kernels for the forces,
+ * attenuation, MAC<->regular conversion, velocity and scalar advection and
+ * the write-backs.  The reference ships no tests or golden outputs and cannot
+ * be built as a program here (Windows/VS2015, missing ZQlib/ZQlibCuda), but
+ * its kernel files ZQ_CUDA_MACtoRegular.cu, ZQ_CUDA_Attenuation3D.cu,
+ * ZQ_CUDA_AddForce3D.cu and ZQ_CUDA_Advection3D.cu compile unmodified as
+ * device modules (oracle/build_ref.py, texture references served by
+ * oracle/ref_shim/texref_shim.cuh), and tests/test_ref_pin_gpu.py runs them
+ * against this file: bit for bit where the arithmetic is theirs, within 1e-5
+ * where their normalised MAC texture coordinates round.  The red-black SOR
+ * stays a restatement: its source lives in the un-vendored ZQlibCuda.  See
+ * the per-function citations for the in-tree evidence each rule is restated
+ * from.  Independent plain-Python / numpy restatements of the reference loops
+ * check it in the tests too (SOR, the advection modes and BFECC, the
+ * write-backs, forces, object stamping, the coarse stages and block step, the
+ * viewer's shader).
  *
  * Arithmetic contract (shared with the CUDA kernels so FP32 results can match
  * bit for bit): no contraction (built with -ffp-contract=off; kernels with

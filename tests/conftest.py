@@ -10,9 +10,24 @@ if str(ROOT) not in sys.path:
     sys.path.insert(0, str(ROOT))
 
 
+def pytest_addoption(parser):
+    parser.addoption("--runlong", action="store_true", default=False,
+                     help="also run the tests marked long (trajectories of several minutes of oracle time)")
+
+
+def pytest_collection_modifyitems(config, items):
+    if config.getoption("--runlong"):
+        return
+    skip = pytest.mark.skip(reason="long: run with --runlong")
+    for item in items:
+        if "long" in item.keywords:
+            item.add_marker(skip)
+
+
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300); runs the CUDA library through the C ABI")
     config.addinivalue_line("markers", "slow: long-running parity case")
+    config.addinivalue_line("markers", "long: minutes of oracle time; runs only with --runlong")
 
 
 @pytest.fixture(scope="session")

@@ -217,17 +217,19 @@ def _control64_check(ndirs, seed=0):
 
 @pytest.mark.slow
 def test_control64_gradient(zqs_lib):
-    rel64, errs, gnorm = _control64_check(4)
+    """Configuration 4 at 64^3 (64 steps, checkpoints every 8; confinement off
+    and dt = 32/N, workloads.control_problem): GPU gradient within 1e-3 of the
+    FP64 CPU gradient, and FP64 central differences (h = 1e-3) along 8 seeded
+    unit directions within 1e-3 of |grad L|."""
+    rel64, errs, gnorm = _control64_check(8)
     assert rel64 <= GRAD_TOL
     for e in errs:
         assert e["err_rel_gnorm"] <= GRAD_TOL, e
 
 
-@pytest.mark.slow
+@pytest.mark.long
 def test_control64_gradient_32_directions(zqs_lib):
-    import os
-    if os.environ.get("ZQS_FULL_ADJOINT_CHECK") != "1":
-        pytest.skip("32-direction FP64 finite differences take minutes; set ZQS_FULL_ADJOINT_CHECK=1")
+    """The same with the 32 directions of the configuration (--runlong)."""
     rel64, errs, gnorm = _control64_check(32)
     assert rel64 <= GRAD_TOL
     for e in errs:

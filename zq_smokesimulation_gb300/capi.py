@@ -123,7 +123,8 @@ class Stats(C.Structure):
 class SorVariant(C.Structure):
     _fields_ = [("depth", C.c_int32), ("tile_x", C.c_int32), ("tile_y", C.c_int32),
                 ("pairs_per_thread", C.c_int32), ("threads", C.c_int32), ("ctas_per_sm", C.c_int32),
-                ("smem_bytes", C.c_int64), ("weights_in_registers", C.c_int32), ("registers", C.c_int32)]
+                ("smem_bytes", C.c_int64), ("weights_in_registers", C.c_int32), ("registers", C.c_int32),
+                ("x_cells_per_thread", C.c_int32), ("reserved", C.c_int32)]
 
 
 class AdjointInfo(C.Structure):
@@ -145,12 +146,14 @@ CAPI_SYMBOLS = [
     "zqs_grid_download", "zqs_grid_step", "zqs_grid_use_graph", "zqs_stage_add_force", "zqs_stage_attenuate",
     "zqs_stage_advect_velocity", "zqs_stage_project", "zqs_stage_advect_scalar", "zqs_stage_reinject",
     "zqs_grid_mac_to_regular4", "zqs_grid_stats", "zqs_grid_set_sor_config", "zqs_sor_variant_count",
-    "zqs_sor_variant_info", "zqs_grid_set_sor_variant", "zqs_grid_synchronize", "zqs_grid_launch_count",
+    "zqs_sor_variant_info", "zqs_grid_set_sor_variant", "zqs_grid_get_sor_choice", "zqs_grid_synchronize",
+    "zqs_grid_launch_count",
     "zqs_batch_create", "zqs_batch_destroy", "zqs_batch_step", "zqs_batch_use_graph", "zqs_batch_set_sor_variant",
-    "zqs_batch_launch_count", "zqs_batch_synchronize",
+    "zqs_batch_launch_count", "zqs_batch_synchronize", "zqs_batch_get_sor_choice",
     "zqs_grid_set_force", "zqs_grid_stamp_objects", "zqs_grid_set_coarse_gemm", "zqs_camera_default", "zqs_render_density", "zqs_grid_render",
     "zqs_adjoint_create", "zqs_adjoint_destroy", "zqs_adjoint_forward",
     "zqs_adjoint_backward", "zqs_adjoint_download", "zqs_adjoint_get_info",
+    "zqs_debug_inject_tc_stall", "zqs_debug_fail_alloc",
 ]
 LEGACY_C_SYMBOLS = ["ZQ_Cuda_Prepare_Advection", "Advect_Velocity", "Advect_Scalar", "AddForce3D",
                     "Attenuation3D", "zqs_project_sor", "zqs_project_sor_noalloc"]
@@ -210,11 +213,15 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.zqs_sor_variant_count.restype = i
     lib.zqs_sor_variant_info.argtypes = [i, C.POINTER(SorVariant)]
     lib.zqs_grid_set_sor_variant.argtypes = [vp, i, i]
+    lib.zqs_debug_inject_tc_stall.argtypes = [i]
+    lib.zqs_debug_fail_alloc.argtypes = [i]
+    lib.zqs_grid_get_sor_choice.argtypes = [vp, C.POINTER(i), C.POINTER(i), C.POINTER(C.c_float), vp]
     lib.zqs_batch_create.argtypes = [C.POINTER(vp), C.POINTER(vp), i]
     lib.zqs_batch_destroy.argtypes = [vp]
     lib.zqs_batch_step.argtypes = [vp, i, vp]
     lib.zqs_batch_use_graph.argtypes = [vp, i]
     lib.zqs_batch_set_sor_variant.argtypes = [vp, i, i]
+    lib.zqs_batch_get_sor_choice.argtypes = [vp, C.POINTER(i), C.POINTER(C.c_float)]
     lib.zqs_batch_launch_count.argtypes = [vp]
     lib.zqs_batch_launch_count.restype = C.c_int64
     lib.zqs_batch_synchronize.argtypes = [vp, vp]
@@ -339,6 +346,13 @@ class Grid:
 
     def set_sor_variant(self, index: int = -1, zchunk: int = 0):
         check(self.lib.zqs_grid_set_sor_variant(self.h, index, zchunk), "set_sor_variant")
+
+    def sor_choice(self, stream: int | None = None) -> tuple[int, int, float]:
+        """(variant, zchunk, measured us per iteration) the next projection uses."""
+        v, z, us = C.c_int(), C.c_int(), C.c_float()
+        check(self.lib.zqs_grid_get_sor_choice(self.h, C.byref(v), C.byref(z), C.byref(us),
+                                               C.c_void_p(stream) if stream else None), "get_sor_choice")
+        return v.value, z.value, us.value
 
     def use_graph(self, enable: bool):
         check(self.lib.zqs_grid_use_graph(self.h, 1 if enable else 0), "use_graph")
@@ -505,6 +519,12 @@ class Batch:
 
     def launch_count(self) -> int:
         return int(self.lib.zqs_batch_launch_count(self.h))
+
+    def sor_choice(self) -> tuple[int, float]:
+        """(variant, measured us per iteration) of the batched SOR passes."""
+        v, us = C.c_int(), C.c_float()
+        check(self.lib.zqs_batch_get_sor_choice(self.h, C.byref(v), C.byref(us)), "batch sor_choice")
+        return v.value, us.value
 
 
 class Adjoint:

@@ -167,7 +167,7 @@ ZQS_API int zqs_grid_set_force(zqs_grid* g, const float* F, int src_on_device, v
         return ZQS_OK;
     }
     if (!g->fext_base) {
-        ZQS_CUDA_TRY(cudaMalloc(&g->fext_base, (size_t)L.elems * 3 * 4));
+        ZQS_CUDA_TRY(dev_alloc(&g->fext_base, (size_t)L.elems * 3 * 4));
         ZQS_CUDA_TRY(cudaMemsetAsync(g->fext_base, 0, (size_t)L.elems * 3 * 4, s));
     }
     const size_t n = (size_t)L.W * L.H * L.D;
@@ -231,7 +231,7 @@ ZQS_API int zqs_adjoint_create(zqs_adjoint** out, zqs_grid* g, int nsteps, int c
     const long long nblocks = (long long)((L.W + 31) / 32) * ((L.H + 7) / 8) * L.D;
     const size_t red_len = (size_t)(2 * nblocks + 16);
     const size_t total = (nslots * 5 + nflt) * fe * 4 + nf4 * fe * 16 + red_len * 8 + 256;
-    cudaError_t e = cudaMalloc(&a->mem, total);
+    cudaError_t e = dev_alloc(&a->mem, total);
     if (e != cudaSuccess) return fail(cuda_fail(e, "zqs_adjoint_create: cudaMalloc"));
     e = cudaMemset(a->mem, 0, total);
     if (e != cudaSuccess) return fail(cuda_fail(e, "zqs_adjoint_create: clear"));
@@ -358,7 +358,7 @@ ZQS_API int zqs_adjoint_backward(zqs_adjoint* a, const float* g_density, float* 
     }
     if (g->fext_on) {
         if (!w->fext_base) {
-            ZQS_CUDA_TRY(cudaMalloc(&w->fext_base, (size_t)L.elems * 3 * 4));
+            ZQS_CUDA_TRY(dev_alloc(&w->fext_base, (size_t)L.elems * 3 * 4));
         }
         ZQS_CUDA_TRY(cudaMemcpyAsync(w->fext_base, g->fext_base, (size_t)L.elems * 3 * 4, cudaMemcpyDeviceToDevice,
                                      s));

@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
 #include <string>
@@ -31,8 +32,10 @@ struct zqs_batch {
     int K = 0;
     bool any_closed = false;
     SorBatchPlan plan;
-    int variant = -1;
+    int variant = -1;      // as set by zqs_batch_set_sor_variant (-1: tuned)
     int zchunk = 0;
+    int tuned_variant = -1;  // the batchable variant measured fastest on this batch
+    float tuned_us = 0.0f;   // its time per SOR iteration
     int par = 0;          // table buffer index holding the current velocity and scalars
     bool built = false;
     cudaStream_t own = nullptr;
@@ -138,10 +141,10 @@ void choose_batch_zc(const std::vector<Layout>& Ls, const SorBatchPlan& plan, in
     for (int i = 0; i < n; i++) zc[i] = std::min(best_z, Ls[i].D);
 }
 
-int build_table(zqs_batch* b) {
+int build_table_for(zqs_batch* b, int variant) {
     int rc = check_members(b);
     if (rc) return rc;
-    rc = sor_batch_plan(b->variant, b->plan);
+    rc = sor_batch_plan(variant, b->plan);
     if (rc) return rc;
     const int n = (int)b->grids.size();
     b->n = n;
@@ -218,7 +221,7 @@ int build_table(zqs_batch* b) {
             b->dev = nullptr;
             b->dev_bytes = 0;
         }
-        ZQS_CUDA_TRY(cudaMalloc(&b->dev, need));
+        ZQS_CUDA_TRY(dev_alloc(&b->dev, need));
         b->dev_bytes = need;
     }
     char* base = (char*)b->dev;
@@ -237,6 +240,55 @@ int build_table(zqs_batch* b) {
     b->drop_graphs();
     b->built = true;
     return ZQS_OK;
+}
+
+// Time per iteration of the batch's main SOR pass with the tables as built
+// (pressure of every member overwritten; the next projection restarts at 0).
+int time_batch_sor(zqs_batch* b, float& us) {
+    BatchLaunch bm{b->d_desc, b->d_pre[TC_SORM], b->n, b->total[TC_SORM]};
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    ZQS_CUDA_TRY(cudaEventCreate(&e0));
+    cudaError_t e = cudaEventCreate(&e1);
+    constexpr int kReps = 3;
+    if (e == cudaSuccess) e = launch_sor_batch_pass(b->plan, 0, bm, 0, b->own);  // warm-up
+    if (e == cudaSuccess) e = cudaEventRecord(e0, b->own);
+    for (int r = 0; r < kReps && e == cudaSuccess; r++) e = launch_sor_batch_pass(b->plan, 0, bm, (r + 1) & 1, b->own);
+    if (e == cudaSuccess) e = cudaEventRecord(e1, b->own);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float ms = 0.0f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (e != cudaSuccess) return cuda_fail(e, "zqs_batch: SOR tuning");
+    us = 1000.0f * ms / (kReps * (b->plan.S[0] / 2));
+    return ZQS_OK;
+}
+
+// The tables for the configured variant; with variant -1 (and ZQS_AUTOTUNE
+// not 0) every batchable variant is timed on this batch's own tile lists once
+// and the fastest per iteration kept (all give bit-identical results).
+int build_table(zqs_batch* b) {
+    if (b->variant >= 0) return build_table_for(b, b->variant);
+    const char* env = std::getenv("ZQS_AUTOTUNE");
+    if ((env && env[0] == '0') || b->grids[0]->params.sor_iters == 0) return build_table_for(b, -1);
+    if (b->tuned_variant < 0) {
+        float best = 1e30f;
+        for (int v = 0; v < sor_variant_count(); v++) {
+            if (!sor_variant_batchable(v)) continue;
+            int rc = build_table_for(b, v);
+            if (rc) return rc;
+            float us = 0.0f;
+            rc = time_batch_sor(b, us);
+            if (rc) return rc;
+            if (us < best) {
+                best = us;
+                b->tuned_variant = v;
+                b->tuned_us = us;
+            }
+        }
+        if (b->tuned_variant < 0) return build_table_for(b, -1);
+    }
+    return build_table_for(b, b->tuned_variant);
 }
 
 // The table is current when no member changed and every member's current
@@ -351,6 +403,7 @@ ZQS_API int zqs_batch_set_sor_variant(zqs_batch* b, int index, int zchunk) {
     }
     b->variant = index;
     b->zchunk = zchunk;
+    b->tuned_variant = -1;
     b->built = false;  // rebuilt (tile lists change) at the next step
     b->drop_graphs();
     return ZQS_OK;
@@ -411,6 +464,13 @@ ZQS_API int zqs_batch_step(zqs_batch* b, int nsteps, void* stream) {
 }
 
 ZQS_API int64_t zqs_batch_launch_count(const zqs_batch* b) { return b ? b->step_launches : 0; }
+
+ZQS_API int zqs_batch_get_sor_choice(const zqs_batch* b, int* variant, float* us_per_iter) {
+    if (!b) return set_error("zqs_batch_get_sor_choice: NULL batch"), ZQS_EINVAL;
+    if (variant) *variant = b->plan.vmain;
+    if (us_per_iter) *us_per_iter = (b->variant < 0 && b->plan.vmain == b->tuned_variant) ? b->tuned_us : 0.0f;
+    return ZQS_OK;
+}
 
 ZQS_API int zqs_batch_synchronize(zqs_batch* b, void* stream) {
     if (!b) return set_error("NULL batch"), ZQS_EINVAL;

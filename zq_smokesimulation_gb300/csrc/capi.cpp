@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -20,6 +21,24 @@
 namespace zqs {
 
 static thread_local std::string g_last_error;
+
+// zqs_debug_fail_alloc: the allocation that is due to fail counts down to 0
+// (-1: none).
+static std::atomic<long long> g_alloc_fail_in{-1};
+
+cudaError_t dev_alloc_raw(void** p, size_t bytes) {
+    long long n = g_alloc_fail_in.load(std::memory_order_relaxed);
+    while (n >= 0) {
+        if (g_alloc_fail_in.compare_exchange_weak(n, n - 1, std::memory_order_relaxed)) {
+            if (n == 0) {
+                *p = nullptr;
+                return cudaErrorMemoryAllocation;
+            }
+            break;
+        }
+    }
+    return cudaMalloc(p, bytes);
+}
 
 void set_error(const std::string& msg) { g_last_error = msg; }
 
@@ -180,7 +199,7 @@ int host_stage(zqs_grid* g, size_t n, cudaStream_t s, float** out) {
         if (g->stage) cudaFree(g->stage);
         g->stage = nullptr;
         g->stage_cap = 0;
-        ZQS_CUDA_TRY(cudaMalloc(&g->stage, n * sizeof(float)));
+        ZQS_CUDA_TRY(dev_alloc(&g->stage, n * sizeof(float)));
         g->stage_cap = n;
     }
     ZQS_CUDA_TRY(cudaStreamWaitEvent(s, g->stage_ev, 0));
@@ -258,12 +277,12 @@ ZQS_API int zqs_grid_create(zqs_grid** out, int W, int H, int D) {
     g->g.red_len = 3 * nblocks + 16;
     size_t total = nflt * fbytes + 5 * (size_t)L.elems * 16 + (((size_t)L.elems + 255) / 256) * 256 +
                    (size_t)g->g.red_len * 8 + 256;
-    cudaError_t e = cudaMalloc(&g->base, total);
+    cudaError_t e = dev_alloc(&g->base, total);
     if (e != cudaSuccess) {
         delete g;
         return cuda_fail(e, "zqs_grid_create: cudaMalloc");
     }
-    e = cudaMalloc(&g->occ_dense, (size_t)W * H * D);
+    e = dev_alloc(&g->occ_dense, (size_t)W * H * D);
     if (e != cudaSuccess) {
         cudaFree(g->base);
         delete g;
@@ -498,10 +517,22 @@ ZQS_API int zqs_grid_set_sor_config(zqs_grid* g, int temporal_depth, int split_c
         set_error("zqs_grid_set_sor_config: temporal_depth must be in [0, 4]");
         return ZQS_EINVAL;
     }
-    g->sor.temporal_depth = temporal_depth == 0 ? 2 : temporal_depth;
+    g->sor.temporal_depth = temporal_depth;
     g->sor.split = split_colours ? 1 : 0;
     g->sor.variant = -1;
     g->drop_graphs();
+    return ZQS_OK;
+}
+
+ZQS_API int zqs_grid_get_sor_choice(zqs_grid* g, int* variant, int* zchunk, float* us_per_iter, void* stream) {
+    if (!g) return set_error("zqs_grid_get_sor_choice: NULL grid"), ZQS_EINVAL;
+    int rc = g->ready();
+    if (rc) return rc;
+    rc = g->resolve_sor(g->pick(stream));
+    if (rc) return rc;
+    if (variant) *variant = g->sor_eff.split ? -1 : g->sor_eff.variant;
+    if (zchunk) *zchunk = g->sor_eff.zchunk;
+    if (us_per_iter) *us_per_iter = (g->sor_eff.variant == g->tuned.variant) ? g->tuned.us_per_iter : 0.0f;
     return ZQS_OK;
 }
 
@@ -515,6 +546,8 @@ ZQS_API int zqs_grid_step(zqs_grid* g, int nsteps, void* stream) {
     cudaStream_t s = g->pick(stream);
     for (int n = 0; n < nsteps; n++) {
         if (!g->use_graph) {
+            rc = g->resolve_sor(s);
+            if (rc) return rc;
             LaunchCounter lc;
             rc = g->issue_step(s, lc);
             if (rc) return rc;
@@ -523,6 +556,8 @@ ZQS_API int zqs_grid_step(zqs_grid* g, int nsteps, void* stream) {
         }
         const int key = g->vel_par * 2 + g->sca_par;
         if (!g->graph[key]) {
+            rc = g->resolve_sor(s);  // before the capture: the tuner synchronises
+            if (rc) return rc;
             // Capture on the grid's own stream: the launches read the current
             // buffer pointers, so capturing advances the parities; restore them.
             const int vp = g->vel_par, sp = g->sca_par;
@@ -594,7 +629,9 @@ ZQS_API int zqs_stage_project(zqs_grid* g, void* stream) {
     int rc = g->ready();
     if (rc) return rc;
     LaunchCounter lc;
-    return launch_project(g->g, g->kp, g->params.sor_iters, g->sor, g->pick(stream), lc, &g->p_last);
+    rc = g->resolve_sor(g->pick(stream));
+    if (rc) return rc;
+    return launch_project(g->g, g->kp, g->params.sor_iters, g->sor_eff, g->pick(stream), lc, &g->p_last);
 }
 
 ZQS_API int zqs_stage_advect_scalar(zqs_grid* g, int mode, void* stream) {
@@ -693,5 +730,14 @@ ZQS_API int zqs_grid_set_coarse_gemm(zqs_grid* g, int mode) {
 }
 
 ZQS_API int64_t zqs_grid_launch_count(const zqs_grid* g) { return g ? g->step_launches : 0; }
+
+ZQS_API int zqs_debug_fail_alloc(int nth) {
+    if (nth < -1) {
+        set_error("zqs_debug_fail_alloc: nth must be >= -1");
+        return ZQS_EINVAL;
+    }
+    g_alloc_fail_in.store(nth, std::memory_order_relaxed);
+    return ZQS_OK;
+}
 
 }  // extern "C"

@@ -57,7 +57,11 @@ struct VelPass {
     float* out[3];
 };
 
-// One thread per face: bz = comp*(D+1) + k, comp 0/1/2 = u/v/w.
+// One thread per face: bz = 3*k + comp, comp 0/1/2 = u/v/w.  The three
+// components of a plane are adjacent in the launch order, so the CTAs resident
+// together sample the velocity around the same few planes and every quad line
+// comes from DRAM about once (component-major order streamed the three quad
+// arrays once per component).
 // REGIN: the regular (cell-centre float4) velocity for the backtrace and the
 // regular input for the final sample (inRegular_outMAC), else MAC velocity
 // read through its quad copies (inMAC_outMAC).  RAW: every face of the
@@ -70,8 +74,8 @@ __device__ __forceinline__ void advect_vel_macout_tile(const Layout& L, const Ve
                                                        int open, int bx, int by, int bz) {
     const int i = bx * 32 + threadIdx.x;
     const int j = by * 8 + threadIdx.y;
-    const int comp = bz / (L.D + 1);
-    const int k = bz - comp * (L.D + 1);
+    const int k = bz / 3;
+    const int comp = bz - 3 * k;
     int nx = L.W, ny = L.H, nz = L.D;
     if (comp == 0) nx++;
     else if (comp == 1) ny++;

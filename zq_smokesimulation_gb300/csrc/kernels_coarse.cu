@@ -693,7 +693,7 @@ int get_mt(int s, const float** out) {
     for (int r = 0; r < rows; r++)
         for (int q = 0; q < nf; q++) MT[(size_t)q * rows + r] = M[(size_t)r * nf + q];
     float* d = nullptr;
-    ZQS_CUDA_TRY(cudaMalloc(&d, MT.size() * sizeof(float)));
+    ZQS_CUDA_TRY(dev_alloc(&d, MT.size() * sizeof(float)));
     cudaError_t e = cudaMemcpy(d, MT.data(), MT.size() * sizeof(float), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
         cudaFree(d);
@@ -726,9 +726,9 @@ int coarse_alloc_tc(CoarseState* c) {
     if (c->s < 2 || c->Xsplit) return ZQS_OK;
     int rc = subproj_tc_prepare(c->s);
     if (rc) return rc;
-    ZQS_CUDA_TRY(cudaMalloc(&c->Xsplit, subproj_tc_split_bytes(c->nblocks, c->nf)));
+    ZQS_CUDA_TRY(dev_alloc(&c->Xsplit, subproj_tc_split_bytes(c->nblocks, c->nf)));
     if (!c->err) {
-        ZQS_CUDA_TRY(cudaMalloc(&c->err, sizeof(int)));
+        ZQS_CUDA_TRY(dev_alloc(&c->err, sizeof(int)));
         ZQS_CUDA_TRY(cudaMemset(c->err, 0, sizeof(int)));
     }
     return ZQS_OK;
@@ -773,7 +773,7 @@ int coarse_prepare(CoarseState*& cs, const Layout& L, int s, int tc) {
     const size_t bb = ((size_t)c->nblocks + 255) / 256 * 256;
     const size_t xb = s > 1 ? (size_t)c->nblocks * c->nf * 4 : 0;
     const size_t total = 12 * fb + ob + bb + xb;
-    cudaError_t e = cudaMalloc(&c->base, total);
+    cudaError_t e = dev_alloc(&c->base, total);
     if (e != cudaSuccess) {
         delete c;
         return cuda_fail(e, "coarse state allocation");

@@ -88,7 +88,7 @@ extern "C" ZQS_API int zqs_grid_stamp_objects(zqs_grid* g, const zqs_object* obj
         if (g->obj_mask) cudaFree(g->obj_mask);
         g->obj_mask = nullptr;
         g->obj_mask_cap = 0;
-        ZQS_CUDA_TRY(cudaMalloc(&g->obj_mask, need));
+        ZQS_CUDA_TRY(dev_alloc(&g->obj_mask, need));
         g->obj_mask_cap = need;
     }
     if (need > 0) {

@@ -30,7 +30,18 @@
 #include "zqs_batch.h"
 #include "zqs_coarse.h"
 
+#include <sys/stat.h>
+
 #include <algorithm>
+#include <atomic>
+#include <cstdio>
+#include <cstdlib>
+#include <fstream>
+#include <map>
+#include <mutex>
+#include <set>
+#include <sstream>
+#include <string>
 #include <vector>
 
 namespace zqs {
@@ -593,6 +604,213 @@ __device__ __forceinline__ void sor_reg_tile(const Layout& L, const float* __res
     __syncthreads();
 }
 
+// Quad form of the register-column kernel: each thread owns four x-adjacent
+// cells (two of each colour) of its row, so per half-sweep it updates two
+// cells whose x neighbours are, but for one, its own registers; the row's
+// neighbours above and below arrive as one 8-byte shared-memory load each
+// (both colour-c^1 values of the group), the divergence as one, the result
+// leaves as one.  Per two updates: five shared-memory instructions instead of
+// ten in the pair form.  Same schedule (S half-sweeps in flight at lags 2s,
+// one barrier per two ring steps), same update arithmetic, same results.
+//
+// Shared memory per slot and colour c: float2 per thread, (.x, .y) = the
+// group's first and second colour-c cell (x offsets {0,2} when the group's
+// first cell has colour c, else {1,3}); the published pressure and the
+// divergence, NP slots each.  Incoming planes are 16-byte loads (x0 - S is a
+// multiple of 4 because TX and S are, as is the row pitch), flags one 4-byte
+// load.
+template <int S, int TX, int TY>
+struct QuadShape {
+    // x0 - S must be a multiple of 4 for the 16-byte plane loads and stores
+    static_assert(S % 4 == 0 && TX % 4 == 0, "S and TX multiples of 4");
+    static constexpr int RW = TX + 2 * S;  // multiple of 4
+    static constexpr int RH = TY + 2 * S;
+    static constexpr int GW = RW / 4;      // groups per row
+    static constexpr int NT = GW * RH;     // threads per CTA, one group each
+    static constexpr int NP = 2 * S + 2;
+    // floats ahead of the ring: the row -1 (GW float2) and x -1 reads of slot 0
+    static constexpr int GUARD = (2 * GW + 2 + 3) / 4 * 4;
+    static constexpr size_t smem = (size_t)NP * 2 * NT * 8 * 2 + (size_t)GUARD * 4;
+};
+
+template <int S, int TX, int TY>
+__device__ __forceinline__ void sor_quad_tile(const Layout& L, const float* __restrict__ pin,
+                                              float* __restrict__ pout, const float* __restrict__ div,
+                                              const uint8_t* __restrict__ flags, float omega, float om1, int bx,
+                                              int by, int z0, int z1) {
+    using Sh = QuadShape<S, TX, TY>;
+    constexpr int GW = Sh::GW, NP = Sh::NP, NT = Sh::NT;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* pub = reinterpret_cast<float2*>(reinterpret_cast<float*>(smem_raw) + Sh::GUARD);  // [NP][2][NT]
+    float2* sdv = pub + NP * 2 * NT;                                                           // [NP][2][NT]
+    const float* pubf = reinterpret_cast<const float*>(pub);
+
+    const int x0 = bx * TX, y0 = by * TY;
+    const int plane = (int)L.plane;
+    __shared__ float wtab[8];
+    if (threadIdx.x < 8) wtab[threadIdx.x] = threadIdx.x ? omega / (float)threadIdx.x : 0.0f;
+    __syncthreads();
+
+    const int e = threadIdx.x;
+    const int row = e / GW, gq = e - row * GW;
+    const int xl = x0 - S + 4 * gq;  // first cell of the group (multiple of 4)
+    const int j = y0 - S + row;
+    const int ly = row - S, lxl = 4 * gq - S;
+    const bool pin_ok = xl >= 0 && xl < L.W && j >= 0 && j < L.H;
+    const bool out_ok = pin_ok && ly >= 0 && ly < TY && lxl >= 0 && lxl < TX;
+    int gaddr = pin_ok ? lidx(L, xl, j, z0 - S) : 0;
+    // colour of the group's first cell at ring slot qs: bpar ^ (qs & 1) (1 = black)
+    const int bpar = (j + z0) & 1;
+    // act[par] bit 2(s-1)+k: half-sweep s updates the k-th colour-c cell, par = qs & 1
+    unsigned act[2];
+#pragma unroll
+    for (int par = 0; par < 2; par++) {
+        unsigned a = 0;
+#pragma unroll
+        for (int sw = 1; sw <= S; sw++) {
+            const int cs = (sw - 1) & 1;
+            const int odd = bpar ^ par ^ cs;  // colour-c cells at offsets {1,3} when set
+            const int r = S - sw;
+#pragma unroll
+            for (int k = 0; k < 2; k++) {
+                const int lx = lxl + 2 * k + odd;
+                if (lx >= -r && lx < TX + r && ly >= -r && ly < TY + r) a |= 1u << (2 * (sw - 1) + k);
+            }
+        }
+        act[par] = a;
+    }
+    // x neighbour outside the group: the left group's second colour-c^1 cell
+    // when the colour-c cells sit at {0,2}, else the right group's first;
+    // xsel[b] for b = (qs & 1) ^ c, as float offsets into the slot's array
+    int xsel[2];
+    xsel[0] = bpar ? 2 * (e + 1) : 2 * (e - 1) + 1;
+    xsel[1] = bpar ? 2 * (e - 1) + 1 : 2 * (e + 1);
+
+    const int tbeg = z0 - S;
+    const int nsteps = (z1 - z0) + 3 * S + 1;
+    const int flo = max(0, z0 - S), fhi = min(L.D, z1 + S);
+
+    float P[NP][2][2];   // pressure: [slot][colour][k]
+    float Wc[NP][2][2];  // omega/cnt: [slot][colour][k] (0: never updated)
+#pragma unroll
+    for (int a = 0; a < NP; a++)
+#pragma unroll
+        for (int c = 0; c < 2; c++) P[a][c][0] = P[a][c][1] = Wc[a][c][0] = Wc[a][c][1] = 0.0f;
+    float4 np4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), nd4 = np4;
+    unsigned nf = 0;
+    if (pin_ok && tbeg >= flo && tbeg < fhi) {
+        np4 = __ldg(reinterpret_cast<const float4*>(pin + gaddr));
+        nd4 = __ldg(reinterpret_cast<const float4*>(div + gaddr));
+        nf = __ldg(reinterpret_cast<const unsigned*>(flags + gaddr));
+    }
+
+    for (int g = 0; g < nsteps; g += NP) {
+#pragma unroll
+        for (int qs = 0; qs < NP; qs++) {
+            if (g + qs < nsteps) {
+                const int t = tbeg + g + qs;
+                // 1. plane t into registers by colour, and publish
+                {
+                    const bool lc = (bpar ^ (qs & 1)) != 0;  // first cell black
+                    const float w0 = wtab[(nf >> F_CNT_SHIFT) & 7u];
+                    const float w1 = wtab[(nf >> (8 + F_CNT_SHIFT)) & 7u];
+                    const float w2 = wtab[(nf >> (16 + F_CNT_SHIFT)) & 7u];
+                    const float w3 = wtab[(nf >> (24 + F_CNT_SHIFT)) & 7u];
+                    P[qs][0][0] = lc ? np4.y : np4.x;
+                    P[qs][0][1] = lc ? np4.w : np4.z;
+                    P[qs][1][0] = lc ? np4.x : np4.y;
+                    P[qs][1][1] = lc ? np4.z : np4.w;
+                    Wc[qs][0][0] = lc ? w1 : w0;
+                    Wc[qs][0][1] = lc ? w3 : w2;
+                    Wc[qs][1][0] = lc ? w0 : w1;
+                    Wc[qs][1][1] = lc ? w2 : w3;
+                    pub[(qs * 2 + 0) * NT + e] = make_float2(P[qs][0][0], P[qs][0][1]);
+                    pub[(qs * 2 + 1) * NT + e] = make_float2(P[qs][1][0], P[qs][1][1]);
+                    sdv[(qs * 2 + 0) * NT + e] = lc ? make_float2(nd4.y, nd4.w) : make_float2(nd4.x, nd4.z);
+                    sdv[(qs * 2 + 1) * NT + e] = lc ? make_float2(nd4.x, nd4.z) : make_float2(nd4.y, nd4.w);
+                }
+                // 2. prefetch plane t+1
+                gaddr += plane;
+                np4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                nd4 = np4;
+                nf = 0;
+                if (pin_ok && t + 1 >= flo && t + 1 < fhi) {
+                    np4 = __ldg(reinterpret_cast<const float4*>(pin + gaddr));
+                    nd4 = __ldg(reinterpret_cast<const float4*>(div + gaddr));
+                    nf = __ldg(reinterpret_cast<const unsigned*>(flags + gaddr));
+                }
+                // 3. half-sweeps (branch-free: inactive cells keep their value)
+#pragma unroll
+                for (int s = 1; s <= S; s++) {
+                    const int z = t - 2 * s;
+                    const int r = S - s;
+                    if (z >= max(z0 - r, 0) && z < min(z1 + r, L.D)) {
+                        const int c = (s - 1) & 1;  // red first
+                        const int sz = (qs - 2 * s + 2 * NP) % NP;
+                        const int szm = (sz + NP - 1) % NP;
+                        const int szp = (sz + 1) % NP;
+                        const bool E = ((bpar ^ (qs & 1) ^ c) == 0);  // colour-c cells at offsets {0,2}
+                        const float adj = pubf[(sz * 2 + (c ^ 1)) * NT * 2 + xsel[(qs & 1) ^ c]];
+                        const float2 ym = pub[(sz * 2 + (c ^ 1)) * NT + e - GW];
+                        const float2 yp = pub[(sz * 2 + (c ^ 1)) * NT + e + GW];
+                        const float2 dv = sdv[(sz * 2 + c) * NT + e];
+                        const float v0 = P[sz][c ^ 1][0], v1 = P[sz][c ^ 1][1];
+                        const float t0 = E ? adj : v1, t1 = E ? v0 : adj;
+                        const float s0 = ((v0 + t0) + (ym.x + yp.x)) + (P[szm][c ^ 1][0] + P[szp][c ^ 1][0]);
+                        const float s1 = ((v1 + t1) + (ym.y + yp.y)) + (P[szm][c ^ 1][1] + P[szp][c ^ 1][1]);
+                        const float o0 = P[sz][c][0], o1 = P[sz][c][1];
+                        const float w0 = Wc[sz][c][0], w1 = Wc[sz][c][1];
+                        const float n0 = sor_update(o0, s0, dv.x, w0, om1);
+                        const float n1 = sor_update(o1, s1, dv.y, w1, om1);
+                        const unsigned ab = act[qs & 1] >> (2 * (s - 1));
+                        const float r0 = ((ab & 1u) && w0 != 0.0f) ? n0 : o0;
+                        const float r1 = ((ab & 2u) && w1 != 0.0f) ? n1 : o1;
+                        P[sz][c][0] = r0;
+                        P[sz][c][1] = r1;
+                        pub[(sz * 2 + c) * NT + e] = make_float2(r0, r1);
+                    }
+                }
+                // 4. output plane t-2S-1
+                const int zo = t - 2 * S - 1;
+                if (zo >= z0 && zo < z1 && out_ok) {
+                    const int so = (qs - 2 * S - 1 + 2 * NP) % NP;
+                    const bool lc = (bpar ^ (qs & 1) ^ 1) != 0;  // first cell of plane zo black
+                    const float4 o = lc ? make_float4(P[so][1][0], P[so][0][0], P[so][1][1], P[so][0][1])
+                                        : make_float4(P[so][0][0], P[so][1][0], P[so][0][1], P[so][1][1]);
+                    *reinterpret_cast<float4*>(pout + gaddr - (2 * S + 2) * plane) = o;
+                }
+                // one barrier per two steps, as in sor_reg_tile
+                if (qs & 1) __syncthreads();
+            }
+        }
+    }
+    __syncthreads();
+}
+
+template <int S, int TX, int TY>
+__global__ void __launch_bounds__(QuadShape<S, TX, TY>::NT, 1)
+    k_sor_quad(Layout L, const float* __restrict__ pin, float* __restrict__ pout, const float* __restrict__ div,
+               const uint8_t* __restrict__ flags, float omega, float om1, int zc) {
+    const int z0 = blockIdx.z * zc;
+    sor_quad_tile<S, TX, TY>(L, pin, pout, div, flags, omega, om1, blockIdx.x, blockIdx.y, z0, min(z0 + zc, L.D));
+}
+
+// Persistent batched pass of the quad form (as k_sor_reg_batch).
+template <int S, int TX, int TY>
+__global__ void __launch_bounds__(QuadShape<S, TX, TY>::NT, 1) k_sor_quad_batch(BatchLaunch B, int pcur, int which) {
+    for (int t = blockIdx.x; t < B.total; t += gridDim.x) {
+        const int i = batch_find(B.pre, B.n, t);
+        const InstDesc& d = B.desc[i];
+        const int local = t - __ldg(B.pre + i);
+        const int tx = (d.L.W + TX - 1) / TX, ty = (d.L.H + TY - 1) / TY;
+        const int bx = local % tx, r = local / tx;
+        const int by = r % ty, bz = r / ty;
+        const int z0 = bz * d.zc[which];
+        sor_quad_tile<S, TX, TY>(d.L, d.p[pcur], d.p[pcur ^ 1], d.div, d.flags, d.kp.omega, d.kp.om1, bx, by, z0,
+                                 min(z0 + d.zc[which], d.L.D));
+    }
+}
+
 template <int S, int TX, int TY, int PPT, bool WREG>
 __global__ void __launch_bounds__(RegShape<S, TX, TY, PPT>::NT)
     k_sor_reg(Layout L, const float* __restrict__ pin, float* __restrict__ pout, const float* __restrict__ div,
@@ -823,6 +1041,7 @@ struct RbVariant {
     int ctas_per_sm_adj;
     int wreg;       // update weights in registers (k_sor_reg WREG form)
     int regs;       // registers per thread of fn
+    int xcells = 2; // x-adjacent cells per thread (2: a red-black pair, 4: the quad form)
 };
 
 template <int S, int TX, int TY, int PPT>
@@ -904,10 +1123,51 @@ RbVariant reg_variant() {
     return v;
 }
 
+template <int S, int TX, int TY>
+cudaError_t quad_launch(dim3 gr, const Layout& L, const float* pin, float* pout, const float* div,
+                        const uint8_t* flags, float omega, float om1, int zc, cudaStream_t st) {
+    using Sh = QuadShape<S, TX, TY>;
+    k_sor_quad<S, TX, TY><<<gr, Sh::NT, Sh::smem, st>>>(L, pin, pout, div, flags, omega, om1, zc);
+    return cudaGetLastError();
+}
+
+template <int S, int TX, int TY>
+cudaError_t quad_launch_batch(int blocks, const BatchLaunch& B, int pcur, int which, cudaStream_t st) {
+    using Sh = QuadShape<S, TX, TY>;
+    k_sor_quad_batch<S, TX, TY><<<blocks, Sh::NT, Sh::smem, st>>>(B, pcur, which);
+    return cudaGetLastError();
+}
+
+template <int S, int TX, int TY>
+RbVariant quad_variant() {
+    using Sh = QuadShape<S, TX, TY>;
+    RbVariant v;
+    v.S = S;
+    v.TX = TX;
+    v.TY = TY;
+    v.ppt = 2;
+    v.nt = Sh::NT;
+    v.smem = Sh::smem;
+    v.ctas_per_sm = 0;
+    v.launch = &quad_launch<S, TX, TY>;
+    v.fn = (const void*)k_sor_quad<S, TX, TY>;
+    v.launch_batch = &quad_launch_batch<S, TX, TY>;
+    v.fn_batch = (const void*)k_sor_quad_batch<S, TX, TY>;
+    v.ctas_per_sm_batch = 0;
+    v.launch_adj = nullptr;
+    v.fn_adj = nullptr;
+    v.ctas_per_sm_adj = 0;
+    v.wreg = 1;
+    v.regs = 0;
+    v.xcells = 4;
+    return v;
+}
+
 // The registry of fused SOR variants (temporal depth S/2, tile, pairs per thread);
 // 0-9 keep every plane in shared memory (k_sor_rb), 10-17 keep the thread's own
-// column in registers (k_sor_reg), 18-20 also the update weights (WREG).
-constexpr int kNumVariants = 21;
+// column in registers (k_sor_reg), 18-20 also the update weights (WREG), 21-23
+// are the quad form (k_sor_quad: four x-adjacent cells per thread).
+constexpr int kNumVariants = 24;
 RbVariant g_var[kNumVariants];
 // default variant per depth 1..4
 // (measured at 256^3 on GB300: register-column 32x32 at depth 2 with the
@@ -921,7 +1181,12 @@ const int kBatchDefaultVariant = 18;
 // reversed SOR of the adjoint: register-column variants in order of preference
 const int kAdjVariants[] = {13, 12, 11, 10};
 int g_num_sms = 0;
-int g_prepared = 0;
+// Devices (ordinals < 64) whose kernel attributes are set.  The variant table
+// (occupancy, registers) and the SM count come from the first device; another
+// device is accepted when it reports the same, i.e. the same GPU model.
+std::atomic<unsigned long long> g_prepared_mask{0};
+int g_first_device = -1;
+std::mutex g_prep_mu;
 
 // z chunk minimising the estimated pass time: waves x (chunk + pipeline fill)
 int choose_zc(const Layout& L, const RbVariant& v) {
@@ -954,55 +1219,77 @@ cudaError_t launch_pass(const RbVariant& v, const Layout& L, const float* pin, f
 }  // namespace
 
 int sor_prepare() {
-    if (g_prepared) return ZQS_OK;  // per process; one device
-    g_var[0] = rb_variant<2, 32, 16, 1>();
-    g_var[1] = rb_variant<2, 32, 16, 2>();
-    g_var[2] = rb_variant<2, 64, 16, 2>();
-    g_var[3] = rb_variant<4, 32, 16, 1>();
-    g_var[4] = rb_variant<4, 32, 16, 2>();
-    g_var[5] = rb_variant<4, 64, 16, 2>();
-    g_var[6] = rb_variant<6, 32, 16, 2>();
-    g_var[7] = rb_variant<8, 32, 8, 2>();
-    g_var[8] = rb_variant<2, 32, 32, 2>();
-    g_var[9] = rb_variant<4, 32, 32, 2>();
-    g_var[10] = reg_variant<2, 32, 16, 1>();
-    g_var[11] = reg_variant<2, 64, 16, 1>();
-    g_var[12] = reg_variant<4, 32, 16, 1>();
-    g_var[13] = reg_variant<4, 64, 16, 1>();
-    g_var[14] = reg_variant<4, 32, 32, 1>();
-    g_var[15] = reg_variant<6, 32, 16, 1>();
-    g_var[16] = reg_variant<2, 32, 16, 2>();
-    g_var[17] = reg_variant<4, 32, 16, 2>();
-    g_var[18] = reg_variant<4, 32, 32, 1, true>();
-    g_var[19] = reg_variant<4, 64, 16, 1, true>();
-    g_var[20] = reg_variant<6, 32, 16, 1, true>();
     int dev = 0;
     ZQS_CUDA_TRY(cudaGetDevice(&dev));
-    ZQS_CUDA_TRY(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
+    if (dev < 0 || dev >= 64) {
+        set_error("SOR kernels: device ordinals from 64 up are not supported");
+        return ZQS_EUNSUPPORTED;
+    }
+    if ((g_prepared_mask.load(std::memory_order_acquire) >> dev) & 1ull) return ZQS_OK;
+    std::lock_guard<std::mutex> lk(g_prep_mu);
+    if ((g_prepared_mask.load(std::memory_order_relaxed) >> dev) & 1ull) return ZQS_OK;
+    const bool first = g_first_device < 0;
+    if (first) {
+        g_var[0] = rb_variant<2, 32, 16, 1>();
+        g_var[1] = rb_variant<2, 32, 16, 2>();
+        g_var[2] = rb_variant<2, 64, 16, 2>();
+        g_var[3] = rb_variant<4, 32, 16, 1>();
+        g_var[4] = rb_variant<4, 32, 16, 2>();
+        g_var[5] = rb_variant<4, 64, 16, 2>();
+        g_var[6] = rb_variant<6, 32, 16, 2>();
+        g_var[7] = rb_variant<8, 32, 8, 2>();
+        g_var[8] = rb_variant<2, 32, 32, 2>();
+        g_var[9] = rb_variant<4, 32, 32, 2>();
+        g_var[10] = reg_variant<2, 32, 16, 1>();
+        g_var[11] = reg_variant<2, 64, 16, 1>();
+        g_var[12] = reg_variant<4, 32, 16, 1>();
+        g_var[13] = reg_variant<4, 64, 16, 1>();
+        g_var[14] = reg_variant<4, 32, 32, 1>();
+        g_var[15] = reg_variant<6, 32, 16, 1>();
+        g_var[16] = reg_variant<2, 32, 16, 2>();
+        g_var[17] = reg_variant<4, 32, 16, 2>();
+        g_var[18] = reg_variant<4, 32, 32, 1, true>();
+        g_var[19] = reg_variant<4, 64, 16, 1, true>();
+        g_var[20] = reg_variant<6, 32, 16, 1, true>();
+        g_var[21] = quad_variant<4, 32, 32>();
+        g_var[22] = quad_variant<4, 32, 16>();
+        g_var[23] = quad_variant<4, 64, 16>();
+    }
+    int sms = 0;
+    ZQS_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    bool same = first || sms == g_num_sms;
+    // attributes are per device: set them on this one, and compare occupancy
+    auto setup = [&](const void* fn, int nt, size_t smem, int& ctas) -> int {
+        ZQS_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int n = 0;
+        ZQS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, nt, smem));
+        if (first) ctas = n;  // 0: does not fit (never selected)
+        else if (n != ctas) same = false;
+        return ZQS_OK;
+    };
     for (int i = 0; i < kNumVariants; i++) {
         RbVariant& v = g_var[i];
-        ZQS_CUDA_TRY(cudaFuncSetAttribute(v.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)v.smem));
-        int n = 0;
-        ZQS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, v.fn, v.nt, v.smem));
-        v.ctas_per_sm = n;  // 0: does not fit (never selected)
-        cudaFuncAttributes fa;
-        ZQS_CUDA_TRY(cudaFuncGetAttributes(&fa, v.fn));
-        v.regs = fa.numRegs;
-        if (v.fn_batch) {
-            ZQS_CUDA_TRY(
-                cudaFuncSetAttribute(v.fn_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)v.smem));
-            n = 0;
-            ZQS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, v.fn_batch, v.nt, v.smem));
-            v.ctas_per_sm_batch = n;
+        int rc = setup(v.fn, v.nt, v.smem, v.ctas_per_sm);
+        if (rc) return rc;
+        if (first) {
+            cudaFuncAttributes fa;
+            ZQS_CUDA_TRY(cudaFuncGetAttributes(&fa, v.fn));
+            v.regs = fa.numRegs;
         }
-        if (v.fn_adj) {
-            ZQS_CUDA_TRY(cudaFuncSetAttribute(v.fn_adj, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)v.smem));
-            n = 0;
-            ZQS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, v.fn_adj, v.nt, v.smem));
-            v.ctas_per_sm_adj = n;
-        }
+        if (v.fn_batch && (rc = setup(v.fn_batch, v.nt, v.smem, v.ctas_per_sm_batch))) return rc;
+        if (v.fn_adj && (rc = setup(v.fn_adj, v.nt, v.smem, v.ctas_per_sm_adj))) return rc;
     }
-    g_prepared = 1;
+    if (!same) {
+        set_error("SOR kernels: device " + std::to_string(dev) + " differs from device " +
+                  std::to_string(g_first_device) +
+                  " in SM count or kernel occupancy; one GPU model per process is supported");
+        return ZQS_EUNSUPPORTED;
+    }
+    if (first) {
+        g_num_sms = sms;
+        g_first_device = dev;
+    }
+    g_prepared_mask.fetch_or(1ull << dev, std::memory_order_release);
     return ZQS_OK;
 }
 
@@ -1025,6 +1312,148 @@ int sor_variant_info(int i, zqs_sor_variant* out) {
     out->smem_bytes = (int64_t)v.smem;
     out->weights_in_registers = v.wreg;
     out->registers = v.regs;
+    out->x_cells_per_thread = v.xcells;
+    out->reserved = 0;
+    return ZQS_OK;
+}
+
+namespace {
+
+std::mutex g_tune_mu;
+std::map<std::string, SorChoice> g_tune_mem;
+
+// ZQS_TUNE_CACHE names the file ("" disables it); else
+// $XDG_CACHE_HOME/zqs_gb300/sor_tune.txt or $HOME/.cache/zqs_gb300/sor_tune.txt.
+std::string tune_cache_path() {
+    if (const char* e = std::getenv("ZQS_TUNE_CACHE")) return std::string(e);
+    std::string base;
+    if (const char* x = std::getenv("XDG_CACHE_HOME"); x && *x) base = x;
+    else if (const char* h = std::getenv("HOME"); h && *h) base = std::string(h) + "/.cache";
+    return base.empty() ? std::string() : base + "/zqs_gb300/sor_tune.txt";
+}
+
+// The cache key: device name and SM count, grid shape and the registry size
+// (a registry change invalidates older entries).
+std::string tune_key(const Layout& L) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceProp prop;
+    std::string name = "unknown";
+    if (cudaGetDeviceProperties(&prop, dev) == cudaSuccess) name = prop.name;
+    for (char& c : name)
+        if (c == ' ' || c == '|') c = '_';
+    std::ostringstream k;
+    k << name << "|" << g_num_sms << "|" << L.W << "x" << L.H << "x" << L.D << "|r" << kNumVariants;
+    return k.str();
+}
+
+bool choice_usable(const SorChoice& c) {
+    return c.variant >= 0 && c.variant < kNumVariants && g_var[c.variant].ctas_per_sm >= 1 && c.zchunk >= 0;
+}
+
+bool tune_load(const std::string& path, const std::string& key, SorChoice& out) {
+    if (path.empty()) return false;
+    std::ifstream f(path);
+    if (!f) return false;
+    std::string line;
+    bool found = false;
+    while (std::getline(f, line)) {  // the last entry of a key wins
+        std::istringstream is(line);
+        std::string k;
+        SorChoice c;
+        if (is >> k >> c.variant >> c.zchunk >> c.us_per_iter && k == key && choice_usable(c)) {
+            out = c;
+            found = true;
+        }
+    }
+    return found;
+}
+
+void tune_store(const std::string& path, const std::string& key, const SorChoice& c) {
+    if (path.empty()) return;
+    // create the directory chain (best effort: an unwritable cache only costs a re-measure)
+    for (size_t pos = path.find('/', 1); pos != std::string::npos; pos = path.find('/', pos + 1))
+        mkdir(path.substr(0, pos).c_str(), 0755);
+    std::ofstream f(path, std::ios::app);
+    if (f) f << key << " " << c.variant << " " << c.zchunk << " " << c.us_per_iter << "\n";
+}
+
+}  // namespace
+
+int sor_autotune(const DevGrid& g, const KParams& kp, cudaStream_t s, SorChoice& out) {
+    int rc = sor_prepare();
+    if (rc) return rc;
+    const Layout& L = g.L;
+    const std::string key = tune_key(L);
+    const std::string path = tune_cache_path();
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune_mem.find(key);
+        if (it != g_tune_mem.end()) {
+            out = it->second;
+            out.source = 2;
+            return ZQS_OK;
+        }
+        SorChoice c;
+        if (tune_load(path, key, c)) {
+            c.source = 3;
+            g_tune_mem[key] = c;
+            out = c;
+            return ZQS_OK;
+        }
+    }
+    cudaEvent_t a = nullptr, b = nullptr;
+    ZQS_CUDA_TRY(cudaEventCreate(&a));
+    if (cudaEventCreate(&b) != cudaSuccess) {
+        cudaEventDestroy(a);
+        return cuda_fail(cudaErrorUnknown, "sor_autotune: cudaEventCreate");
+    }
+    constexpr int kReps = 3;
+    SorChoice best;
+    float best_us = 1e30f;
+    cudaError_t err = cudaSuccess;
+    for (int vi = 0; vi < kNumVariants && err == cudaSuccess; vi++) {
+        const RbVariant& v = g_var[vi];
+        if (v.ctas_per_sm < 1) continue;
+        std::set<int> zcs = {choose_zc(L, v)};
+        for (int n : {1, 2, 3, 4, 6, 8}) zcs.insert(std::max(1, (L.D + n - 1) / n));
+        for (int zc : zcs) {
+            float* pin = g.p;
+            float* pout = g.p2;
+            err = launch_pass(v, L, pin, pout, g.div, g.flags, kp.omega, kp.om1, zc, s);  // warm-up
+            if (err == cudaSuccess) err = cudaEventRecord(a, s);
+            for (int r = 0; r < kReps && err == cudaSuccess; r++) {
+                std::swap(pin, pout);
+                err = launch_pass(v, L, pin, pout, g.div, g.flags, kp.omega, kp.om1, zc, s);
+            }
+            if (err == cudaSuccess) err = cudaEventRecord(b, s);
+            if (err == cudaSuccess) err = cudaEventSynchronize(b);
+            float ms = 0.0f;
+            if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, a, b);
+            if (err != cudaSuccess) break;
+            const float us = 1000.0f * ms / (kReps * (v.S / 2));
+            if (us < best_us) {
+                best_us = us;
+                best.variant = vi;
+                best.zchunk = zc;
+                best.us_per_iter = us;
+            }
+        }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (err != cudaSuccess) return cuda_fail(err, "sor_autotune");
+    if (!choice_usable(best)) {
+        set_error("sor_autotune: no fused SOR variant fits this device");
+        return ZQS_EUNSUPPORTED;
+    }
+    best.source = 1;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune_mem[key] = best;
+        tune_store(path, key, best);
+    }
+    out = best;
     return ZQS_OK;
 }
 
@@ -1059,7 +1488,7 @@ int launch_project(DevGrid& g, const KParams& kp, int K, const SorConfig& cfg, c
     ZQS_LAUNCH_CHECK("divergence");
     float* cur = g.p;
     float* nxt = g.p2;
-    if (cfg.split || cfg.temporal_depth <= 0) {
+    if (cfg.split) {
         for (int it = 0; it < K; it++) {
             k_sor_colour<<<gc, b, 0, s>>>(L, cur, g.div, g.flags, 0, kp.omega, kp.om1);
             k_sor_colour<<<gc, b, 0, s>>>(L, cur, g.div, g.flags, 1, kp.omega, kp.om1);
@@ -1069,7 +1498,8 @@ int launch_project(DevGrid& g, const KParams& kp, int K, const SorConfig& cfg, c
     } else {
         int rc = sor_prepare();
         if (rc) return rc;
-        int vmain = cfg.variant >= 0 ? cfg.variant : kDefaultVariant[std::min(std::max(cfg.temporal_depth, 1), 4)];
+        const int depth = cfg.temporal_depth > 0 ? cfg.temporal_depth : 2;
+        int vmain = cfg.variant >= 0 ? cfg.variant : kDefaultVariant[std::min(depth, 4)];
         if (vmain >= kNumVariants || g_var[vmain].ctas_per_sm < 1) {
             set_error("SOR variant does not fit this device");
             return ZQS_EUNSUPPORTED;
@@ -1164,6 +1594,12 @@ int launch_project_batch(const BatchLaunch& cell, const BatchLaunch& face, const
     ZQS_LAUNCH_CHECK("k_gradient_batch");
     if (pfin) *pfin = pcur;
     return ZQS_OK;
+}
+
+cudaError_t launch_sor_batch_pass(const SorBatchPlan& plan, int which, const BatchLaunch& B, int pcur,
+                                  cudaStream_t s) {
+    const RbVariant& v = g_var[which == 0 ? plan.vmain : plan.vrem];
+    return v.launch_batch(std::min(plan.slots[which], B.total), B, pcur, which, s);
 }
 
 int launch_sor_adjoint_pairs(const Layout& L, float* q, float* q2, const float* wt, float* acc, float om1,

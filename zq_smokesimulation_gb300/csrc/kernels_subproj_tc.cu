@@ -27,6 +27,7 @@
 // issuing work, waits (bounded) for what it issued, frees its tensor memory
 // and returns; the host reports the flag.
 #include <algorithm>
+#include <atomic>
 #include <cstdint>
 #include <cstring>
 #include <map>
@@ -51,6 +52,7 @@ constexpr int kTileA = kTcM * kTcK * 4;      // 8 KB: one hi or lo tile of X
 constexpr int kSmemBudget = 224 * 1024;       // dynamic: 227 KB less the kernel's static shared memory
 constexpr int kSmemExtra = 1024 + 256;       // alignment slack, barriers, TMEM address
 constexpr long long kWaitLimit = 1LL << 24;  // try_wait polls before a wait gives up
+constexpr long long kInjectWaitLimit = 1LL << 12;  // the same with the stall injected (test hook)
 
 // FP32 -> TF32 (1 + 8 + 10 bits) by round to nearest even, as an FP32 bit pattern.
 __host__ __device__ __forceinline__ uint32_t tf32_rne_bits(uint32_t b) {
@@ -76,8 +78,8 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
 }
 
 // Bounded wait for the completion of the phase with this parity.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-    for (long long n = 0; n < kWaitLimit; n++)
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, long long limit) {
+    for (long long n = 0; n < limit; n++)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
@@ -139,7 +141,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     k_subproj_tc(Layout L, Layout Lc, int s, int rows, int nblocks, int nk, int bn,
                  const unsigned char* __restrict__ Xs, const unsigned char* __restrict__ Ms,
                  const uint8_t* __restrict__ bobs, float* __restrict__ u, float* __restrict__ v,
-                 float* __restrict__ w, int nstages, int* __restrict__ err) {
+                 float* __restrict__ w, int nstages, int* __restrict__ err, long long wait_limit, int stall) {
     extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
     // 1024-byte alignment for the swizzle atoms
     const uint32_t raw = smem_u32(tc_smem_raw);
@@ -193,10 +195,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     const unsigned char* ms = Ms + (size_t)blockIdx.x * nk * bytes_b;
     int produced = 0;  // producer: chunks whose copies were issued
     if (warp == 0 && lane == 0) {
-        for (int j = 0; j < nk; j++) {
+        // stall (test hook): issue nothing, so the MMA lane's first wait runs
+        // out with no copy and no MMA in flight
+        for (int j = 0; j < (stall ? 0 : nk); j++) {
             const int st = j % nstages;
             // the stage's previous chunk (j - nstages) released by its MMAs
-            if (j >= nstages && !mbar_wait(empty + 8 * st, (uint32_t)((j / nstages - 1) & 1))) {
+            if (j >= nstages && !mbar_wait(empty + 8 * st, (uint32_t)((j / nstages - 1) & 1), wait_limit)) {
                 s_fail = 1;
                 break;
             }
@@ -215,7 +219,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         int consumed = 0;
         for (int kc = 0; kc < nk; kc++) {
             const int st = kc % nstages;
-            if (!mbar_wait(full + 8 * st, (uint32_t)((kc / nstages) & 1))) {
+            if (!mbar_wait(full + 8 * st, (uint32_t)((kc / nstages) & 1), wait_limit)) {
                 s_fail = 1;
                 break;
             }
@@ -241,11 +245,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     __syncthreads();
     const bool ok = !s_fail;
     // bounded waits for everything issued, whatever happened
-    if (tid == 0 && !mbar_wait(done, 0u)) s_fail = 1;
+    if (tid == 0 && !mbar_wait(done, 0u, wait_limit)) s_fail = 1;
     if (warp == 0 && lane == 0 && !ok) {
         // copies issued but never consumed still land before the CTA leaves
         for (int j = (produced > nstages ? produced - nstages : 0); j < produced; j++)
-            mbar_wait(full + 8 * (j % nstages), (uint32_t)((j / nstages) & 1));
+            mbar_wait(full + 8 * (j % nstages), (uint32_t)((j / nstages) & 1), wait_limit);
     }
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -374,8 +378,8 @@ int get_msplit(int s, MSplit& out) {
         const int packed = subproj_block_face(P, s, q, 0, 0, 0, comp);
         ft[q] = (uint32_t)packed | ((uint32_t)comp << 24);
     }
-    ZQS_CUDA_TRY(cudaMalloc(&m.img, bytes));
-    cudaError_t e = cudaMalloc(&m.ftab, ft.size() * sizeof(uint32_t));
+    ZQS_CUDA_TRY(dev_alloc(&m.img, bytes));
+    cudaError_t e = dev_alloc(&m.ftab, ft.size() * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMemcpy(m.img, img.data(), bytes, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(m.ftab, ft.data(), ft.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
@@ -409,6 +413,8 @@ size_t subproj_tc_split_bytes(int nblocks, int nf) {
     return (size_t)(2 * bpad * kpad) * sizeof(float);
 }
 
+std::atomic<int> g_tc_stall{0};
+
 int launch_subproj_tc(const Layout& L, const Layout& Lc, int s, int nf, int rows, int nblocks, float* Xsplit,
                       const uint8_t* bobs, float* u, float* v, float* w, int* err, cudaStream_t st,
                       LaunchCounter& lc) {
@@ -437,11 +443,17 @@ int launch_subproj_tc(const Layout& L, const Layout& Lc, int s, int nf, int rows
     unsigned char* Xs = reinterpret_cast<unsigned char*>(Xsplit);
     k_gather_split_tf32<<<(unsigned)bpad, 256, 0, st>>>(L, Lc, s, nf, nblocks, nk, m.ftab, u, v, w, Xs);
     const dim3 grid(m.ntiles, (unsigned)(bpad / kTcM), 1);
+    const int stall = g_tc_stall.load(std::memory_order_relaxed);
     k_subproj_tc<<<grid, kTcThreads, smem, st>>>(L, Lc, s, rows, nblocks, nk, m.bn, Xs, m.img, bobs, u, v, w,
-                                                 nstages, err);
+                                                 nstages, err, stall ? kInjectWaitLimit : kWaitLimit, stall);
     lc.n += 2;
     ZQS_LAUNCH_CHECK("k_subproj_tc");
     return ZQS_OK;
 }
 
 }  // namespace zqs
+
+extern "C" ZQS_API int zqs_debug_inject_tc_stall(int enable) {
+    zqs::g_tc_stall.store(enable ? 1 : 0, std::memory_order_relaxed);
+    return ZQS_OK;
+}

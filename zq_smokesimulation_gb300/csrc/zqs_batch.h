@@ -66,6 +66,10 @@ struct SorBatchPlan {
 };
 int sor_batch_plan(int variant, SorBatchPlan& out);  // variant -1: the batch default
 bool sor_variant_batchable(int variant);
+// One fused SOR pass of kind `which` (0: main variant, 1: remainder) over the
+// tile list B, pressure p[pcur] -> p[pcur ^ 1] of every instance (the tuner's probe).
+cudaError_t launch_sor_batch_pass(const SorBatchPlan& plan, int which, const BatchLaunch& B, int pcur,
+                                  cudaStream_t s);
 
 int launch_force_batch(const BatchLaunch& cell, const BatchLaunch& face, int vcur, int scur, int blocks,
                        cudaStream_t s, LaunchCounter& lc);

@@ -2,6 +2,7 @@
 // (capi.cpp) and the batched runner (batch.cpp).  Not installed.
 #pragma once
 
+#include <cstdlib>
 #include <utility>
 
 #include "zqs_internal.h"
@@ -18,7 +19,10 @@ struct zqs_grid {
     bool has_occ = false;
     KParams kp{};
     SourceList src{};
-    SorConfig sor{2, 0};
+    SorConfig sor{};               // as configured (temporal_depth 0: the tuned variant)
+    SorConfig sor_eff{};           // as launched: sor with the tuned variant filled in
+    SorChoice tuned{};             // sor_autotune's result for this grid's shape
+    bool tune_done = false;
     float* p_last = nullptr;
     bool use_graph = true;
     cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -67,6 +71,33 @@ struct zqs_grid {
         }
         return ZQS_OK;
     }
+    // The SOR configuration to launch.  With temporal_depth 0 and no explicit
+    // variant the tuned variant and z chunk are used; the tuner runs on the
+    // first call that is not inside a stream capture (it synchronises s), and
+    // ZQS_AUTOTUNE=0 in the environment keeps the static default instead.
+    int resolve_sor(cudaStream_t s) {
+        sor_eff = sor;
+        if (sor.split || sor.temporal_depth != 0 || sor.variant >= 0) return ZQS_OK;
+        // no fine-grid SOR to tune (coarse solver, or no iterations yet)
+        if (params.solver == ZQS_SOLVER_COARSE_OPEN || params.sor_iters == 0) return ZQS_OK;
+        if (!tune_done) {
+            const char* env = std::getenv("ZQS_AUTOTUNE");
+            cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+            if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) cs = cudaStreamCaptureStatusActive;
+            if (env && env[0] == '0') {
+                tune_done = true;  // static default
+            } else if (cs == cudaStreamCaptureStatusNone) {
+                int rc = sor_autotune(g, kp, s, tuned);
+                if (rc) return rc;
+                tune_done = true;
+            }
+        }
+        if (tuned.variant >= 0) {
+            sor_eff.variant = tuned.variant;
+            sor_eff.zchunk = tuned.zchunk;
+        }
+        return ZQS_OK;
+    }
     // The launches of one step, issued on stream s (captured or direct).
     int issue_step(cudaStream_t s, LaunchCounter& lc) {
         int rc = launch_force(g, kp, true, s, lc);
@@ -74,7 +105,7 @@ struct zqs_grid {
         rc = launch_advect_velocity(g, kp, params.adv_vel_mode, true, s, lc);
         if (rc) return rc;
         swap_velocity();
-        rc = launch_project(g, kp, params.sor_iters, sor, s, lc, &p_last);
+        rc = launch_project(g, kp, params.sor_iters, sor_eff, s, lc, &p_last);
         if (rc) return rc;
         rc = launch_advect_scalar(g, kp, params.adv_sca_mode, true, &src, s, lc);
         if (rc) return rc;

@@ -87,6 +87,15 @@ struct DevGrid {
     CoarseState* coarse = nullptr;  // ZQS_SOLVER_COARSE_OPEN state (owned by the grid handle)
 };
 
+// ---- device allocation -----------------------------------------------------
+// Every device allocation of the library goes through dev_alloc, so the test
+// hook zqs_debug_fail_alloc can make a chosen one fail as out-of-memory.
+cudaError_t dev_alloc_raw(void** p, size_t bytes);
+template <class T>
+inline cudaError_t dev_alloc(T** p, size_t bytes) {
+    return dev_alloc_raw(reinterpret_cast<void**>(p), bytes);
+}
+
 // ---- error reporting -------------------------------------------------------
 void set_error(const std::string& msg);
 int cuda_fail(cudaError_t e, const char* what);
@@ -128,16 +137,31 @@ int launch_advect_scalar(const DevGrid& g, const KParams& kp, int mode, bool fol
 int launch_reinject(const DevGrid& g, const SourceList& src, cudaStream_t s, LaunchCounter& lc);
 
 struct SorConfig {
-    int temporal_depth = 2;  // iterations per fused pass (>=1)
+    int temporal_depth = 0;  // iterations per fused pass; 0: the tuned variant (launch_project
+                             // itself falls back to the depth-2 default when nothing was tuned)
     int split = 0;           // 1: one launch per colour (plain kernel)
     int variant = -1;        // fused kernel variant (-1: default for the depth)
     int zchunk = 0;          // z planes per CTA (0: chosen from the grid)
 };
 int sor_variant_count();
 int sor_variant_info(int i, zqs_sor_variant* out);
+
+// Per grid shape and device: the fused SOR variant and z chunk with the
+// shortest measured time per iteration.  Times every variant that fits, at a
+// few z chunks each, on the grid's own pressure, divergence and flags
+// buffers (the pressure is overwritten: call it where the next projection
+// starts from p = 0 anyway); synchronises the stream, so never inside a
+// stream capture.  Results are kept in memory and in an on-disk file.
+struct SorChoice {
+    int variant = -1;
+    int zchunk = 0;
+    float us_per_iter = 0.0f;
+    int source = 0;  // 0 none, 1 measured now, 2 this process's cache, 3 the on-disk cache
+};
+int sor_autotune(const DevGrid& g, const KParams& kp, cudaStream_t s, SorChoice& out);
 int launch_project(DevGrid& g, const KParams& kp, int K, const SorConfig& cfg, cudaStream_t s,
                    LaunchCounter& lc, float** p_final);
-int sor_prepare();  // sets kernel attributes once per process (outside any capture)
+int sor_prepare();  // sets the SOR kernels' attributes once per device (outside any capture)
 int launch_stats(const DevGrid& g, const KParams& kp, const float* p, zqs_stats* out, cudaStream_t s);
 
 }  // namespace zqs
