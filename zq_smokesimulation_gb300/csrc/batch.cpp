@@ -11,6 +11,8 @@
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -53,6 +55,30 @@ struct zqs_batch {
         }
     }
 };
+
+namespace zqs {
+
+int persistent_blocks(const void* kernel, int threads, size_t dyn_smem, int cap) {
+    static std::mutex mu;
+    static std::map<std::pair<const void*, int>, int> resident;  // (kernel, device) -> blocks
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return std::max(1, cap);
+    std::lock_guard<std::mutex> lk(mu);
+    const auto key = std::make_pair(kernel, dev);
+    auto it = resident.find(key);
+    if (it == resident.end()) {
+        int per_sm = 0, sms = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, dyn_smem) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+            cudaGetLastError();
+            return std::max(1, cap);
+        }
+        it = resident.emplace(key, std::max(1, per_sm) * std::max(1, sms)).first;
+    }
+    return std::max(1, std::min(cap, it->second));
+}
+
+}  // namespace zqs
 
 namespace {
 
@@ -359,7 +385,7 @@ ZQS_API int zqs_batch_create(zqs_batch** out, zqs_grid* const* grids, int n) {
         delete b;
         return cuda_fail(e, "zqs_batch_create");
     }
-    b->blocks = std::max(1, sms) * 8;  // 8 resident 256-thread CTAs per SM
+    b->blocks = std::max(1, sms) * 8;  // at most 8 resident 256-thread CTAs per SM (persistent_blocks)
     rc = build_table(b);
     if (rc) {
         if (b->dev) cudaFree(b->dev);

@@ -530,7 +530,8 @@ ZQS_API int zqs_grid_get_sor_choice(zqs_grid* g, int* variant, int* zchunk, floa
     if (rc) return rc;
     rc = g->resolve_sor(g->pick(stream));
     if (rc) return rc;
-    if (variant) *variant = g->sor_eff.split ? -1 : g->sor_eff.variant;
+    const SorConfig& e = g->sor_eff;
+    if (variant) *variant = e.split ? -1 : (e.variant >= 0 ? e.variant : sor_default_variant(e.temporal_depth));
     if (zchunk) *zchunk = g->sor_eff.zchunk;
     if (us_per_iter) *us_per_iter = (g->sor_eff.variant == g->tuned.variant) ? g->tuned.us_per_iter : 0.0f;
     return ZQS_OK;

@@ -531,7 +531,8 @@ int launch_advect_scalar(const DevGrid& g, const KParams& kp, int mode, bool fol
 
 int launch_mac_quads_batch(const BatchLaunch& face, int vcur, int blocks, cudaStream_t s, LaunchCounter& lc) {
     dim3 b(32, 8, 1);
-    k_mac_quads_batch<<<std::min(blocks, face.total), b, 0, s>>>(face, vcur);
+    k_mac_quads_batch<<<persistent_blocks((const void*)k_mac_quads_batch, 256, 0, std::min(blocks, face.total)), b, 0,
+                        s>>>(face, vcur);
     lc.n++;
     ZQS_LAUNCH_CHECK("k_mac_quads_batch");
     return ZQS_OK;
@@ -539,7 +540,8 @@ int launch_mac_quads_batch(const BatchLaunch& face, int vcur, int blocks, cudaSt
 
 int launch_advect_velocity_batch(const BatchLaunch& advf, int vcur, int blocks, cudaStream_t s, LaunchCounter& lc) {
     dim3 b(32, 8, 1);
-    k_advect_vel_batch<<<std::min(blocks, advf.total), b, 0, s>>>(advf, vcur);
+    k_advect_vel_batch<<<persistent_blocks((const void*)k_advect_vel_batch, 256, 0, std::min(blocks, advf.total)), b, 0,
+                         s>>>(advf, vcur);
     lc.n++;
     ZQS_LAUNCH_CHECK("k_advect_vel_batch");
     return ZQS_OK;
@@ -548,7 +550,8 @@ int launch_advect_velocity_batch(const BatchLaunch& advf, int vcur, int blocks, 
 int launch_advect_scalar_batch(const BatchLaunch& cell, int vcur, int scur, int blocks, cudaStream_t s,
                                LaunchCounter& lc) {
     dim3 b(32, 8, 1);
-    k_advect_scalar_batch<<<std::min(blocks, cell.total), b, 0, s>>>(cell, vcur, scur);
+    k_advect_scalar_batch<<<persistent_blocks((const void*)k_advect_scalar_batch, 256, 0, std::min(blocks, cell.total)), b, 0,
+                            s>>>(cell, vcur, scur);
     lc.n++;
     ZQS_LAUNCH_CHECK("k_advect_scalar_batch");
     return ZQS_OK;

@@ -245,9 +245,12 @@ int launch_attenuate(const DevGrid& g, const KParams& kp, cudaStream_t s, Launch
 int launch_force_batch(const BatchLaunch& cell, const BatchLaunch& face, int vcur, int scur, int blocks,
                        cudaStream_t s, LaunchCounter& lc) {
     dim3 b(32, 8, 1);
-    k_vorticity_batch<<<std::min(blocks, cell.total), b, 0, s>>>(cell, vcur);
-    k_force_cell_batch<<<std::min(blocks, cell.total), b, 0, s>>>(cell, scur);
-    k_force_faces_batch<<<std::min(blocks, face.total), b, 0, s>>>(face, vcur);
+    k_vorticity_batch<<<persistent_blocks((const void*)k_vorticity_batch, 256, 0, std::min(blocks, cell.total)), b, 0,
+                        s>>>(cell, vcur);
+    k_force_cell_batch<<<persistent_blocks((const void*)k_force_cell_batch, 256, 0, std::min(blocks, cell.total)), b, 0,
+                         s>>>(cell, scur);
+    k_force_faces_batch<<<persistent_blocks((const void*)k_force_faces_batch, 256, 0, std::min(blocks, face.total)), b, 0,
+                          s>>>(face, vcur);
     lc.n += 3;
     ZQS_LAUNCH_CHECK("batched force kernels");
     return ZQS_OK;

@@ -1295,6 +1295,8 @@ int sor_prepare() {
 
 int sor_variant_count() { return kNumVariants; }
 
+int sor_default_variant(int depth) { return kDefaultVariant[depth <= 0 ? 2 : std::min(depth, 4)]; }
+
 int sor_variant_info(int i, zqs_sor_variant* out) {
     if (i < 0 || i >= kNumVariants || !out) {
         set_error("sor variant index out of range");
@@ -1567,11 +1569,13 @@ int launch_project_batch(const BatchLaunch& cell, const BatchLaunch& face, const
                          const BatchLaunch& sorr, const SorBatchPlan& plan, int K, bool any_closed, int vcur,
                          int blocks, cudaStream_t s, LaunchCounter& lc, int* pfin) {
     dim3 b(32, 8, 1);
-    k_divergence_batch<<<std::min(blocks, cell.total), b, 0, s>>>(cell, vcur);
+    k_divergence_batch<<<persistent_blocks((const void*)k_divergence_batch, 256, 0, std::min(blocks, cell.total)), b, 0,
+                         s>>>(cell, vcur);
     lc.n++;
     if (any_closed) {
         k_reduce_mean_batch<<<cell.n, 256, 0, s>>>(cell.desc, cell.pre);
-        k_div_subtract_batch<<<std::min(blocks, cell.total), b, 0, s>>>(cell);
+        k_div_subtract_batch<<<persistent_blocks((const void*)k_div_subtract_batch, 256, 0, std::min(blocks, cell.total)), b, 0,
+                               s>>>(cell);
         lc.n += 2;
     }
     ZQS_LAUNCH_CHECK("batched divergence");
@@ -1589,7 +1593,8 @@ int launch_project_batch(const BatchLaunch& cell, const BatchLaunch& face, const
         pcur ^= 1;
         remaining -= d;
     }
-    k_gradient_batch<<<std::min(blocks, face.total), b, 0, s>>>(face, vcur, pcur);
+    k_gradient_batch<<<persistent_blocks((const void*)k_gradient_batch, 256, 0, std::min(blocks, face.total)), b, 0,
+                       s>>>(face, vcur, pcur);
     lc.n++;
     ZQS_LAUNCH_CHECK("k_gradient_batch");
     if (pfin) *pfin = pcur;

@@ -64,6 +64,11 @@ struct SorBatchPlan {
     int S[2] = {0, 0}, TX[2] = {0, 0}, TY[2] = {0, 0};
     int slots[2] = {0, 0};  // resident CTAs on the device (SMs x CTAs per SM)
 };
+// Blocks of a persistent batched launch: as many as are resident on the
+// device at once for this kernel (its occupancy x SM count), at most cap.  A
+// larger grid would leave blocks waiting for whole tile lists of others.
+int persistent_blocks(const void* kernel, int threads, size_t dyn_smem, int cap);
+
 int sor_batch_plan(int variant, SorBatchPlan& out);  // variant -1: the batch default
 bool sor_variant_batchable(int variant);
 // One fused SOR pass of kind `which` (0: main variant, 1: remainder) over the

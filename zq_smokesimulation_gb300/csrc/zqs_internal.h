@@ -145,6 +145,7 @@ struct SorConfig {
 };
 int sor_variant_count();
 int sor_variant_info(int i, zqs_sor_variant* out);
+int sor_default_variant(int depth);  // the fixed variant launch_project uses for a depth (0: 2)
 
 // Per grid shape and device: the fused SOR variant and z chunk with the
 // shortest measured time per iteration.  Times every variant that fits, at a
