@@ -384,6 +384,10 @@ ZQS_API int zqs_adjoint_backward(zqs_adjoint* a, const float* g_density, float* 
     rc = launch_adj_weights(L, w->g.flags, w->kp.omega, b.wt, s, lc);
     if (rc) return rc;
     const int K = g->params.sor_iters;
+    if (K > 1) {  // before the first capture; q, q2 and acc are set up again by every reversed step
+        rc = sor_adj_autotune(L, b.q, b.q2, b.wt, b.acc, w->kp.om1, s);
+        if (rc) return rc;
+    }
     for (int sg = a->ncp - 1; sg >= 0; sg--) {
         const int s0 = sg * a->every;
         const int s1 = std::min(s0 + a->every, a->nsteps);

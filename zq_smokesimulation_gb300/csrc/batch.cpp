@@ -29,6 +29,8 @@ struct zqs_batch {
     size_t dev_bytes = 0;
     InstDesc* d_desc = nullptr;
     int* d_pre[TC_COUNT] = {};
+    std::vector<int> h_pre[TC_COUNT];   // host copies of the prefix arrays
+    std::vector<AdvHotTable> hot;       // advection parameter tables, kAdvHotMax instances each
     int total[TC_COUNT] = {};
     int n = 0;
     int K = 0;
@@ -234,7 +236,35 @@ int build_table_for(zqs_batch* b, int variant) {
             pre[c][r + 1] = (int)next;
         }
     }
-    for (int c = 0; c < TC_COUNT; c++) b->total[c] = pre[c][n];
+    for (int c = 0; c < TC_COUNT; c++) {
+        b->total[c] = pre[c][n];
+        b->h_pre[c] = pre[c];
+    }
+    // the advection kernels' parameter tables, one per chunk of instances
+    b->hot.clear();
+    for (int c0 = 0; c0 < n; c0 += kAdvHotMax) {
+        b->hot.emplace_back();
+        AdvHotTable& T = b->hot.back();
+        memset(&T, 0, sizeof(T));
+        T.base = c0;
+        T.n = std::min(kAdvHotMax, n - c0);
+        for (int q = 0; q < T.n; q++) {
+            const InstDesc& d = b->h_desc[c0 + q];
+            AdvHot& a = T.h[q];
+            a.L = d.L;
+            a.kp = d.kp;
+            for (int m = 0; m < 3; m++) {
+                a.q[m] = d.q4[m];
+                a.vel[0][m] = d.vel[0][m];
+                a.vel[1][m] = d.vel[1][m];
+            }
+            a.flags = d.flags;
+            for (int m = 0; m < 2; m++) {
+                a.sca[0][m] = d.sca[0][m];
+                a.sca[1][m] = d.sca[1][m];
+            }
+        }
+    }
 
     // one device block: descriptors, then the prefix arrays
     const size_t desc_bytes = ((sizeof(InstDesc) * n + 255) / 256) * 256;
@@ -333,19 +363,20 @@ bool table_current(const zqs_batch* b) {
 
 int issue_batch_step(zqs_batch* b, int par, cudaStream_t s, LaunchCounter& lc, int* pfin) {
     BatchLaunch bl[TC_COUNT];
-    for (int c = 0; c < TC_COUNT; c++) bl[c] = BatchLaunch{b->d_desc, b->d_pre[c], b->n, b->total[c]};
+    for (int c = 0; c < TC_COUNT; c++)
+        bl[c] = BatchLaunch{b->d_desc, b->d_pre[c], b->n, b->total[c], b->h_pre[c].data()};
     int rc = launch_force_batch(bl[TC_CELL], bl[TC_FACE], par, par, b->blocks, s, lc);
     if (rc) return rc;
     rc = launch_mac_quads_batch(bl[TC_FACE], par, b->blocks, s, lc);
     if (rc) return rc;
-    rc = launch_advect_velocity_batch(bl[TC_ADVF], par, b->blocks, s, lc);
+    rc = launch_advect_velocity_batch(bl[TC_ADVF], b->hot, par, b->blocks, s, lc);
     if (rc) return rc;
     rc = launch_project_batch(bl[TC_CELL], bl[TC_FACE], bl[TC_SORM], bl[TC_SORR], b->plan, b->K, b->any_closed,
                               par ^ 1, b->blocks, s, lc, pfin);
     if (rc) return rc;
     rc = launch_mac_quads_batch(bl[TC_FACE], par ^ 1, b->blocks, s, lc);
     if (rc) return rc;
-    return launch_advect_scalar_batch(bl[TC_CELL], par ^ 1, par, b->blocks, s, lc);
+    return launch_advect_scalar_batch(bl[TC_CELL], b->hot, par ^ 1, par, b->blocks, s, lc);
 }
 
 }  // namespace

@@ -305,39 +305,45 @@ __global__ void __launch_bounds__(256) k_mac_quads_batch(BatchLaunch B, int vcur
     }
 }
 
-__global__ void __launch_bounds__(256) k_advect_vel_batch(BatchLaunch B, int vcur) {
-    for (int t = blockIdx.x; t < B.total; t += gridDim.x) {
+static_assert(sizeof(AdvHotTable) + 64 <= 32764, "the hot table must fit the kernel parameter space");
+
+// Batched velocity advection over the tiles [t0, t1) of one table chunk
+// (launched with one CTA per tile; the loop also serves smaller grids).
+__global__ void __launch_bounds__(256, 5) k_advect_vel_batch(BatchLaunch B, const __grid_constant__ AdvHotTable T,
+                                                         int vcur, int t0, int t1) {
+    for (int t = t0 + blockIdx.x; t < t1; t += gridDim.x) {
         const int i = batch_find(B.pre, B.n, t);
-        const InstDesc& d = B.desc[i];
+        const AdvHot& d = T.h[i - T.base];
         const int lt = t - __ldg(B.pre + i);
         const int gx = (d.L.W + 1 + 31) / 32, gy = (d.L.H + 1 + 7) / 8;
         const int bx = lt % gx, r = lt / gx, by = r % gy, bz = r / gy;
-        const KParams kp = d.kp;
         const int nxt = vcur ^ 1;
         VelPass P;
         for (int m = 0; m < 3; m++) {
-            P.q[m] = d.q4[m];
+            P.q[m] = d.q[m];
             P.in[m] = d.vel[vcur][m];
             P.keep[m] = d.vel[vcur][m];
             P.out[m] = d.vel[nxt][m];
         }
-        P.vel4 = P.in4 = d.t4a;
-        advect_vel_macout_tile<false, false, false, false>(d.L, P, d.flags, kp, 1, bx, by, bz);
+        P.vel4 = P.in4 = nullptr;  // MAC velocity only
+        advect_vel_macout_tile<false, false, false, false>(d.L, P, d.flags, d.kp, 1, bx, by, bz);
     }
 }
 
-__global__ void __launch_bounds__(256) k_advect_scalar_batch(BatchLaunch B, int vcur, int scur) {
-    for (int t = blockIdx.x; t < B.total; t += gridDim.x) {
+// Batched scalar advection (+ attenuation, + reinjection) over the tiles
+// [t0, t1) of one table chunk; the sources come from the instance descriptor.
+__global__ void __launch_bounds__(256, 5) k_advect_scalar_batch(BatchLaunch B, const __grid_constant__ AdvHotTable T,
+                                                            int vcur, int scur, int t0, int t1) {
+    for (int t = t0 + blockIdx.x; t < t1; t += gridDim.x) {
         const int i = batch_find(B.pre, B.n, t);
-        const InstDesc& d = B.desc[i];
+        const AdvHot& d = T.h[i - T.base];
         const int lt = t - __ldg(B.pre + i);
         const int gx = (d.L.W + 31) / 32, gy = (d.L.H + 7) / 8;
         const int bx = lt % gx, r = lt / gx, by = r % gy, bz = r / gy;
-        const KParams kp = d.kp;
         const int nxt = scur ^ 1;
-        const float4* q[3] = {d.q4[0], d.q4[1], d.q4[2]};
-        advect_scalar_tile<false>(d.L, d.t4a, q, d.flags, d.sca[scur][0], d.sca[scur][1], d.sca[nxt][0],
-                                  d.sca[nxt][1], kp, kp.temp_atten, kp.dens_atten, d.src, bx, by, bz);
+        advect_scalar_tile<false>(d.L, nullptr, d.q, d.flags, d.sca[scur][0], d.sca[scur][1], d.sca[nxt][0],
+                                  d.sca[nxt][1], d.kp, d.kp.temp_atten, d.kp.dens_atten, B.desc[i].src, bx, by,
+                                  bz);
     }
 }
 
@@ -538,21 +544,32 @@ int launch_mac_quads_batch(const BatchLaunch& face, int vcur, int blocks, cudaSt
     return ZQS_OK;
 }
 
-int launch_advect_velocity_batch(const BatchLaunch& advf, int vcur, int blocks, cudaStream_t s, LaunchCounter& lc) {
+int launch_advect_velocity_batch(const BatchLaunch& advf, const std::vector<AdvHotTable>& hot, int vcur,
+                                 int blocks, cudaStream_t s, LaunchCounter& lc) {
     dim3 b(32, 8, 1);
-    k_advect_vel_batch<<<persistent_blocks((const void*)k_advect_vel_batch, 256, 0, std::min(blocks, advf.total)), b, 0,
-                         s>>>(advf, vcur);
-    lc.n++;
+    for (const AdvHotTable& T : hot) {
+        const int t0 = advf.pre_host[T.base], t1 = advf.pre_host[T.base + T.n];
+        if (t1 <= t0) continue;
+        // one CTA per tile: backtrace costs vary across tiles (plume against
+        // still air), and the block scheduler balances them as CTAs finish
+        k_advect_vel_batch<<<t1 - t0, b, 0, s>>>(advf, T, vcur, t0, t1);
+        (void)blocks;
+        lc.n++;
+    }
     ZQS_LAUNCH_CHECK("k_advect_vel_batch");
     return ZQS_OK;
 }
 
-int launch_advect_scalar_batch(const BatchLaunch& cell, int vcur, int scur, int blocks, cudaStream_t s,
-                               LaunchCounter& lc) {
+int launch_advect_scalar_batch(const BatchLaunch& cell, const std::vector<AdvHotTable>& hot, int vcur, int scur,
+                               int blocks, cudaStream_t s, LaunchCounter& lc) {
     dim3 b(32, 8, 1);
-    k_advect_scalar_batch<<<persistent_blocks((const void*)k_advect_scalar_batch, 256, 0, std::min(blocks, cell.total)), b, 0,
-                            s>>>(cell, vcur, scur);
-    lc.n++;
+    for (const AdvHotTable& T : hot) {
+        const int t0 = cell.pre_host[T.base], t1 = cell.pre_host[T.base + T.n];
+        if (t1 <= t0) continue;
+        k_advect_scalar_batch<<<t1 - t0, b, 0, s>>>(cell, T, vcur, scur, t0, t1);  // one CTA per tile
+        (void)blocks;
+        lc.n++;
+    }
     ZQS_LAUNCH_CHECK("k_advect_scalar_batch");
     return ZQS_OK;
 }

@@ -1607,12 +1607,73 @@ cudaError_t launch_sor_batch_pass(const SorBatchPlan& plan, int which, const Bat
     return v.launch_batch(std::min(plan.slots[which], B.total), B, pcur, which, s);
 }
 
+namespace {
+std::map<std::string, int> g_adj_tuned;  // (device, shape) -> variant of the reversed SOR's main pass (g_tune_mu)
+
+cudaError_t adj_pass(const RbVariant& v, const Layout& L, const float* qin, float* qout, const float* wt, float* acc,
+                     float om1, cudaStream_t s) {
+    RbVariant occ = v;
+    occ.ctas_per_sm = v.ctas_per_sm_adj;
+    const int zc = choose_zc(L, occ);
+    dim3 gr((L.W + v.TX - 1) / v.TX, (L.H + v.TY - 1) / v.TY, (L.D + zc - 1) / zc);
+    return v.launch_adj(gr, L, qin, qout, wt, acc, om1, zc, s);
+}
+}  // namespace
+
+int sor_adj_autotune(const Layout& L, float* q, float* q2, const float* wt, float* acc, float om1, cudaStream_t s) {
+    int rc = sor_prepare();
+    if (rc) return rc;
+    const char* env = std::getenv("ZQS_AUTOTUNE");
+    if (env && env[0] == '0') return ZQS_OK;
+    const std::string key = tune_key(L);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        if (g_adj_tuned.count(key)) return ZQS_OK;
+    }
+    cudaEvent_t a = nullptr, b = nullptr;
+    ZQS_CUDA_TRY(cudaEventCreate(&a));
+    if (cudaEventCreate(&b) != cudaSuccess) {
+        cudaEventDestroy(a);
+        return cuda_fail(cudaErrorUnknown, "sor_adj_autotune: cudaEventCreate");
+    }
+    int best = -1;
+    float best_us = 1e30f;
+    cudaError_t err = cudaSuccess;
+    for (int vi = 0; vi < kNumVariants && err == cudaSuccess; vi++) {
+        const RbVariant& v = g_var[vi];
+        if (!v.launch_adj || v.ctas_per_sm_adj < 1 || v.S != 4) continue;
+        err = adj_pass(v, L, q, q2, wt, acc, om1, s);  // warm-up
+        if (err == cudaSuccess) err = cudaEventRecord(a, s);
+        for (int r = 0; r < 3 && err == cudaSuccess; r++)
+            err = adj_pass(v, L, (r & 1) ? q2 : q, (r & 1) ? q : q2, wt, acc, om1, s);
+        if (err == cudaSuccess) err = cudaEventRecord(b, s);
+        if (err == cudaSuccess) err = cudaEventSynchronize(b);
+        float ms = 0.0f;
+        if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, a, b);
+        if (err == cudaSuccess && ms < best_us) {
+            best_us = ms;
+            best = vi;
+        }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (err != cudaSuccess) return cuda_fail(err, "sor_adj_autotune");
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    if (best >= 0) g_adj_tuned[key] = best;
+    return ZQS_OK;
+}
+
 int launch_sor_adjoint_pairs(const Layout& L, float* q, float* q2, const float* wt, float* acc, float om1,
                              int npairs, cudaStream_t s, LaunchCounter& lc, float** qcur) {
     int rc = sor_prepare();
     if (rc) return rc;
     auto fits = [](int i) { return g_var[i].launch_adj && g_var[i].ctas_per_sm_adj > 0; };
     int vmain = -1, vrem = -1;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_adj_tuned.find(tune_key(L));
+        if (it != g_adj_tuned.end() && fits(it->second)) vmain = it->second;
+    }
     for (int i : kAdjVariants)
         if (vmain < 0 && fits(i) && g_var[i].S == 4) vmain = i;
     for (int i : kAdjVariants)
@@ -1629,11 +1690,7 @@ int launch_sor_adjoint_pairs(const Layout& L, float* q, float* q2, const float* 
         const int dmain = g_var[vmain].S / 2;
         const RbVariant& v = remaining >= dmain ? g_var[vmain] : g_var[vrem];
         const int d = v.S / 2;
-        RbVariant occ = v;
-        occ.ctas_per_sm = v.ctas_per_sm_adj;
-        const int zc = choose_zc(L, occ);
-        dim3 gr((L.W + v.TX - 1) / v.TX, (L.H + v.TY - 1) / v.TY, (L.D + zc - 1) / zc);
-        cudaError_t e = v.launch_adj(gr, L, cur, nxt, wt, acc, om1, zc, s);
+        cudaError_t e = adj_pass(v, L, cur, nxt, wt, acc, om1, s);
         if (e != cudaSuccess) return cuda_fail(e, "k_sor_reg_adj");
         lc.n++;
         std::swap(cur, nxt);

@@ -58,6 +58,11 @@ int launch_adj_weights(const Layout& L, const uint8_t* flags, float omega, float
 // (register-column kernel, ADJ form); q and q2 ping-pong, *qcur = result.
 int launch_sor_adjoint_pairs(const Layout& L, float* q, float* q2, const float* wt, float* acc, float om1,
                              int npairs, cudaStream_t s, LaunchCounter& lc, float** qcur);
+// Once per (device, shape): time the ADJ forms of the depth-2 variants on
+// these buffers (q, q2 and acc are overwritten) and keep the fastest for
+// launch_sor_adjoint_pairs; synchronises s, never inside a capture.
+// ZQS_AUTOTUNE=0 keeps the fixed order.
+int sor_adj_autotune(const Layout& L, float* q, float* q2, const float* wt, float* acc, float om1, cudaStream_t s);
 int launch_adj_step(const Layout& L, const AdjFwd& f, const AdjBufs& b, const KParams& kp, const SourceList& src,
                     int K, cudaStream_t s, LaunchCounter& lc);
 

@@ -8,6 +8,8 @@
 // single-grid kernel runs, on that instance's buffers and parameters.
 #pragma once
 
+#include <vector>
+
 #include "zqs_internal.h"
 
 namespace zqs {
@@ -50,11 +52,33 @@ __device__ __forceinline__ int batch_find(const int* __restrict__ pre, int n, in
     return lo;
 }
 
+// The fields the batched advection kernels read inside their backtrace loops,
+// for a chunk of consecutive instances, passed by value in the kernels'
+// parameter space: loop invariants (extents, pitches, step sizes, buffer
+// pointers) are then constant-bank operands, as in the single-grid kernels,
+// rather than registers loaded from the descriptor in global memory, which
+// cost the batched kernels occupancy.
+struct AdvHot {
+    Layout L;
+    KParams kp;
+    const float4* q[3];   // quad copies of the current velocity
+    const uint8_t* flags;
+    float* vel[2][3];     // velocity ping-pong
+    float* sca[2][2];     // scalar ping-pong
+};
+constexpr int kAdvHotMax = 96;  // instances per table (the parameter space holds 32 KB)
+struct AdvHotTable {
+    int base;  // first instance (table row) of the chunk
+    int n;     // instances in the chunk
+    AdvHot h[kAdvHotMax];
+};
+
 struct BatchLaunch {
     const InstDesc* desc;  // device array of n descriptors
     const int* pre;        // device prefix array (n+1) of the launch's tile class
     int n;
     int total;             // pre[n]
+    const int* pre_host = nullptr;  // host copy of pre (launch ranges of table chunks)
 };
 
 // SOR plan of a batch: the main fused variant (depth S/2) and the variant that
@@ -79,9 +103,11 @@ cudaError_t launch_sor_batch_pass(const SorBatchPlan& plan, int which, const Bat
 int launch_force_batch(const BatchLaunch& cell, const BatchLaunch& face, int vcur, int scur, int blocks,
                        cudaStream_t s, LaunchCounter& lc);
 int launch_mac_quads_batch(const BatchLaunch& face, int vcur, int blocks, cudaStream_t s, LaunchCounter& lc);
-int launch_advect_velocity_batch(const BatchLaunch& advf, int vcur, int blocks, cudaStream_t s, LaunchCounter& lc);
-int launch_advect_scalar_batch(const BatchLaunch& cell, int vcur, int scur, int blocks, cudaStream_t s,
-                               LaunchCounter& lc);
+// One launch per table chunk, over the chunk's tiles [pre[base], pre[base + n]).
+int launch_advect_velocity_batch(const BatchLaunch& advf, const std::vector<AdvHotTable>& hot, int vcur,
+                                 int blocks, cudaStream_t s, LaunchCounter& lc);
+int launch_advect_scalar_batch(const BatchLaunch& cell, const std::vector<AdvHotTable>& hot, int vcur, int scur,
+                               int blocks, cudaStream_t s, LaunchCounter& lc);
 // Divergence (+ closed-solver mean removal), K SOR iterations, gradient on the
 // velocity buffer vcur; *pfin receives the pressure buffer holding the result.
 int launch_project_batch(const BatchLaunch& cell, const BatchLaunch& face, const BatchLaunch& sorm,
