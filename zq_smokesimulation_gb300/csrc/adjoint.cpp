@@ -11,8 +11,8 @@
 // vorticity are recomputed from its start state with the forward force
 // kernels, the end state gives the projected velocity, and launch_adj_step
 // runs the adjoint kernels (kernels_adjoint.cu).  Memory: (nsteps/k + 1) + k
-// state slots of 5 padded fields, about 25 padded fields of adjoint buffers,
-// and one work grid.
+// state slots of 5 padded fields, about 76 padded float fields of adjoint
+// buffers (20 float, 14 float4), and one work grid.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -113,6 +113,8 @@ struct zqs_adjoint {
     // fix1 = velocity at the end of the step; t4a/t4b = vorticity and force
     Slot fix0, fix1;
     float4 *t4a = nullptr, *t4b = nullptr;
+    float4* q4[3] = {};  // quad copies of fix1's velocity
+    float4* q2[3] = {};  // quad copies of the advection input (fix0's velocity after the force stage)
     cudaGraphExec_t graph = nullptr;
     long long graph_gen = -1;
     long long graph_launches = 0;
@@ -137,6 +139,19 @@ int issue_adj_step(zqs_adjoint* a, int K, cudaStream_t s, LaunchCounter& lc) {
     view.t4b = a->t4b;
     int rc = launch_force(view, w->kp, true, s, lc);
     if (rc) return rc;
+    // the samplers' quad copies: advection input (view) and end velocity
+    view.qu = a->q2[0];
+    view.qv = a->q2[1];
+    view.qw = a->q2[2];
+    if ((rc = launch_mac_quads(view, s, lc))) return rc;
+    DevGrid end = view;
+    end.u = a->fix1.f(L, 0);
+    end.v = a->fix1.f(L, 1);
+    end.w = a->fix1.f(L, 2);
+    end.qu = a->q4[0];
+    end.qv = a->q4[1];
+    end.qw = a->q4[2];
+    if ((rc = launch_mac_quads(end, s, lc))) return rc;
     AdjFwd f;
     f.u4 = a->fix1.f(L, 0);
     f.v4 = a->fix1.f(L, 1);
@@ -148,6 +163,10 @@ int issue_adj_step(zqs_adjoint* a, int K, cudaStream_t s, LaunchCounter& lc) {
     f.rho0 = view.rho;
     f.vort = view.t4a;
     f.flags = view.flags;
+    for (int c = 0; c < 3; c++) {
+        f.q4[c] = a->q4[c];
+        f.q2[c] = a->q2[c];
+    }
     return launch_adj_step(L, f, a->b, w->kp, w->src, K, s, lc);
 }
 
@@ -227,10 +246,11 @@ ZQS_API int zqs_adjoint_create(zqs_adjoint** out, zqs_grid* g, int nsteps, int c
     const size_t fe = (size_t)L.elems;
     const size_t nslots = (size_t)a->ncp + 1 + (size_t)(a->every - 1) + 2;  // + fix0, fix1
     const size_t nflt = 9 + 8 + 3;        // gu.., gu3.., gu2.., gT, grho, gTa, grhoa, q, q2, acc, wt, gF(3)
-    const size_t nf4 = 5;                 // gom4, gg4, gw4, t4a, t4b
+    const size_t nf4 = 11;                // gom4, gg4, gw4, t4a, t4b, q4 (3), q2 (3)
+    const size_t gqe = fe + 2;            // a quad accumulator with its float4 of margin (+1 spare)
     const long long nblocks = (long long)((L.W + 31) / 32) * ((L.H + 7) / 8) * L.D;
     const size_t red_len = (size_t)(2 * nblocks + 16);
-    const size_t total = (nslots * 5 + nflt) * fe * 4 + nf4 * fe * 16 + red_len * 8 + 256;
+    const size_t total = (nslots * 5 + nflt) * fe * 4 + nf4 * fe * 16 + 3 * gqe * 16 + red_len * 8 + 256;
     cudaError_t e = dev_alloc(&a->mem, total);
     if (e != cudaSuccess) return fail(cuda_fail(e, "zqs_adjoint_create: cudaMalloc"));
     e = cudaMemset(a->mem, 0, total);
@@ -273,6 +293,9 @@ ZQS_API int zqs_adjoint_create(zqs_adjoint** out, zqs_grid* g, int nsteps, int c
     b.gw4 = (float4*)take(fe * 16) + L.plane;
     a->t4a = (float4*)take(fe * 16) + L.plane;
     a->t4b = (float4*)take(fe * 16) + L.plane;
+    for (int c = 0; c < 3; c++) a->q4[c] = (float4*)take(fe * 16) + L.plane;
+    for (int c = 0; c < 3; c++) a->q2[c] = (float4*)take(fe * 16) + L.plane;
+    for (int c = 0; c < 3; c++) b.gq[c] = (float4*)take(gqe * 16) + L.plane + 1;
     b.red = (double*)take(red_len * 8);
     b.red_len = (long long)red_len;
     // the work grid: same parameters, occupancy and SOR setup

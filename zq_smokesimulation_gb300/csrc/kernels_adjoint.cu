@@ -49,15 +49,67 @@ __device__ __forceinline__ void tri_scatter(float* __restrict__ f, const Corners
     atomicAdd(f + c.r11 + c.i1, ((x1 * y1) * z1) * val);
 }
 
-__device__ __forceinline__ Corners corners_u(const Layout& L, float x, float y, float z) {
-    return corners(L, L.W + 1, L.H, L.D, x, y - 0.5f, z - 0.5f);
+// Base corner of a trilinear sample in the quad layout (tri0 in
+// zqs_sample.cuh), plus the axes the clamp-to-edge rule pinned to the last
+// texel (i0 == n-1).  There the clamped sample is flat along that axis (both
+// corners are the same texel), so its derivative is 0; the quad form's
+// unclamped +1 corner enters the value with weight t = 0 only, but would give
+// a one-sided difference, which tri_grad_q replaces by that 0.
+struct QC {
+    int r;
+    float tx, ty, tz;
+    bool hx, hy, hz;
+};
+__device__ __forceinline__ QC qcorner(const Layout& L, int nx, int ny, int nz, float gx, float gy, float gz) {
+    const Ax ax = axis(gx, nx), ay = axis(gy, ny), az = axis(gz, nz);
+    QC c;
+    c.r = (az.i0 * L.py + ay.i0) * L.px + ax.i0;
+    c.tx = ax.t;
+    c.ty = ay.t;
+    c.tz = az.t;
+    c.hx = ax.i0 == nx - 1;
+    c.hy = ay.i0 == ny - 1;
+    c.hz = az.i0 == nz - 1;
+    return c;
 }
-__device__ __forceinline__ Corners corners_v(const Layout& L, float x, float y, float z) {
-    return corners(L, L.W, L.H + 1, L.D, x - 0.5f, y, z - 0.5f);
+__device__ __forceinline__ QC qcorner_u(const Layout& L, float x, float y, float z) {
+    return qcorner(L, L.W + 1, L.H, L.D, x, y - 0.5f, z - 0.5f);
 }
-__device__ __forceinline__ Corners corners_w(const Layout& L, float x, float y, float z) {
-    return corners(L, L.W, L.H, L.D + 1, x - 0.5f, y - 0.5f, z);
+__device__ __forceinline__ QC qcorner_v(const Layout& L, float x, float y, float z) {
+    return qcorner(L, L.W, L.H + 1, L.D, x - 0.5f, y, z - 0.5f);
 }
+__device__ __forceinline__ QC qcorner_w(const Layout& L, float x, float y, float z) {
+    return qcorner(L, L.W, L.H, L.D + 1, x - 0.5f, y - 0.5f, z);
+}
+
+// tri_grad from the quad copy Q of the field: the eight corners are the two
+// 16-byte loads Q[r] = (c000, c001, c100, c101) and Q[r + px] = (c010, c011,
+// c110, c111); same expressions, and 0 along clamped axes.
+__device__ __forceinline__ void tri_grad_q(const float4* __restrict__ Q, const Layout& L, const QC& c, float g[3]) {
+    const float4 a = __ldg(Q + c.r);
+    const float4 b = __ldg(Q + c.r + L.px);
+    const float c000 = a.x, c001 = a.y, c100 = a.z, c101 = a.w;
+    const float c010 = b.x, c011 = b.y, c110 = b.z, c111 = b.w;
+    const float c00 = lerpf(c000, c100, c.tx), c10 = lerpf(c010, c110, c.tx);
+    const float c01 = lerpf(c001, c101, c.tx), c11 = lerpf(c011, c111, c.tx);
+    const float c0 = lerpf(c00, c10, c.ty), c1 = lerpf(c01, c11, c.ty);
+    g[0] = c.hx ? 0.0f : lerpf(lerpf(c100 - c000, c110 - c010, c.ty), lerpf(c101 - c001, c111 - c011, c.ty), c.tz);
+    g[1] = c.hy ? 0.0f : lerpf(c10 - c00, c11 - c01, c.tz);
+    g[2] = c.hz ? 0.0f : c1 - c0;
+}
+
+// tri_scatter into a quad accumulator: the same eight products, as two
+// 16-byte atomics (vector atomicAdd, compute capability 9.0 and up).  A
+// clamped axis has t = 0, so its +1 corners receive exact zeros.
+__device__ __forceinline__ void tri_scatter_q(float4* __restrict__ G, const Layout& L, const QC& c, float val) {
+    if (val == 0.0f) return;
+    const float x0 = 1.0f - c.tx, x1 = c.tx, y0 = 1.0f - c.ty, y1 = c.ty, z0 = 1.0f - c.tz, z1 = c.tz;
+    atomicAdd(G + c.r, make_float4(((x0 * y0) * z0) * val, ((x0 * y0) * z1) * val, ((x1 * y0) * z0) * val,
+                                   ((x1 * y0) * z1) * val));
+    atomicAdd(G + c.r + L.px, make_float4(((x0 * y1) * z0) * val, ((x0 * y1) * z1) * val,
+                                          ((x1 * y1) * z0) * val, ((x1 * y1) * z1) * val));
+}
+
 __device__ __forceinline__ Corners corners_c(const Layout& L, float x, float y, float z) {
     return corners(L, L.W, L.H, L.D, x - 0.5f, y - 0.5f, z - 0.5f);
 }
@@ -73,9 +125,11 @@ __device__ __forceinline__ bool bt_ok(const Layout& L, const uint8_t* __restrict
 }
 
 // The forward backtrace (zqs_sample.cuh) with every position kept in xs;
-// returns m, the index of the point the forward samples at.
+// returns m, the index of the point the forward samples at.  VelF is the
+// forward's sampler (MacVelQ: the quad copies, bit-identical to the fields).
+template <class VelF>
 __device__ __forceinline__ int backtrace_record(const Layout& L, const uint8_t* __restrict__ flags,
-                                                const MacVel& vel, const KParams& kp, float px, float py, float pz,
+                                                const VelF& vel, const KParams& kp, float px, float py, float pz,
                                                 float* xs) {
     float vx, vy, vz;
     vel(px, py, pz, vx, vy, vz);
@@ -111,23 +165,22 @@ __device__ __forceinline__ int backtrace_record(const Layout& L, const uint8_t* 
 }
 
 // Reverse of x_{s+1} = x_s - c*vel(x_s) for s = m-1 .. 0: the velocity
-// adjoint -c*gx is scattered at x_s and gx += J_vel(x_s)^T (-c*gx).
-__device__ __forceinline__ void backtrace_adjoint(const Layout& L, const float* __restrict__ u,
-                                                  const float* __restrict__ v, const float* __restrict__ w,
-                                                  float* __restrict__ gu, float* __restrict__ gv,
-                                                  float* __restrict__ gw, const float* xs, int m, float c,
+// adjoint -c*gx is scattered at x_s into the quad accumulators gq and
+// gx += J_vel(x_s)^T (-c*gx), with J from the quad copies q.
+__device__ __forceinline__ void backtrace_adjoint(const Layout& L, const float4* const (&q)[3],
+                                                  float4* const (&gq)[3], const float* xs, int m, float c,
                                                   float gx[3]) {
     for (int s = m - 1; s >= 0; s--) {
         const float x = xs[3 * s], y = xs[3 * s + 1], z = xs[3 * s + 2];
         const float g0 = -c * gx[0], g1 = -c * gx[1], g2 = -c * gx[2];
-        const Corners cu = corners_u(L, x, y, z), cv = corners_v(L, x, y, z), cw = corners_w(L, x, y, z);
-        tri_scatter(gu, cu, g0);
-        tri_scatter(gv, cv, g1);
-        tri_scatter(gw, cw, g2);
+        const QC cu = qcorner_u(L, x, y, z), cv = qcorner_v(L, x, y, z), cw = qcorner_w(L, x, y, z);
+        tri_scatter_q(gq[0], L, cu, g0);
+        tri_scatter_q(gq[1], L, cv, g1);
+        tri_scatter_q(gq[2], L, cw, g2);
         float J0[3], J1[3], J2[3];
-        tri_grad(u, cu, J0);
-        tri_grad(v, cv, J1);
-        tri_grad(w, cw, J2);
+        tri_grad_q(q[0], L, cu, J0);
+        tri_grad_q(q[1], L, cv, J1);
+        tri_grad_q(q[2], L, cw, J2);
         gx[0] += (J0[0] * g0 + J1[0] * g1) + J2[0] * g2;
         gx[1] += (J0[1] * g0 + J1[1] * g1) + J2[1] * g2;
         gx[2] += (J0[2] * g0 + J1[2] * g1) + J2[2] * g2;
@@ -166,7 +219,7 @@ __global__ void __launch_bounds__(256) k_adj_scalar(Layout L, AdjFwd f, AdjBufs 
     const float gT = b.gT[c], gD = b.grho[c];
     if (gT == 0.0f && gD == 0.0f) return;
     float xs[3 * (kAdjMaxSubsteps + 1)];
-    const MacVel mv{L, {f.u4}, {f.v4}, {f.w4}};
+    const MacVelQ mv{L, {f.q4[0]}, {f.q4[1]}, {f.q4[2]}};
     const int m = backtrace_record(L, f.flags, mv, kp, (float)i + 0.5f, (float)j + 0.5f, (float)k + 0.5f, xs);
     const float x = xs[3 * m], y = xs[3 * m + 1], z = xs[3 * m + 2];
     const Corners cc = corners_c(L, x, y, z);
@@ -177,7 +230,7 @@ __global__ void __launch_bounds__(256) k_adj_scalar(Layout L, AdjFwd f, AdjBufs 
     tri_grad(f.T0, cc, g1);
     tri_grad(f.rho0, cc, g2);
     float gx[3] = {aT * g1[0] + aD * g2[0], aT * g1[1] + aD * g2[1], aT * g1[2] + aD * g2[2]};
-    backtrace_adjoint(L, f.u4, f.v4, f.w4, b.gu, b.gv, b.gw, xs, m, chain_c(kp), gx);
+    backtrace_adjoint(L, f.q4, b.gq, xs, m, chain_c(kp), gx);
 }
 
 // ---------------------------------------------------------------- projection
@@ -345,13 +398,14 @@ __global__ void k_adj_divT(Layout L, const uint8_t* __restrict__ flags, AdjBufs 
 
 // ---------------------------------------------------------------- velocity advection
 
-// Per live face (bz = comp*(D+1) + k): transposed final sample of the input
-// component and the backtrace chain, all into gu2 (atomics).
+// Per live face (bz = 3k + comp, the three components of a plane adjacent in
+// the launch order as in the forward): transposed final sample of the input
+// component and the backtrace chain, all into the quad accumulators gq.
 __global__ void __launch_bounds__(256) k_adj_advect_vel(Layout L, AdjFwd f, AdjBufs b, KParams kp) {
     const int i = blockIdx.x * 32 + threadIdx.x;
     const int j = blockIdx.y * 8 + threadIdx.y;
-    const int comp = blockIdx.z / (L.D + 1);
-    const int k = blockIdx.z - comp * (L.D + 1);
+    const int k = blockIdx.z / 3;
+    const int comp = blockIdx.z - 3 * k;
     int nx = L.W, ny = L.H, nz = L.D;
     if (comp == 0) nx++;
     else if (comp == 1) ny++;
@@ -366,27 +420,40 @@ __global__ void __launch_bounds__(256) k_adj_advect_vel(Layout L, AdjFwd f, AdjB
     const float py0 = (comp == 1) ? (float)j : (float)j + 0.5f;
     const float pz0 = (comp == 2) ? (float)k : (float)k + 0.5f;
     float xs[3 * (kAdjMaxSubsteps + 1)];
-    const MacVel mv{L, {f.u2}, {f.v2}, {f.w2}};
+    const MacVelQ mv{L, {f.q2[0]}, {f.q2[1]}, {f.q2[2]}};
     const int m = backtrace_record(L, f.flags, mv, kp, px0, py0, pz0, xs);
     const float x = xs[3 * m], y = xs[3 * m + 1], z = xs[3 * m + 2];
     float gx[3];
-    if (comp == 0) {
-        const Corners cc = corners_u(L, x, y, z);
-        tri_scatter(b.gu2, cc, g);
-        tri_grad(f.u2, cc, gx);
-    } else if (comp == 1) {
-        const Corners cc = corners_v(L, x, y, z);
-        tri_scatter(b.gv2, cc, g);
-        tri_grad(f.v2, cc, gx);
-    } else {
-        const Corners cc = corners_w(L, x, y, z);
-        tri_scatter(b.gw2, cc, g);
-        tri_grad(f.w2, cc, gx);
-    }
+    const QC cc = comp == 0 ? qcorner_u(L, x, y, z) : (comp == 1 ? qcorner_v(L, x, y, z) : qcorner_w(L, x, y, z));
+    // (selects, not a dynamic index into the parameter arrays)
+    tri_scatter_q(comp == 0 ? b.gq[0] : (comp == 1 ? b.gq[1] : b.gq[2]), L, cc, g);
+    tri_grad_q(comp == 0 ? f.q2[0] : (comp == 1 ? f.q2[1] : f.q2[2]), L, cc, gx);
     gx[0] *= g;
     gx[1] *= g;
     gx[2] *= g;
-    backtrace_adjoint(L, f.u2, f.v2, f.w2, b.gu2, b.gv2, b.gw2, xs, m, chain_c(kp), gx);
+    backtrace_adjoint(L, f.q2, b.gq, xs, m, chain_c(kp), gx);
+}
+
+// g += the quad accumulators folded back onto their texels (bz = 3k + comp,
+// every face index): texel t collects gq[t].x + gq[t - plane].y + gq[t - 1].z
+// + gq[t - plane - 1].w.  Padding entries only ever receive exact zeros.
+__global__ void __launch_bounds__(256) k_adj_fold(Layout L, AdjBufs b, float* __restrict__ gu,
+                                                  float* __restrict__ gv, float* __restrict__ gw) {
+    const int i = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * 8 + threadIdx.y;
+    const int k = blockIdx.z / 3;
+    const int comp = blockIdx.z - 3 * k;
+    int nx = L.W, ny = L.H, nz = L.D;
+    if (comp == 0) nx++;
+    else if (comp == 1) ny++;
+    else nz++;
+    if (i >= nx || j >= ny || k >= nz) return;
+    const int c = lidx(L, i, j, k);
+    const int pl = (int)L.plane;
+    const float4* G = comp == 0 ? b.gq[0] : (comp == 1 ? b.gq[1] : b.gq[2]);
+    const float s = (G[c].x + G[c - pl].y) + (G[c - 1].z + G[c - pl - 1].w);
+    float* dst = comp == 0 ? gu : (comp == 1 ? gv : gw);
+    if (s != 0.0f) dst[c] += s;
 }
 
 // ---------------------------------------------------------------- forces
@@ -560,12 +627,19 @@ int launch_adj_step(const Layout& L, const AdjFwd& f, const AdjBufs& b, const KP
     dim3 gc((L.W + 31) / 32, (L.H + 7) / 8, L.D);
     dim3 gf((L.W + 1 + 31) / 32, (L.H + 1 + 7) / 8, L.D + 1);
     dim3 ga((L.W + 1 + 31) / 32, (L.H + 1 + 7) / 8, 3 * (L.D + 1));
+    dim3 gq3((L.W + 1 + 31) / 32, (L.H + 1 + 7) / 8, 3 * (L.D + 1));
     const size_t cell_bytes = (size_t)L.elems * 4;
+    // the three quad accumulators are contiguous, each with a float4 before
+    // its leading guard plane and one spare after it
+    const size_t gq_bytes = 3 * (size_t)(L.elems + 2) * 16;
+    float4* gq_base = b.gq[0] - L.plane - 1;
     // scalar advection + reinjection
     ZQS_CUDA_TRY(cudaMemsetAsync(b.gTa - L.plane, 0, cell_bytes, s));
     ZQS_CUDA_TRY(cudaMemsetAsync(b.grhoa - L.plane, 0, cell_bytes, s));
+    ZQS_CUDA_TRY(cudaMemsetAsync(gq_base, 0, gq_bytes, s));
     k_adj_scalar<<<gc, blk, 0, s>>>(L, f, b, kp, src);
-    lc.n++;
+    k_adj_fold<<<gq3, blk, 0, s>>>(L, b, b.gu, b.gv, b.gw);
+    lc.n += 2;
     ZQS_LAUNCH_CHECK("k_adj_scalar");
     // projection: G^T, reversed SOR, div^T
     const int open = kp.solver == ZQS_SOLVER_OPEN ? 1 : 0;
@@ -604,8 +678,10 @@ int launch_adj_step(const Layout& L, const AdjFwd& f, const AdjBufs& b, const KP
     lc.n++;
     ZQS_LAUNCH_CHECK("k_adj_divT");
     // velocity advection
+    ZQS_CUDA_TRY(cudaMemsetAsync(gq_base, 0, gq_bytes, s));
     k_adj_advect_vel<<<ga, blk, 0, s>>>(L, f, b, kp);
-    lc.n++;
+    k_adj_fold<<<gq3, blk, 0, s>>>(L, b, b.gu2, b.gv2, b.gw2);
+    lc.n += 2;
     ZQS_LAUNCH_CHECK("k_adj_advect_vel");
     // forces (+ attenuation)
     k_adj_force_cell<<<gc, blk, 0, s>>>(L, f, b, kp);
