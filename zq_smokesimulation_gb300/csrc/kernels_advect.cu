@@ -82,7 +82,10 @@ __device__ __forceinline__ void advect_vel_macout_tile(const Layout& L, const Ve
     else nz++;
     if (i >= nx || j >= ny || k >= nz) return;
     const int c = lidx(L, i, j, k);
-    float* dst = P.out[comp];
+    // per-component pointers by select (a dynamic index into P would copy it
+    // to local memory)
+    auto pick = [comp](auto a, auto b, auto c) { return comp == 0 ? a : (comp == 1 ? b : c); };
+    float* dst = pick(P.out[0], P.out[1], P.out[2]);
     bool live = true;
     if (!RAW) {
         const uint8_t fl = __ldg(flags + c);
@@ -101,16 +104,17 @@ __device__ __forceinline__ void advect_vel_macout_tile(const Layout& L, const Ve
             backtrace(L, flags, rv, kp, px, py, pz);
             out = tri4c(P.in4, comp, corners(L, L.W, L.H, L.D, px - 0.5f, py - 0.5f, pz - 0.5f));
         } else {
-            const MacVelT<QuadTri, NEG> mv{L, {P.q[0]}, {P.q[1]}, {P.q[2]}};
+            MacVelQC<NEG> mv(L, P.q[0], P.q[1], P.q[2]);
             backtrace(L, flags, mv, kp, px, py, pz);
             Tri0 t;
             if (comp == 0) t = tri0(L, L.W + 1, L.H, L.D, px, py - 0.5f, pz - 0.5f);
             else if (comp == 1) t = tri0(L, L.W, L.H + 1, L.D, px - 0.5f, py, pz - 0.5f);
             else t = tri0(L, L.W, L.H, L.D + 1, px - 0.5f, py - 0.5f, pz);
-            out = SEPIN ? tri0_sample(P.in[comp], L, t) : tri0_quad(P.q[comp], L, t);
+            out = SEPIN ? tri0_sample(pick(P.in[0], P.in[1], P.in[2]), L, t)
+                        : mv.sample(comp, pick(P.q[0], P.q[1], P.q[2]), t);
         }
     } else {
-        out = __ldg(P.keep[comp] + c);
+        out = __ldg(pick(P.keep[0], P.keep[1], P.keep[2]) + c);
     }
     dst[c] = out;
 }
@@ -269,7 +273,7 @@ __device__ __forceinline__ void advect_scalar_tile(const Layout& L, const float4
         const RegVelT<NEG> rv{L, vel4};
         backtrace(L, flags, rv, kp, px, py, pz);
     } else {
-        const MacVelT<QuadTri, NEG> mv{L, {q[0]}, {q[1]}, {q[2]}};
+        MacVelQC<NEG> mv(L, q[0], q[1], q[2]);
         backtrace(L, flags, mv, kp, px, py, pz);
     }
     const Tri0 cs = tri0(L, L.W, L.H, L.D, px - 0.5f, py - 0.5f, pz - 0.5f);
@@ -309,7 +313,7 @@ static_assert(sizeof(AdvHotTable) + 64 <= 32764, "the hot table must fit the ker
 
 // Batched velocity advection over the tiles [t0, t1) of one table chunk
 // (launched with one CTA per tile; the loop also serves smaller grids).
-__global__ void __launch_bounds__(256, 5) k_advect_vel_batch(BatchLaunch B, const __grid_constant__ AdvHotTable T,
+__global__ void __launch_bounds__(256, 4) k_advect_vel_batch(BatchLaunch B, const __grid_constant__ AdvHotTable T,
                                                          int vcur, int t0, int t1) {
     for (int t = t0 + blockIdx.x; t < t1; t += gridDim.x) {
         const int i = batch_find(B.pre, B.n, t);
@@ -332,7 +336,7 @@ __global__ void __launch_bounds__(256, 5) k_advect_vel_batch(BatchLaunch B, cons
 
 // Batched scalar advection (+ attenuation, + reinjection) over the tiles
 // [t0, t1) of one table chunk; the sources come from the instance descriptor.
-__global__ void __launch_bounds__(256, 5) k_advect_scalar_batch(BatchLaunch B, const __grid_constant__ AdvHotTable T,
+__global__ void __launch_bounds__(256, 4) k_advect_scalar_batch(BatchLaunch B, const __grid_constant__ AdvHotTable T,
                                                             int vcur, int scur, int t0, int t1) {
     for (int t = t0 + blockIdx.x; t < t1; t += gridDim.x) {
         const int i = batch_find(B.pre, B.n, t);

@@ -184,9 +184,8 @@ __device__ __forceinline__ float3 tri4(const float4* __restrict__ f, const Corne
     r.z = lerpf(z0, z1, c.tz);
     return r;
 }
-__device__ __forceinline__ float tri0_quad(const float4* __restrict__ q, const Layout& L, const Tri0& c) {
-    const float4 a = __ldg(q + c.r);
-    const float4 b = __ldg(q + c.r + L.px);
+// tri0_quad on the two quads already loaded (a = Q[r], b = Q[r + px]).
+__device__ __forceinline__ float tri0_quad_ab(const float4& a, const float4& b, const Tri0& c) {
     const float2 ma = lerp_step2(a.x, a.y, a.z, a.w, c.tx, c.tx);
     const float2 mb = lerp_step2(b.x, b.y, b.z, b.w, c.tx, c.tx);
     const float c00 = __fadd_rn(a.x, ma.x), c01 = __fadd_rn(a.y, ma.y);  // lerpf(a.x, a.z), lerpf(a.y, a.w)
@@ -194,6 +193,9 @@ __device__ __forceinline__ float tri0_quad(const float4* __restrict__ q, const L
     const float2 my = lerp_step2(c00, c01, c10, c11, c.ty, c.ty);
     const float c0 = __fadd_rn(c00, my.x), c1 = __fadd_rn(c01, my.y);  // lerpf(c00, c10), lerpf(c01, c11)
     return lerpf(c0, c1, c.tz);
+}
+__device__ __forceinline__ float tri0_quad(const float4* __restrict__ q, const Layout& L, const Tri0& c) {
+    return tri0_quad_ab(__ldg(q + c.r), __ldg(q + c.r + L.px), c);
 }
 
 // Corner fetch policies of the MAC sampler: the field itself, or its quads.
@@ -259,6 +261,86 @@ struct MacVelT {
         ck = min(zw.i0, L.D - 1);
     }
 };
+// MacVelT<QuadTri> that keeps each component's last two quads (and the last
+// occupancy byte) in registers: while a backtrace stays inside the same
+// interpolation cells from one substep to the next (everywhere the flow moves
+// less than a cell per step) the samples reuse them instead of gathering
+// through L1 again.  Same values into the same arithmetic: bit-identical to
+// MacVelT<QuadTri>.  One instance per thread and backtrace.
+template <bool NEG = false>
+struct MacVelQC {
+    Layout L;
+    const float4 *qu, *qv, *qw;
+    int ru = -1, rv = -1, rw = -1, rf = -1;
+    float4 au, bu, av, bv, aw, bw;
+    uint8_t fl = 0;
+    __device__ __forceinline__ MacVelQC(const Layout& L_, const float4* u, const float4* v, const float4* w)
+        : L(L_), qu(u), qv(v), qw(w) {}
+    __device__ __forceinline__ void operator()(float px, float py, float pz, float& vx, float& vy, float& vz,
+                                               int& ci, int& cj, int& ck) {
+        const Ax xu = axis(px, L.W + 1), xc = axis(px - 0.5f, L.W);
+        const Ax yv = axis(py, L.H + 1), yc = axis(py - 0.5f, L.H);
+        const Ax zw = axis(pz, L.D + 1), zc = axis(pz - 0.5f, L.D);
+        const int rcc = zc.i0 * L.py;
+        Tri0 cu, cv, cw;
+        cu.r = (rcc + yc.i0) * L.px + xu.i0;
+        cu.tx = xu.t;
+        cu.ty = yc.t;
+        cu.tz = zc.t;
+        cv.r = (rcc + yv.i0) * L.px + xc.i0;
+        cv.tx = xc.t;
+        cv.ty = yv.t;
+        cv.tz = zc.t;
+        cw.r = (zw.i0 * L.py + yc.i0) * L.px + xc.i0;
+        cw.tx = xc.t;
+        cw.ty = yc.t;
+        cw.tz = zw.t;
+        if (cu.r != ru) {
+            ru = cu.r;
+            au = __ldg(qu + ru);
+            bu = __ldg(qu + ru + L.px);
+        }
+        if (cv.r != rv) {
+            rv = cv.r;
+            av = __ldg(qv + rv);
+            bv = __ldg(qv + rv + L.px);
+        }
+        if (cw.r != rw) {
+            rw = cw.r;
+            aw = __ldg(qw + rw);
+            bw = __ldg(qw + rw + L.px);
+        }
+        vx = tri0_quad_ab(au, bu, cu);
+        vy = tri0_quad_ab(av, bv, cv);
+        vz = tri0_quad_ab(aw, bw, cw);
+        if (NEG) {
+            vx = -vx;
+            vy = -vy;
+            vz = -vz;
+        }
+        ci = min(xu.i0, L.W - 1);
+        cj = min(yv.i0, L.H - 1);
+        ck = min(zw.i0, L.D - 1);
+    }
+    // tri0_quad of component comp (quad copy q) at c, from the cache when
+    // its last sample of that component had the same base
+    __device__ __forceinline__ float sample(int comp, const float4* __restrict__ q, const Tri0& c) const {
+        if (comp == 0 && c.r == ru) return tri0_quad_ab(au, bu, c);
+        if (comp == 1 && c.r == rv) return tri0_quad_ab(av, bv, c);
+        if (comp == 2 && c.r == rw) return tri0_quad_ab(aw, bw, c);
+        return tri0_quad(q, L, c);
+    }
+    // occupancy byte of cell (i, j, k), reloaded only when the cell changes
+    __device__ __forceinline__ uint8_t flag(const uint8_t* __restrict__ flags, int i, int j, int k) {
+        const int c = lidx(L, i, j, k);
+        if (c != rf) {
+            rf = c;
+            fl = __ldg(flags + c);
+        }
+        return fl;
+    }
+};
+
 using MacVel = MacVelT<FieldTri>;   // corners from the fields
 using MacVelQ = MacVelT<QuadTri>;   // corners from the quad copies
 template <bool NEG = false>
@@ -367,6 +449,56 @@ __device__ __forceinline__ void backtrace(const Layout& L, const uint8_t* __rest
         const int i = min((int)floorf(px), L.W - 1), j = min((int)floorf(py), L.H - 1);
         const int k = min((int)floorf(pz), L.D - 1);
         if (__ldg(flags + lidx(L, i, j, k)) & F_FREE) {
+            lx = px;
+            ly = py;
+            lz = pz;
+        }
+    }
+    px = lx;
+    py = ly;
+    pz = lz;
+}
+
+// backtrace() for the caching MAC sampler: the same loop as above, the
+// occupancy test through the sampler's cached byte.
+template <bool NEG>
+__device__ __forceinline__ void backtrace(const Layout& L, const uint8_t* __restrict__ flags, MacVelQC<NEG>& vel,
+                                          const KParams& kp, float& px, float& py, float& pz) {
+    float vx, vy, vz;
+    int ci, cj, ck;
+    vel(px, py, pz, vx, vy, vz, ci, cj, ck);
+    float lx = px, ly = py, lz = pz;
+    const float Wf = (float)L.W, Hf = (float)L.H, Df = (float)L.D;
+    auto inside = [&](float x, float y, float z) -> bool {
+        return x >= 0.0f && x <= Wf && y >= 0.0f && y <= Hf && z >= 0.0f && z <= Df;
+    };
+    const float dt = kp.dt_sub;
+    int istep = 0;
+    bool broke = false;
+    do {
+        if (!inside(px, py, pz) || !(vel.flag(flags, ci, cj, ck) & F_FREE)) {
+            broke = true;
+            break;
+        }
+        lx = px;
+        ly = py;
+        lz = pz;
+        if (kp.inv_h != 0.0f) {
+            px = px - (vx * dt) * kp.inv_h;
+            py = py - (vy * dt) * kp.inv_h;
+            pz = pz - (vz * dt) * kp.inv_h;
+        } else {
+            px = px - (vx * dt) / kp.h;
+            py = py - (vy * dt) / kp.h;
+            pz = pz - (vz * dt) / kp.h;
+        }
+        istep++;
+        if (istep < kp.substeps) vel(px, py, pz, vx, vy, vz, ci, cj, ck);
+    } while (istep < kp.substeps);
+    if (kp.full && !broke && inside(px, py, pz)) {
+        const int i = min((int)floorf(px), L.W - 1), j = min((int)floorf(py), L.H - 1);
+        const int k = min((int)floorf(pz), L.D - 1);
+        if (vel.flag(flags, i, j, k) & F_FREE) {
             lx = px;
             ly = py;
             lz = pz;
