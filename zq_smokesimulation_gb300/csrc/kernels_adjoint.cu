@@ -126,11 +126,11 @@ __device__ __forceinline__ bool bt_ok(const Layout& L, const uint8_t* __restrict
 
 // The forward backtrace (zqs_sample.cuh) with every position kept in xs;
 // returns m, the index of the point the forward samples at.  VelF is the
-// forward's sampler (MacVelQ: the quad copies, bit-identical to the fields).
+// forward's sampler (MacVelQC: the quad copies with the last quads kept in
+// registers, bit-identical to the fields).
 template <class VelF>
-__device__ __forceinline__ int backtrace_record(const Layout& L, const uint8_t* __restrict__ flags,
-                                                const VelF& vel, const KParams& kp, float px, float py, float pz,
-                                                float* xs) {
+__device__ __forceinline__ int backtrace_record(const Layout& L, const uint8_t* __restrict__ flags, VelF& vel,
+                                                const KParams& kp, float px, float py, float pz, float* xs) {
     float vx, vy, vz;
     vel(px, py, pz, vx, vy, vz);
     xs[0] = px;
@@ -219,7 +219,7 @@ __global__ void __launch_bounds__(256) k_adj_scalar(Layout L, AdjFwd f, AdjBufs 
     const float gT = b.gT[c], gD = b.grho[c];
     if (gT == 0.0f && gD == 0.0f) return;
     float xs[3 * (kAdjMaxSubsteps + 1)];
-    const MacVelQ mv{L, {f.q4[0]}, {f.q4[1]}, {f.q4[2]}};
+    MacVelQC<> mv(L, f.q4[0], f.q4[1], f.q4[2]);
     const int m = backtrace_record(L, f.flags, mv, kp, (float)i + 0.5f, (float)j + 0.5f, (float)k + 0.5f, xs);
     const float x = xs[3 * m], y = xs[3 * m + 1], z = xs[3 * m + 2];
     const Corners cc = corners_c(L, x, y, z);
@@ -420,7 +420,7 @@ __global__ void __launch_bounds__(256) k_adj_advect_vel(Layout L, AdjFwd f, AdjB
     const float py0 = (comp == 1) ? (float)j : (float)j + 0.5f;
     const float pz0 = (comp == 2) ? (float)k : (float)k + 0.5f;
     float xs[3 * (kAdjMaxSubsteps + 1)];
-    const MacVelQ mv{L, {f.q2[0]}, {f.q2[1]}, {f.q2[2]}};
+    MacVelQC<> mv(L, f.q2[0], f.q2[1], f.q2[2]);
     const int m = backtrace_record(L, f.flags, mv, kp, px0, py0, pz0, xs);
     const float x = xs[3 * m], y = xs[3 * m + 1], z = xs[3 * m + 2];
     float gx[3];

@@ -322,6 +322,10 @@ struct MacVelQC {
         cj = min(yv.i0, L.H - 1);
         ck = min(zw.i0, L.D - 1);
     }
+    __device__ __forceinline__ void operator()(float px, float py, float pz, float& vx, float& vy, float& vz) {
+        int ci, cj, ck;
+        (*this)(px, py, pz, vx, vy, vz, ci, cj, ck);
+    }
     // tri0_quad of component comp (quad copy q) at c, from the cache when
     // its last sample of that component had the same base
     __device__ __forceinline__ float sample(int comp, const float4* __restrict__ q, const Tri0& c) const {
