@@ -1166,8 +1166,10 @@ RbVariant quad_variant() {
 // The registry of fused SOR variants (temporal depth S/2, tile, pairs per thread);
 // 0-9 keep every plane in shared memory (k_sor_rb), 10-17 keep the thread's own
 // column in registers (k_sor_reg), 18-20 also the update weights (WREG), 21-23
-// are the quad form (k_sor_quad: four x-adjacent cells per thread).
-constexpr int kNumVariants = 24;
+// are the quad form (k_sor_quad: four x-adjacent cells per thread), 24 the
+// WREG form on 32x30 tiles (nine tile rows cover 256: 144 CTAs of one SM each
+// at two z chunks, where 32x32 tiles give 128).
+constexpr int kNumVariants = 25;
 RbVariant g_var[kNumVariants];
 // default variant per depth 1..4
 // (measured at 256^3 on GB300: register-column 32x32 at depth 2 with the
@@ -1254,6 +1256,7 @@ int sor_prepare() {
         g_var[21] = quad_variant<4, 32, 32>();
         g_var[22] = quad_variant<4, 32, 16>();
         g_var[23] = quad_variant<4, 64, 16>();
+        g_var[24] = reg_variant<4, 32, 30, 1, true>();
     }
     int sms = 0;
     ZQS_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
