@@ -369,14 +369,14 @@ int issue_batch_step(zqs_batch* b, int par, cudaStream_t s, LaunchCounter& lc, i
     if (rc) return rc;
     rc = launch_mac_quads_batch(bl[TC_FACE], par, b->blocks, s, lc);
     if (rc) return rc;
-    rc = launch_advect_velocity_batch(bl[TC_ADVF], b->hot, par, b->blocks, s, lc);
+    rc = launch_advect_velocity_batch(bl[TC_ADVF], b->hot, par, s, lc);
     if (rc) return rc;
     rc = launch_project_batch(bl[TC_CELL], bl[TC_FACE], bl[TC_SORM], bl[TC_SORR], b->plan, b->K, b->any_closed,
                               par ^ 1, b->blocks, s, lc, pfin);
     if (rc) return rc;
     rc = launch_mac_quads_batch(bl[TC_FACE], par ^ 1, b->blocks, s, lc);
     if (rc) return rc;
-    return launch_advect_scalar_batch(bl[TC_CELL], b->hot, par ^ 1, par, b->blocks, s, lc);
+    return launch_advect_scalar_batch(bl[TC_CELL], b->hot, par ^ 1, par, s, lc);
 }
 
 }  // namespace

@@ -549,7 +549,7 @@ int launch_mac_quads_batch(const BatchLaunch& face, int vcur, int blocks, cudaSt
 }
 
 int launch_advect_velocity_batch(const BatchLaunch& advf, const std::vector<AdvHotTable>& hot, int vcur,
-                                 int blocks, cudaStream_t s, LaunchCounter& lc) {
+                                 cudaStream_t s, LaunchCounter& lc) {
     dim3 b(32, 8, 1);
     for (const AdvHotTable& T : hot) {
         const int t0 = advf.pre_host[T.base], t1 = advf.pre_host[T.base + T.n];
@@ -557,7 +557,6 @@ int launch_advect_velocity_batch(const BatchLaunch& advf, const std::vector<AdvH
         // one CTA per tile: backtrace costs vary across tiles (plume against
         // still air), and the block scheduler balances them as CTAs finish
         k_advect_vel_batch<<<t1 - t0, b, 0, s>>>(advf, T, vcur, t0, t1);
-        (void)blocks;
         lc.n++;
     }
     ZQS_LAUNCH_CHECK("k_advect_vel_batch");
@@ -565,13 +564,12 @@ int launch_advect_velocity_batch(const BatchLaunch& advf, const std::vector<AdvH
 }
 
 int launch_advect_scalar_batch(const BatchLaunch& cell, const std::vector<AdvHotTable>& hot, int vcur, int scur,
-                               int blocks, cudaStream_t s, LaunchCounter& lc) {
+                               cudaStream_t s, LaunchCounter& lc) {
     dim3 b(32, 8, 1);
     for (const AdvHotTable& T : hot) {
         const int t0 = cell.pre_host[T.base], t1 = cell.pre_host[T.base + T.n];
         if (t1 <= t0) continue;
         k_advect_scalar_batch<<<t1 - t0, b, 0, s>>>(cell, T, vcur, scur, t0, t1);  // one CTA per tile
-        (void)blocks;
         lc.n++;
     }
     ZQS_LAUNCH_CHECK("k_advect_scalar_batch");

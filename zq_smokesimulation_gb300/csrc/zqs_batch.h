@@ -105,9 +105,9 @@ int launch_force_batch(const BatchLaunch& cell, const BatchLaunch& face, int vcu
 int launch_mac_quads_batch(const BatchLaunch& face, int vcur, int blocks, cudaStream_t s, LaunchCounter& lc);
 // One launch per table chunk, over the chunk's tiles [pre[base], pre[base + n]).
 int launch_advect_velocity_batch(const BatchLaunch& advf, const std::vector<AdvHotTable>& hot, int vcur,
-                                 int blocks, cudaStream_t s, LaunchCounter& lc);
+                                 cudaStream_t s, LaunchCounter& lc);
 int launch_advect_scalar_batch(const BatchLaunch& cell, const std::vector<AdvHotTable>& hot, int vcur, int scur,
-                               int blocks, cudaStream_t s, LaunchCounter& lc);
+                               cudaStream_t s, LaunchCounter& lc);
 // Divergence (+ closed-solver mean removal), K SOR iterations, gradient on the
 // velocity buffer vcur; *pfin receives the pressure buffer holding the result.
 int launch_project_batch(const BatchLaunch& cell, const BatchLaunch& face, const BatchLaunch& sorm,
