@@ -229,7 +229,10 @@ ZQS_API int zqs_sor_variant_info(int index, zqs_sor_variant* out);
  * planes each CTA streams (0: chosen from the grid and the device). */
 ZQS_API int zqs_grid_set_sor_variant(zqs_grid* g, int index, int zchunk);
 
-/* Wait for all work queued on the stream (NULL: the handle's own stream). */
+/* Wait for all work queued on the stream (NULL: the handle's own stream).
+ * Returns ZQS_ETIMEOUT when a bounded device-side wait gave up since the last
+ * check: a tensor-core wait of the coarse solver (below), or a per-step
+ * barrier wait of the split-barrier SOR variants (a device-wide count). */
 ZQS_API int zqs_grid_synchronize(zqs_grid* g, void* stream);
 
 /* Kernel launches issued by the last zqs_grid_step call (for accounting). */

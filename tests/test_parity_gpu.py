@@ -282,6 +282,7 @@ def test_sor_fused_variants_equal_split(zqs_lib, variant, case):
         g2.load_state(w.occ, w.u, w.v, w.w, w.T, w.rho)
         g2.set_sor_variant(variant, zchunk)
         g2.project()
+        g2.sync()   # raises on a device-side wait that gave up (split-barrier variants)
         a = {k: g1.download(f) for k, f in (("p", capi.FIELD_PRESSURE), ("v", capi.FIELD_V))}
         b = {k: g2.download(f) for k, f in (("p", capi.FIELD_PRESSURE), ("v", capi.FIELD_V))}
         assert_same(b, a, keys=("p", "v"), what=f"variant {variant} zchunk {zchunk}")

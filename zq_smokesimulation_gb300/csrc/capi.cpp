@@ -712,7 +712,8 @@ ZQS_API int zqs_grid_set_sor_variant(zqs_grid* g, int index, int zchunk) {
 ZQS_API int zqs_grid_synchronize(zqs_grid* g, void* stream) {
     if (!g) return set_error("NULL grid"), ZQS_EINVAL;
     ZQS_CUDA_TRY(cudaStreamSynchronize(g->pick(stream)));
-    return coarse_check(g->g.coarse, g->pick(stream));
+    int rc = coarse_check(g->g.coarse, g->pick(stream));
+    return rc ? rc : sor_sync_check();
 }
 
 ZQS_API int zqs_grid_set_coarse_gemm(zqs_grid* g, int mode) {

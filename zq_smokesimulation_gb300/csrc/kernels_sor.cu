@@ -364,7 +364,37 @@ struct RegShape {
 // updates), flags are not read, the half-sweeps run black first, each update
 // is q = (1-omega) q + wt * sum(q_n), and every cell's value before each
 // update is added to acc (read and written in place by the owning thread).
-template <int S, int TX, int TY, int PPT, bool ADJ = false, bool WREG = false>
+// Bounded waits of the split-barrier form (SPLIT below): a wait that gives up
+// counts itself here and lets the thread go on (the pass's result is then
+// wrong, which the caller can detect; the kernel still ends).
+__device__ unsigned int g_sor_sync_timeouts;
+
+__device__ __forceinline__ void sor_bar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"((uint32_t)__cvta_generic_to_shared(bar)),
+                 "r"(count)
+                 : "memory");
+}
+__device__ __forceinline__ void sor_bar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"((uint32_t)__cvta_generic_to_shared(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void sor_bar_wait(uint64_t* bar, uint32_t parity) {
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(bar);
+    for (int it = 0; it < (1 << 22); it++) {
+        uint32_t ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (ok) return;
+    }
+    atomicAdd(&g_sor_sync_timeouts, 1u);
+}
+
+template <int S, int TX, int TY, int PPT, bool ADJ = false, bool WREG = false, bool SPLIT = false>
 __device__ __forceinline__ void sor_reg_tile(const Layout& L, const float* __restrict__ pin,
                                              float* __restrict__ pout, const float* __restrict__ div,
                                              const uint8_t* __restrict__ flags, float omega, float om1, int bx,
@@ -464,10 +494,25 @@ __device__ __forceinline__ void sor_reg_tile(const Layout& L, const float* __res
         if (ADJ && out_ok[q] && tbeg >= z0 && tbeg < z1) na[q] = *reinterpret_cast<const float2*>(acc + gaddr[q]);
     }
 
+    // SPLIT: the two-step spacing of every shared-memory dependence (see the
+    // barrier at the end of a step) is kept with two mbarriers instead of a
+    // block barrier every two steps: a thread arrives on sbar[n & 1] when it
+    // has finished step n and, before step n, waits until every thread has
+    // finished step n-2, so warps may run up to a step apart.
+    __shared__ uint64_t sbar[2];
+    if (SPLIT) {
+        if (threadIdx.x == 0) {
+            sor_bar_init(&sbar[0], NT);
+            sor_bar_init(&sbar[1], NT);
+        }
+        __syncthreads();
+    }
+
     for (int g = 0; g < nsteps; g += NP) {
 #pragma unroll
         for (int qs = 0; qs < NP; qs++) {
             if (g + qs < nsteps) {
+                if (SPLIT && g + qs >= 2) sor_bar_wait(&sbar[qs & 1], (uint32_t)((((g + qs) >> 1) - 1) & 1));
                 const int t = tbeg + g + qs;
                 // 1. plane t: registers by colour, and publish
 #pragma unroll
@@ -597,7 +642,8 @@ __device__ __forceinline__ void sor_reg_tile(const Layout& L, const float* __res
                 // step t-2 (the slot published at step t held plane t-NP, last read
                 // by half-sweep S at step t-2).  A barrier after every odd ring slot
                 // (NP is even) separates every such pair of steps.
-                if (qs & 1) __syncthreads();
+                if (SPLIT) sor_bar_arrive(&sbar[qs & 1]);
+                else if (qs & 1) __syncthreads();
             }
         }
     }
@@ -818,6 +864,15 @@ __global__ void __launch_bounds__(RegShape<S, TX, TY, PPT>::NT)
     const int z0 = blockIdx.z * zc;
     sor_reg_tile<S, TX, TY, PPT, false, WREG>(L, pin, pout, div, flags, omega, om1, blockIdx.x, blockIdx.y, z0,
                                               min(z0 + zc, L.D));
+}
+
+template <int S, int TX, int TY, int PPT>
+__global__ void __launch_bounds__(RegShape<S, TX, TY, PPT>::NT)
+    k_sor_reg_split(Layout L, const float* __restrict__ pin, float* __restrict__ pout, const float* __restrict__ div,
+                    const uint8_t* __restrict__ flags, float omega, float om1, int zc) {
+    const int z0 = blockIdx.z * zc;
+    sor_reg_tile<S, TX, TY, PPT, false, true, true>(L, pin, pout, div, flags, omega, om1, blockIdx.x, blockIdx.y, z0,
+                                                    min(z0 + zc, L.D));
 }
 
 // Persistent batched pass: tile t of the flat SOR tile space belongs to the
@@ -1123,6 +1178,26 @@ RbVariant reg_variant() {
     return v;
 }
 
+template <int S, int TX, int TY, int PPT>
+cudaError_t split_launch(dim3 gr, const Layout& L, const float* pin, float* pout, const float* div,
+                         const uint8_t* flags, float omega, float om1, int zc, cudaStream_t st) {
+    using Sh = RegShape<S, TX, TY, PPT>;
+    k_sor_reg_split<S, TX, TY, PPT><<<gr, Sh::NT, Sh::smem, st>>>(L, pin, pout, div, flags, omega, om1, zc);
+    return cudaGetLastError();
+}
+
+template <int S, int TX, int TY, int PPT>
+RbVariant split_variant() {
+    RbVariant v = reg_variant<S, TX, TY, PPT, true>();
+    v.launch = &split_launch<S, TX, TY, PPT>;
+    v.fn = (const void*)k_sor_reg_split<S, TX, TY, PPT>;
+    v.launch_batch = nullptr;
+    v.fn_batch = nullptr;
+    v.launch_adj = nullptr;
+    v.fn_adj = nullptr;
+    return v;
+}
+
 template <int S, int TX, int TY>
 cudaError_t quad_launch(dim3 gr, const Layout& L, const float* pin, float* pout, const float* div,
                         const uint8_t* flags, float omega, float om1, int zc, cudaStream_t st) {
@@ -1169,7 +1244,7 @@ RbVariant quad_variant() {
 // are the quad form (k_sor_quad: four x-adjacent cells per thread), 24 the
 // WREG form on 32x30 tiles (nine tile rows cover 256: 144 CTAs of one SM each
 // at two z chunks, where 32x32 tiles give 128).
-constexpr int kNumVariants = 25;
+constexpr int kNumVariants = 27;
 RbVariant g_var[kNumVariants];
 // default variant per depth 1..4
 // (measured at 256^3 on GB300: register-column 32x32 at depth 2 with the
@@ -1257,6 +1332,8 @@ int sor_prepare() {
         g_var[22] = quad_variant<4, 32, 16>();
         g_var[23] = quad_variant<4, 64, 16>();
         g_var[24] = reg_variant<4, 32, 30, 1, true>();
+        g_var[25] = split_variant<4, 32, 32, 1>();
+        g_var[26] = split_variant<4, 32, 30, 1>();
     }
     int sms = 0;
     ZQS_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -1297,6 +1374,16 @@ int sor_prepare() {
 }
 
 int sor_variant_count() { return kNumVariants; }
+
+int sor_sync_check() {
+    unsigned int n = 0;
+    ZQS_CUDA_TRY(cudaMemcpyFromSymbol(&n, g_sor_sync_timeouts, sizeof(n)));
+    if (n == 0) return ZQS_OK;
+    const unsigned int zero = 0;
+    ZQS_CUDA_TRY(cudaMemcpyToSymbol(g_sor_sync_timeouts, &zero, sizeof(zero)));
+    set_error("SOR: " + std::to_string(n) + " split-barrier waits gave up; the pressure is not valid");
+    return ZQS_ETIMEOUT;
+}
 
 int sor_default_variant(int depth) { return kDefaultVariant[depth <= 0 ? 2 : std::min(depth, 4)]; }
 

@@ -163,6 +163,9 @@ int sor_autotune(const DevGrid& g, const KParams& kp, cudaStream_t s, SorChoice&
 int launch_project(DevGrid& g, const KParams& kp, int K, const SorConfig& cfg, cudaStream_t s,
                    LaunchCounter& lc, float** p_final);
 int sor_prepare();  // sets the SOR kernels' attributes once per device (outside any capture)
+// ZQS_ETIMEOUT (and clears the count) when a bounded wait of the split-barrier
+// SOR variants gave up on the current device since the last check.
+int sor_sync_check();
 int launch_stats(const DevGrid& g, const KParams& kp, const float* p, zqs_stats* out, cudaStream_t s);
 
 }  // namespace zqs
