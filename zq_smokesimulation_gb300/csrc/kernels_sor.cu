@@ -374,24 +374,34 @@ __device__ __forceinline__ void sor_bar_init(uint64_t* bar, uint32_t count) {
                  "r"(count)
                  : "memory");
 }
+__device__ __forceinline__ void sor_bar_inval(uint64_t* bar) {
+    asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"((uint32_t)__cvta_generic_to_shared(bar)) : "memory");
+}
 __device__ __forceinline__ void sor_bar_arrive(uint64_t* bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"((uint32_t)__cvta_generic_to_shared(bar))
                  : "memory");
 }
+__device__ __forceinline__ bool sor_bar_try(uint32_t a, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(a), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __noinline__ void sor_bar_wait_slow(uint32_t a, uint32_t parity) {
+    for (int it = 0; it < (1 << 22); it++)
+        if (sor_bar_try(a, parity)) return;
+    atomicAdd(&g_sor_sync_timeouts, 1u);
+}
+// One try inline (the phase has usually completed: warps drift by less than
+// a step), the bounded polling loop out of line.
 __device__ __forceinline__ void sor_bar_wait(uint64_t* bar, uint32_t parity) {
     const uint32_t a = (uint32_t)__cvta_generic_to_shared(bar);
-    for (int it = 0; it < (1 << 22); it++) {
-        uint32_t ok;
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-            "selp.u32 %0, 1, 0, p;\n\t}"
-            : "=r"(ok)
-            : "r"(a), "r"(parity)
-            : "memory");
-        if (ok) return;
-    }
-    atomicAdd(&g_sor_sync_timeouts, 1u);
+    if (!sor_bar_try(a, parity)) sor_bar_wait_slow(a, parity);
 }
 
 template <int S, int TX, int TY, int PPT, bool ADJ = false, bool WREG = false, bool SPLIT = false>
@@ -509,10 +519,16 @@ __device__ __forceinline__ void sor_reg_tile(const Layout& L, const float* __res
     }
 
     for (int g = 0; g < nsteps; g += NP) {
+        // step n = g + qs waits for phase ((n >> 1) - 1) of sbar[n & 1]; with
+        // g a multiple of NP = 2S + 2 (NP/2 odd) that parity is
+        // (g / NP + qs / 2 + 1) & 1
+        const uint32_t gpar = (uint32_t)(g / NP) & 1u;
 #pragma unroll
         for (int qs = 0; qs < NP; qs++) {
             if (g + qs < nsteps) {
-                if (SPLIT && g + qs >= 2) sor_bar_wait(&sbar[qs & 1], (uint32_t)((((g + qs) >> 1) - 1) & 1));
+                static_assert(!SPLIT || (NP / 2) % 2 == 1, "the parity rule needs NP/2 odd");
+                if (SPLIT && (qs >= 2 || g > 0))
+                    sor_bar_wait(&sbar[qs & 1], gpar ^ (uint32_t)((qs / 2 + 1) & 1));
                 const int t = tbeg + g + qs;
                 // 1. plane t: registers by colour, and publish
 #pragma unroll
@@ -648,6 +664,10 @@ __device__ __forceinline__ void sor_reg_tile(const Layout& L, const float* __res
         }
     }
     __syncthreads();
+    if (SPLIT && threadIdx.x == 0) {  // a persistent block initialises them again for its next tile
+        sor_bar_inval(&sbar[0]);
+        sor_bar_inval(&sbar[1]);
+    }
 }
 
 // Quad form of the register-column kernel: each thread owns four x-adjacent
@@ -878,7 +898,7 @@ __global__ void __launch_bounds__(RegShape<S, TX, TY, PPT>::NT)
 // Persistent batched pass: tile t of the flat SOR tile space belongs to the
 // instance found in the prefix array; pressure goes p[pcur] -> p[pcur^1], z
 // chunk zc[which].
-template <int S, int TX, int TY, int PPT, bool WREG>
+template <int S, int TX, int TY, int PPT, bool WREG, bool SPLIT = false>
 __global__ void __launch_bounds__(RegShape<S, TX, TY, PPT>::NT)
     k_sor_reg_batch(BatchLaunch B, int pcur, int which) {
     for (int t = blockIdx.x; t < B.total; t += gridDim.x) {
@@ -889,19 +909,20 @@ __global__ void __launch_bounds__(RegShape<S, TX, TY, PPT>::NT)
         const int bx = local % tx, r = local / tx;
         const int by = r % ty, bz = r / ty;
         const int z0 = bz * d.zc[which];
-        sor_reg_tile<S, TX, TY, PPT, false, WREG>(d.L, d.p[pcur], d.p[pcur ^ 1], d.div, d.flags, d.kp.omega,
-                                                  d.kp.om1, bx, by, z0, min(z0 + d.zc[which], d.L.D));
+        sor_reg_tile<S, TX, TY, PPT, false, WREG, SPLIT>(d.L, d.p[pcur], d.p[pcur ^ 1], d.div, d.flags,
+                                                         d.kp.omega, d.kp.om1, bx, by, z0,
+                                                         min(z0 + d.zc[which], d.L.D));
     }
 }
 
 // The reversed SOR of the adjoint (ADJ form of the tile): q ping-pongs, acc in place.
-template <int S, int TX, int TY, int PPT>
+template <int S, int TX, int TY, int PPT, bool SPLIT = false>
 __global__ void __launch_bounds__(RegShape<S, TX, TY, PPT>::NT)
     k_sor_reg_adj(Layout L, const float* __restrict__ qin, float* __restrict__ qout, const float* __restrict__ wt,
                   float* __restrict__ acc, float om1, int zc) {
     const int z0 = blockIdx.z * zc;
-    sor_reg_tile<S, TX, TY, PPT, true>(L, qin, qout, wt, nullptr, 0.0f, om1, blockIdx.x, blockIdx.y, z0,
-                                       min(z0 + zc, L.D), acc);
+    sor_reg_tile<S, TX, TY, PPT, true, false, SPLIT>(L, qin, qout, wt, nullptr, 0.0f, om1, blockIdx.x, blockIdx.y,
+                                                     z0, min(z0 + zc, L.D), acc);
 }
 
 // u -= p_R - p_L on live faces; OPEN also updates domain faces with p = 0 outside.
@@ -1139,18 +1160,18 @@ cudaError_t reg_launch(dim3 gr, const Layout& L, const float* pin, float* pout, 
     return cudaGetLastError();
 }
 
-template <int S, int TX, int TY, int PPT, bool WREG>
+template <int S, int TX, int TY, int PPT, bool WREG, bool SPLIT = false>
 cudaError_t reg_launch_batch(int blocks, const BatchLaunch& B, int pcur, int which, cudaStream_t st) {
     using Sh = RegShape<S, TX, TY, PPT>;
-    k_sor_reg_batch<S, TX, TY, PPT, WREG><<<blocks, Sh::NT, Sh::smem, st>>>(B, pcur, which);
+    k_sor_reg_batch<S, TX, TY, PPT, WREG, SPLIT><<<blocks, Sh::NT, Sh::smem, st>>>(B, pcur, which);
     return cudaGetLastError();
 }
 
-template <int S, int TX, int TY, int PPT>
+template <int S, int TX, int TY, int PPT, bool SPLIT = false>
 cudaError_t reg_launch_adj(dim3 gr, const Layout& L, const float* qin, float* qout, const float* wt, float* acc,
                            float om1, int zc, cudaStream_t st) {
     using Sh = RegShape<S, TX, TY, PPT>;
-    k_sor_reg_adj<S, TX, TY, PPT><<<gr, Sh::NT, Sh::smem, st>>>(L, qin, qout, wt, acc, om1, zc);
+    k_sor_reg_adj<S, TX, TY, PPT, SPLIT><<<gr, Sh::NT, Sh::smem, st>>>(L, qin, qout, wt, acc, om1, zc);
     return cudaGetLastError();
 }
 
@@ -1191,10 +1212,10 @@ RbVariant split_variant() {
     RbVariant v = reg_variant<S, TX, TY, PPT, true>();
     v.launch = &split_launch<S, TX, TY, PPT>;
     v.fn = (const void*)k_sor_reg_split<S, TX, TY, PPT>;
-    v.launch_batch = nullptr;
-    v.fn_batch = nullptr;
-    v.launch_adj = nullptr;
-    v.fn_adj = nullptr;
+    v.launch_batch = &reg_launch_batch<S, TX, TY, PPT, true, true>;
+    v.fn_batch = (const void*)k_sor_reg_batch<S, TX, TY, PPT, true, true>;
+    v.launch_adj = &reg_launch_adj<S, TX, TY, PPT, true>;
+    v.fn_adj = (const void*)k_sor_reg_adj<S, TX, TY, PPT, true>;
     return v;
 }
 
