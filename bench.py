@@ -93,17 +93,18 @@ def load_peaks():
 
 
 def profile_traffic(name: str, variant: int):
-    """DRAM bytes per launch of the SOR kernel from the committed ncu summary,
-    when the summary is of the same variant."""
+    """DRAM bytes per launch of the SOR kernel from the committed ncu summary:
+    the `sor_variant: N` / `traffic_bytes_per_launch: X` pair of the variant
+    that ran (None when that variant was not captured)."""
     f = ROOT / "profiles" / f"{name}.md"
     if not f.exists():
         return None
-    text = f.read_text()
-    mv = re.search(r"sor_variant:\s*(-?[0-9]+)", text)
-    if not mv or int(mv.group(1)) != variant:
-        return None
-    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", text)
-    return float(m.group(1)) if m else None
+    pairs = re.findall(r"sor_variant:\s*(-?[0-9]+)\s*\n\s*traffic_bytes_per_launch:\s*([0-9.eE+]+)",
+                       f.read_text())
+    for v, t in pairs:
+        if int(v) == variant:
+            return float(t)
+    return None
 
 
 class ClockSampler:
