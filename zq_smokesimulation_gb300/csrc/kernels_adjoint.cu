@@ -7,7 +7,9 @@
 // Gather where the transpose has a fixed stencil (G^T, div^T, the face
 // averaging, the curl and gradient stencils: no atomics), scatter with FP32
 // atomicAdd where it does not (the transposed trilinear samples of the
-// backtraces).  Discrete decisions of the forward (backtrace breaks, clamps,
+// backtraces: 16-byte atomics into quad accumulators for the velocity, folded
+// onto the faces afterwards by k_adj_fold; scalar atomics for the final
+// scalar samples).  Discrete decisions of the forward (backtrace breaks, clamps,
 // floor cells, a zero-length confinement normal) are held fixed.
 #include <algorithm>
 
