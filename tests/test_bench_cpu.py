@@ -27,3 +27,15 @@ def test_reference_arm_prints_one_contract_line(capsys, monkeypatch):
     cfg = d["config"]
     assert cfg["workload"] == "plain64" and cfg["grid"] == [64, 64, 64]
     assert cfg["sor_iters"] == 200 and cfg["substeps"] == 20
+
+
+def test_sor_traffic_read_per_variant():
+    """The roofline's `traffic` comes from the committed ncu summary of the SOR
+    pass, one `sor_variant` / `traffic_bytes_per_launch` pair per captured
+    variant; a variant that was not captured reports None."""
+    import bench
+    for v in (18, 25, 26):   # the fixed default and the tuner's usual picks at 256^3
+        t = bench.profile_traffic("k_sor_plain256", v)
+        assert t is not None and 1.5e8 < t < 2.5e8, (v, t)
+    assert bench.profile_traffic("k_sor_plain256", 999) is None
+    assert bench.profile_traffic("no_such_profile", 18) is None
