@@ -680,7 +680,7 @@ def run_ours(args):
                        "advection": "inMAC_outMAC + MAC scalar", "sor_depth": depth, "graph": True,
                        "sor_variant": sor_v, "sor_zchunk": sor_zc, "sor_tuned_us_per_iter": sor_us,
                        "sor_kernel": (None if vinfo is None else
-                                      f"{'k_sor_quad' if vinfo.x_cells_per_thread == 4 else 'k_sor_reg/rb'}"
+                                      f"{'k_sor_quad' if vinfo.x_cells_per_thread == 4 else ('k_sor_reg_split' if vinfo.split_barrier else 'k_sor_reg/rb')}"
                                       f"<depth {vinfo.depth}, {vinfo.tile_x}x{vinfo.tile_y}>"),
                        "l2": "working set %.2f GB > 129 MB L2, no flush" % (g.layout().field_elems * 4 * 21.25 / 1e9),
                        "parallelism": "replicas" if world > 1 else "single"},

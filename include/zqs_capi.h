@@ -215,13 +215,15 @@ ZQS_API int zqs_grid_get_sor_choice(zqs_grid* g, int* variant, int* zchunk, floa
  * tile, cell pairs per thread, threads and shared memory per CTA, CTAs that fit
  * on one SM of the current device (0: does not fit), whether the update
  * weights are held in registers, registers per thread, x-adjacent cells per
- * thread (2: the pair forms, 4: the quad form). */
+ * thread (2: the pair forms, 4: the quad form), and how the CTA's threads
+ * synchronise (0: a block barrier every two ring steps, 1: per-step mbarrier
+ * waits that let warps run a step apart). */
 typedef struct zqs_sor_variant {
     int32_t depth, tile_x, tile_y, pairs_per_thread, threads, ctas_per_sm;
     int64_t smem_bytes;
     int32_t weights_in_registers, registers;
     int32_t x_cells_per_thread; /* 2: one red-black pair per row, 4: two x-adjacent pairs */
-    int32_t reserved;
+    int32_t split_barrier;      /* 1: k_sor_reg_split (per-step mbarriers) */
 } zqs_sor_variant;
 ZQS_API int zqs_sor_variant_count(void);
 ZQS_API int zqs_sor_variant_info(int index, zqs_sor_variant* out);

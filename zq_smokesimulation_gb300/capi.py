@@ -124,7 +124,7 @@ class SorVariant(C.Structure):
     _fields_ = [("depth", C.c_int32), ("tile_x", C.c_int32), ("tile_y", C.c_int32),
                 ("pairs_per_thread", C.c_int32), ("threads", C.c_int32), ("ctas_per_sm", C.c_int32),
                 ("smem_bytes", C.c_int64), ("weights_in_registers", C.c_int32), ("registers", C.c_int32),
-                ("x_cells_per_thread", C.c_int32), ("reserved", C.c_int32)]
+                ("x_cells_per_thread", C.c_int32), ("split_barrier", C.c_int32)]
 
 
 class AdjointInfo(C.Structure):

@@ -1118,6 +1118,7 @@ struct RbVariant {
     int wreg;       // update weights in registers (k_sor_reg WREG form)
     int regs;       // registers per thread of fn
     int xcells = 2; // x-adjacent cells per thread (2: a red-black pair, 4: the quad form)
+    int split = 0;  // 1: per-step mbarrier waits (k_sor_reg_split)
 };
 
 template <int S, int TX, int TY, int PPT>
@@ -1216,6 +1217,7 @@ RbVariant split_variant() {
     v.fn_batch = (const void*)k_sor_reg_batch<S, TX, TY, PPT, true, true>;
     v.launch_adj = &reg_launch_adj<S, TX, TY, PPT, true>;
     v.fn_adj = (const void*)k_sor_reg_adj<S, TX, TY, PPT, true>;
+    v.split = 1;
     return v;
 }
 
@@ -1426,7 +1428,7 @@ int sor_variant_info(int i, zqs_sor_variant* out) {
     out->weights_in_registers = v.wreg;
     out->registers = v.regs;
     out->x_cells_per_thread = v.xcells;
-    out->reserved = 0;
+    out->split_barrier = v.split;
     return ZQS_OK;
 }
 
